@@ -1,0 +1,251 @@
+/*
+ * ref_harness.c -- drives the reference's own hot-path functions (compiled unmodified from
+ * the reference sources against ref_shim/) in the order src/mitos.c:205-422,794-863 and
+ * analyse/src/mitos_read.c:278-419 call them, so the oracle restatement can be pinned
+ * against the reference code.  TEST INFRASTRUCTURE ONLY; built into oracle/_ref/.
+ *
+ * The CIC deposit and the overdensity exist in the reference only inside main()
+ * (analyse/src/mitos_read.c:278-376); for those two steps this harness calls the oracle's
+ * line-by-line restatement.  Linear P(k) shells are an extension with no reference code.
+ */
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include "mitos.h"
+#include "../../oracle/mitos_oracle.h"
+
+/* one external definition of the C99 inline sinc of include/fft_kernels.h:187 */
+extern inline double sinc(double x);
+
+void ref_draws(uint64_t seed, int64_t n, uint64_t *out) {
+    rng_state s = rand_uint64_init(seed);
+    for (int64_t i = 0; i < n; i++) out[i] = rand_uint64(&s);
+}
+
+void ref_norms(uint64_t seed, int64_t n, double *out) {
+    rng_state s = rand_uint64_init(seed);
+    for (int64_t i = 0; i < n; i++) out[i] = sampleNorm(&s);
+}
+
+/* generate_complex_grf + enforce_hermiticity, src/mitos.c:216-221 */
+int ref_grf(int N, double boxlen, uint64_t seed, int hermitian, double *out) {
+    struct distributed_grid grf;
+    alloc_local_grid(&grf, N, boxlen, MPI_COMM_WORLD);
+    rng_state s = rand_uint64_init(seed);
+    generate_complex_grf(&grf, &s);
+    if (hermitian) enforce_hermiticity(&grf);
+    memcpy(out, grf.fbox, sizeof(fftw_complex) * grf.local_size);
+    free_local_grid(&grf);
+    return 0;
+}
+
+/* one r2c or c2r of a padded grid through fft_r2c_dg / fft_c2r_dg */
+int ref_fft_dg(int N, double boxlen, int to_momentum, double *real_padded, double *complex_half) {
+    struct distributed_grid g;
+    alloc_local_grid(&g, N, boxlen, MPI_COMM_WORLD);
+    size_t n = sizeof(fftw_complex) * g.local_size;
+    if (to_momentum) {
+        memcpy(g.box, real_padded, n);
+        fft_r2c_dg(&g);
+        memcpy(complex_half, g.fbox, n);
+    } else {
+        memcpy(g.fbox, complex_half, n);
+        g.momentum_space = 1;
+        fft_c2r_dg(&g);
+        memcpy(real_padded, g.box, n);
+    }
+    free_local_grid(&g);
+    return 0;
+}
+
+static char *g_titles[64];
+
+int ref_ic_pipeline(int N, int M, double L, uint64_t seed, double A_s, double n_s, double k_pivot,
+                    int k_size, int tau_size, int n_functions, const double *kv,
+                    const double *log_tau, const double *redshift, const double *Dg,
+                    const double *fg, const double *Hh, const double *delta, int index_src,
+                    double z_ini, int lpt_order, int ma_cycles, int pk_bins, int pk_linear,
+                    double mass, double *out_grf, double *out_delta_k, double *out_phi_k,
+                    double *out_d0, double *out_d1, double *out_d2, float *out_pos,
+                    double *out_rho, double *pk_k, double *pk_p, long *pk_obs) {
+    if (n_functions > 64) return 1;
+    for (int i = 0; i < n_functions; i++) {
+        if (!g_titles[i]) {
+            g_titles[i] = malloc(16);
+            snprintf(g_titles[i], 16, "f%d", i);
+        }
+    }
+    struct perturb_data ptdat;
+    memset(&ptdat, 0, sizeof ptdat);
+    ptdat.k_size = k_size;
+    ptdat.tau_size = tau_size;
+    ptdat.n_functions = n_functions;
+    ptdat.delta = (double *)delta;
+    ptdat.k = (double *)kv;
+    ptdat.log_tau = (double *)log_tau;
+    ptdat.redshift = (double *)redshift;
+    ptdat.D_growth = (double *)Dg;
+    ptdat.f_growth = (double *)fg;
+    ptdat.H_Hubble = (double *)Hh;
+    ptdat.titles = g_titles;
+    struct perturb_spline spline;
+    initPerturbSpline(&spline, DEFAULT_K_ACC_TABLE_SIZE, &ptdat);
+
+    struct cosmology cosmo;
+    memset(&cosmo, 0, sizeof cosmo);
+    cosmo.A_s = A_s;
+    cosmo.n_s = n_s;
+    cosmo.k_pivot = k_pivot;
+    cosmo.z_ini = z_ini;
+    cosmo.z_source = z_ini;
+
+    /* src/mitos.c:148-177 */
+    rng_state seed_state = rand_uint64_init(seed + 0);
+    cosmo.log_tau_ini = perturbLogTauAtRedshift(&spline, cosmo.z_ini);
+    cosmo.log_tau_source = perturbLogTauAtRedshift(&spline, cosmo.z_source);
+    const double D_source = perturbGrowthFactorAtLogTau(&spline, cosmo.log_tau_source);
+    const double D_ini = perturbGrowthFactorAtLogTau(&spline, cosmo.log_tau_ini);
+
+    /* :206-227 */
+    struct distributed_grid grf;
+    alloc_local_grid(&grf, N, L, MPI_COMM_WORLD);
+    generate_complex_grf(&grf, &seed_state);
+    enforce_hermiticity(&grf);
+    fft_apply_kernel_dg(&grf, &grf, kernel_power_no_transfer, &cosmo);
+    const size_t cb = sizeof(fftw_complex) * grf.local_size;
+    if (out_grf) memcpy(out_grf, grf.fbox, cb);
+    fft_c2r_dg(&grf);
+    /* :300 */
+    fft_r2c_dg(&grf);
+
+    /* :308-317 */
+    struct distributed_grid grid, potential, derivative;
+    alloc_local_grid(&grid, N, L, MPI_COMM_WORLD);
+    alloc_local_grid(&potential, N, L, MPI_COMM_WORLD);
+    alloc_local_grid(&derivative, N, L, MPI_COMM_WORLD);
+
+    /* :356-377 */
+    double rescale_factor = (cosmo.z_ini != cosmo.z_source) ? D_ini / D_source : 1.0;
+    char title[16];
+    snprintf(title, sizeof title, "f%d", index_src);
+    int err = generatePerturbationGrid(&cosmo, &spline, &grf, &grid, title, "", rescale_factor);
+    if (err) return err;
+    if (out_delta_k) {
+        /* the transfer-function product before the c2r; recompute it the same way */
+        struct distributed_grid tmp;
+        alloc_local_grid(&tmp, N, L, MPI_COMM_WORLD);
+        int tau_index; double u_tau;
+        perturbSplineFindTau(&spline, cosmo.log_tau_source, &tau_index, &u_tau);
+        struct spline_params sp = {&spline, index_src, tau_index, u_tau};
+        fft_apply_kernel_dg(&tmp, &grf, kernel_transfer_function, &sp);
+        memcpy(out_delta_k, tmp.fbox, cb);
+        free_local_grid(&tmp);
+    }
+    fft_r2c_dg(&grid);
+
+    /* :380-389 */
+    if (ma_cycles > 0) err = solveMongeAmpere(&potential, &grid, &derivative, ma_cycles);
+    else if (lpt_order == 2) err = solve2LPT(&potential, &grid, &derivative, 1.0, -3. / 7.);
+    else fft_apply_kernel_dg(&potential, &grid, kernel_inv_poisson, NULL);
+    if (err) return err;
+    if (out_phi_k) memcpy(out_phi_k, potential.fbox, cb);
+
+    /* :395-416 */
+    struct Hermite_kern_params Hkp;
+    Hkp.order = 3;
+    Hkp.N = N;
+    Hkp.boxlen = L;
+    fft_apply_kernel_dg(&potential, &potential, kernel_undo_Hermite_window, &Hkp);
+    const kernel_func derivative_kernels[] = {kernel_dx, kernel_dy, kernel_dz};
+    double *disp[3];
+    double *outs[3] = {out_d0, out_d1, out_d2};
+    for (int i = 0; i < 3; i++) {
+        fft_apply_kernel_dg(&derivative, &potential, derivative_kernels[i], NULL);
+        fft_c2r_dg(&derivative);
+        disp[i] = malloc(cb);
+        memcpy(disp[i], derivative.box, cb);
+        if (outs[i]) memcpy(outs[i], derivative.box, cb);
+    }
+    fft_c2r_dg(&potential);
+    free_local_grid(&grf);
+    free_local_grid(&grid);
+    free_local_grid(&potential);
+    free_local_grid(&derivative);
+
+    /* :772-863 particle lattice and TSC displacement (one rank) */
+    struct params pars;
+    memset(&pars, 0, sizeof pars);
+    pars.BoxLen = L;
+    struct particle_type ptype;
+    memset(&ptype, 0, sizeof ptype);
+    ptype.TotalNumber = (long long)M * M * M;
+    ptype.CubeRootNumber = M;
+    ptype.Mass = mass;
+    long long chunk_size = (long long)M * M * M;
+    struct particle *parts = malloc(chunk_size * sizeof(struct particle));
+    genParticlesFromGrid_local(&parts, &pars, NULL, &cosmo, &ptype, M, 0, 0, 0);
+    for (int dir = 0; dir < 3; dir++) {
+        struct left_right_slice lrs;
+        lrs.local_slice = disp[dir];
+        lrs.local_NX = N;
+        lrs.local_X0 = 0;
+        lrs.left_slice = disp[dir];
+        lrs.left_NX = 0;
+        lrs.left_X0 = 0;
+        lrs.right_slice = disp[dir];
+        lrs.right_NX = 0;
+        lrs.right_X0 = 0;
+#pragma omp parallel for
+        for (long long i = 0; i < chunk_size; i++) {
+            double x = parts[i].X;
+            double y = parts[i].Y;
+            double z = parts[i].Z;
+            double d = gridTSC_dg(&lrs, x, y, z, L, N);
+            if (dir == 0) parts[i].X -= d;
+            else if (dir == 1) parts[i].Y -= d;
+            else parts[i].Z -= d;
+        }
+    }
+    /* :1072-1077 */
+    for (long long i = 0; i < chunk_size; i++) {
+        parts[i].X = fwrap(parts[i].X, L);
+        parts[i].Y = fwrap(parts[i].Y, L);
+        parts[i].Z = fwrap(parts[i].Z, L);
+    }
+    for (int i = 0; i < 3; i++) free(disp[i]);
+    float *pos = malloc(sizeof(float) * 3 * chunk_size);
+    for (long long i = 0; i < chunk_size; i++) {
+        pos[3 * i] = parts[i].X;
+        pos[3 * i + 1] = parts[i].Y;
+        pos[3 * i + 2] = parts[i].Z;
+    }
+    float pmass = parts[0].mass;
+    free(parts);
+    if (out_pos) memcpy(out_pos, pos, sizeof(float) * 3 * chunk_size);
+
+    /* analyse/src/mitos_read.c:278-419 */
+    double *box = calloc((size_t)N * N * N, sizeof(double));
+    double total_mass = orc_cic_deposit(chunk_size, pos, (double)pmass, N, L, box);
+    free(pos);
+    orc_overdensity(N, L, total_mass, box);
+    if (out_rho) memcpy(out_rho, box, sizeof(double) * N * N * N);
+    fftw_complex *fbox = fftw_malloc((size_t)N * N * (N / 2 + 1) * sizeof(fftw_complex));
+    fftw_plan r2c = fftw_plan_dft_r2c_3d(N, N, N, box, fbox, FFTW_ESTIMATE);
+    fft_execute(r2c);
+    fft_normalize_r2c(fbox, N, L);
+    undoCICWindow(fbox, N, L);
+    if (pk_linear) {
+        orc_powerspec_lin(N, L, (double *)fbox, (double *)fbox, pk_bins, pk_k, pk_p, pk_obs);
+    } else {
+        int *obs = calloc(pk_bins, sizeof(int));
+        calc_cross_powerspec(N, L, fbox, fbox, pk_bins, pk_k, pk_p, obs);
+        for (int i = 0; i < pk_bins; i++) pk_obs[i] = obs[i];
+        free(obs);
+    }
+    fftw_destroy_plan(r2c);
+    fftw_free(fbox);
+    free(box);
+    cleanPerturbSpline(&spline);
+    return 0;
+}
