@@ -1,0 +1,306 @@
+#!/usr/bin/env python3
+"""Initial-condition throughput on GB300: 512^3 grid, 512^3 particles, box 1000 Mpc/h, FP32.
+
+One step = one full initial condition through the C ABI (ic_pipeline_run): xoshiro256** white
+noise -> primordial power x BBKS transfer -> 2LPT potential (six Hessians, second-order
+source, Poisson) -> TSC window undo -> three displacement grids -> lattice displacement (TSC
+gather) + wrap -> CIC -> overdensity r2c -> CIC window undo -> P(k) in 128 linear shells.
+
+  value  ICs/s with the transfer table on the host and all grids in HBM (device-timed,
+         CUDA events on the library stream); every grid is 0.54 GB, larger than L2.
+  e2e    the same call with the particle positions (512^3 x 3 floats) copied to pinned host
+         memory every step, plus the table upload and the P(k) read.
+  --impl reference   the reference algorithm restated in C (oracle/, OpenMP, FP64) on the
+         host cores: one 256^3 IC per step, scaled by the cell count (x8) to 512^3 ICs.
+
+N > 1 GPUs run independent replicas (different seeds): the IC does not shard.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "512^3 2LPT initial-condition throughput (noise->2LPT->displacements->CIC->P(k))"
+UNIT = "IC/s"
+
+
+def algorithmic_bytes(name: str, G: float) -> float:
+    """minimum bytes a launch of each kernel must move, in units of one complex grid G"""
+    table = {"noise": 1, "x_hess": 4, "y_hess": 9, "z_hess_2lpt": 7, "z_hess_ma": 8, "z_r2c": 2,
+             "y_plain": 2, "x_plain": 2, "x_combine": 3, "x_add_poisson": 3, "x_disp": 3,
+             "y_disp": 5, "z_disp": 6, "displace_cic": 4, "x_pk": 1, "z_c2r": 2}
+    return table.get(name, 0) * G
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region"""
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        load = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(load), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peak_hbm():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        return float(json.load(open(p))["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel: str, N: int):
+    """DRAM bytes per launch of a kernel from the committed ncu summary (scaled to N)"""
+    p = os.path.join(HERE, "profiles", "ncu_traffic.json")
+    if not os.path.exists(p):
+        return None
+    d = json.load(open(p))
+    e = d.get(kernel)
+    if not e:
+        return None
+    return e["dram_bytes"] * (N / e["N"]) ** 3
+
+
+def cpu_baseline(args, table, steps=1):
+    """the oracle (reference algorithm in C, FP64, all host threads) on one 256^3 IC per step"""
+    import oracle
+    Ns = 256
+    Ls = args.boxlen * Ns / args.N
+    prm = oracle.ic_params(Ns, Ns, Ls, args.seed, table, pk_bins=args.bins // 2, pk_linear=True)
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        oracle.ic_pipeline(prm)
+        times.append(time.perf_counter() - t0)
+    scale = (args.N / Ns) ** 3
+    sec_per_ic = statistics.median(times) * scale
+    return {"value": 1.0 / sec_per_ic, "unit": UNIT, "cores": oracle.lib().orc_num_threads(),
+            "kind": "port",
+            "sample": f"one {Ns}^3 IC (L = {Ls:g}) per step, {statistics.median(times):.2f} s, "
+                      f"scaled x{scale:g} by cell count to a {args.N}^3 IC"}, times
+
+
+def run_reference(args):
+    ws, rank, _ = dist_setup()
+    if rank != 0:
+        return 0
+    from mitos_gb300.perturb import load_table
+    table = load_table()
+    for _ in range(args.warmup):
+        pass  # the CPU port has no warm-up state; warm-up steps would only repeat the work
+    base, times = cpu_baseline(args, table, steps=args.steps)
+    total = sum(times) * (args.N / 256) ** 3
+    line = {"impl": "reference", "metric": METRIC, "value": base["value"], "unit": UNIT,
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 / base["value"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (xoshiro noise, BBKS table)",
+            "config": config(args), "cpu_baseline": base,
+            "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def config(args):
+    return {"workload": f"{args.N}^3 grid, {args.N}^3 particles, box {args.boxlen:g} Mpc/h, z=31, 2LPT, "
+                        f"CIC, P(k) {args.bins} linear shells",
+            "N": args.N, "M": args.N, "boxlen": args.boxlen, "precision": args.precision,
+            "pk_bins": args.bins, "parallelism": "replicas (independent seeds per GPU)",
+            "l2": "inputs larger than L2 (each grid 0.54 GB)", "cuda_graph": False}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--N", type=int, default=512)
+    ap.add_argument("--boxlen", type=float, default=1000.0)
+    ap.add_argument("--bins", type=int, default=128)
+    ap.add_argument("--seed", type=int, default=42)
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    ws, rank, local = dist_setup()
+    dist = None
+    if ws > 1:
+        import torch
+        import torch.distributed as td
+        torch.cuda.set_device(local)
+        td.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        dist = td
+
+    import mitos_gb300.lib as ml
+    from mitos_gb300.perturb import load_table
+    table = load_table()
+    spline = ml.Spline(table)
+    prec = ml.FP32 if args.precision == "fp32" else ml.FP64
+    N = args.N
+    seed0 = args.seed + 1000 * rank
+
+    def cfg(step):
+        return ml.ic_config(N, N, args.boxlen, seed0 + step, table, method=ml.METHOD_2LPT,
+                            pk_bins=args.bins, pk_linear=True, precision=prec)
+
+    L = ml.load()
+    bins = args.bins
+    kb, pb, ob = np.zeros(bins), np.zeros(bins), np.zeros(bins, np.int64)
+    res = ml.ICResult(kb.ctypes.data_as(ml._dp), pb.ctypes.data_as(ml._dp), ob.ctypes.data_as(ml._lp),
+                      None, 0, 0.0)
+
+    def step(i, with_pos=None):
+        c = cfg(i)
+        res.pos = with_pos
+        ml._check(L.ic_pipeline_run(ctypes.byref(c), ctypes.byref(spline.sp), ctypes.byref(res)))
+
+    def barrier():
+        L.mitos_sync()
+        if dist:
+            dist.barrier()
+
+    for i in range(args.warmup):
+        step(i)
+    launches0 = ml.launch_count()
+    clocks = Clocks(local)
+    barrier()
+    clocks.start()
+    ml.timer_start()
+    for i in range(args.steps):
+        step(args.warmup + i)
+    ms = ml.timer_stop()
+    barrier()
+    clk = clocks.stop()
+    launches = (ml.launch_count() - launches0) // args.steps
+    if dist:
+        import torch
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = ws * args.steps / (ms / 1e3)
+
+    # e2e: positions to pinned host memory every step (the IC product), table up, P(k) down
+    import torch
+    npart = N ** 3
+    pinned = torch.empty((npart, 3), dtype=torch.float32, pin_memory=True) if torch.cuda.is_available() else None
+    pos_ptr = ctypes.cast(pinned.data_ptr(), ml._fp) if pinned is not None else None
+    step(0, pos_ptr)
+    barrier()
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        step(args.warmup + i, pos_ptr)
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    e2e_val = ws * args.steps / e2e_s
+
+    # per-kernel durations of one IC (roofline of the dominant kernel)
+    ml.kernel_timing(True)
+    step(0)
+    kt = ml.kernel_times()
+    ml.kernel_timing(False)
+    G = N * N * (N // 2 + 1) * (8 if prec == ml.FP32 else 16)
+    agg = {}
+    for name, t in kt:
+        a = agg.setdefault(name, [0.0, 0])
+        a[0] += t
+        a[1] += 1
+    dom = max(agg, key=lambda k: agg[k][0])
+    dom_ms = agg[dom][0] / agg[dom][1]
+    peak, peak_kind = peak_hbm()
+    achieved = algorithmic_bytes(dom, G) / (dom_ms / 1e3) / 1e9
+    traffic = ncu_traffic(dom, N)
+    kernels = {k: {"ms": round(v[0] / v[1], 4), "launches": v[1],
+                   "GBps": round(algorithmic_bytes(k, G) / (v[0] / v[1] / 1e3) / 1e9, 1) if algorithmic_bytes(k, G) else None}
+               for k, v in sorted(agg.items(), key=lambda kv: -kv[1][0])}
+    alg_ic = 37 * G  # survey byte model per IC with two-pass FFTs, (15 + 22 (P - 1)) G
+    if rank != 0:
+        return 0
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if prec == ml.FP32 else "f64",
+            "data": "synthetic (xoshiro256** white noise, BBKS transfer table)", "config": config(args),
+            "gpu_launches": int(launches),
+            "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 3 * table.k_size * 8,
+                    "d2h_bytes_per_step": npart * 12 + 3 * bins * 8},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                         "traffic": traffic, "algorithmic_bytes": algorithmic_bytes(dom, G),
+                         "ms": dom_ms},
+            "ic_hbm": {"model_bytes": alg_ic, "GBps": alg_ic / (ms_per_step / 1e3) / 1e9,
+                       "frac": alg_ic / (ms_per_step / 1e3) / 1e9 / peak},
+            "kernels": kernels, "clocks": clk}
+    if not args.no_cpu_baseline:
+        base, _ = cpu_baseline(args, table, steps=1)
+        line["cpu_baseline"] = base
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

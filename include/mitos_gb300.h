@@ -1,0 +1,282 @@
+/*
+ * mitos_gb300.h -- C ABI of the GB300 (sm_103a) initial-condition library.
+ *
+ * The library replaces the FFTW-MPI hot path of Mitos (wullm/mitos) on one GPU.  It exports
+ * the reference's own entry points with the reference's signatures, so the reference driver
+ * (src/mitos.c) and analysis code (analyse/src/mitos_read.c) call it unchanged once they are
+ * compiled against this header instead of the reference headers named beside each item.
+ * A few entry points are new; each says so.
+ *
+ * Differences from the reference, all deliberate:
+ *   - struct distributed_grid keeps the reference fields in the reference order and appends
+ *     private fields; fbox and box are DEVICE pointers (use dg_copy_to_host/_from_host).
+ *   - A grid is FP64 (complex128 / double, as the reference) or FP32 (complex64 / float);
+ *     alloc_local_grid uses the precision set by mitos_set_precision (default FP64).
+ *   - One rank: NX = N, X0 = 0.  MPI_Comm is kept as an opaque pointer-sized type.
+ *   - Functions return an int status instead of exiting: 0 ok, 1 shape mismatch, 2 not in
+ *     momentum space, 3 unsupported kernel callback or size, 4 CUDA error, 5 out of memory,
+ *     6 bounded wait timed out, 7 no convergence.  mitos_last_error() describes the last one.
+ *   - Every entry point is synchronous on return (its work on the library stream is done).
+ */
+#ifndef MITOS_GB300_H
+#define MITOS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- types kept from the reference headers ------------------------------------------- */
+#if !defined(MPI_VERSION) && !defined(ORC_SHIM_MPI_H)
+typedef struct mitos_comm_opaque *MPI_Comm; /* pointer-sized, as OpenMPI's MPI_Comm */
+#define MPI_COMM_WORLD ((MPI_Comm)0)
+#endif
+
+#if defined(FFTW3_H)
+typedef fftw_complex mitos_c128;
+typedef fftwf_complex mitos_c64;
+#else
+typedef double mitos_c128[2]; /* layout of fftw_complex */
+typedef float mitos_c64[2];   /* layout of fftwf_complex */
+#endif
+
+#define MITOS_FP64 0
+#define MITOS_FP32 1
+
+/* include/distributed_grid.h:29-60, fields in the reference order, private fields appended */
+struct distributed_grid {
+    int N;
+    double boxlen;
+    MPI_Comm comm;
+    char momentum_space;
+    long int NX;
+    long int X0;
+    long int local_size; /* complex elements: NX * N * (N/2 + 1) */
+    mitos_c128 *fbox;    /* device; complex64 storage when precision == MITOS_FP32 */
+    double *box;         /* device; float storage when precision == MITOS_FP32, padded to N+2 */
+    /* ---- appended (not in the reference) ---- */
+    int precision;
+    int flags;
+    void *priv;
+};
+
+/* include/random_xorshift.h:11-13 + include/random.h:25 */
+struct xoshiro256ss_state {
+    uint64_t s[4];
+};
+typedef struct xoshiro256ss_state rng_state;
+
+/* include/fft.h:31-39 */
+struct kernel {
+    double kx, ky, kz;
+    double k;
+    double kern[2]; /* double complex in the reference; same layout */
+    const void *params;
+};
+
+/* include/input.h:127-141 */
+struct cosmology {
+    double h;
+    double n_s;
+    double A_s;
+    double k_pivot;
+    double z_ini;
+    double log_tau_ini;
+    double rho_crit;
+    double z_source;
+    double log_tau_source;
+};
+
+/* include/perturb_data.h:28-53 */
+struct perturb_data {
+    int k_size;
+    int tau_size;
+    int n_functions;
+    double *delta; /* [n_functions][tau_size][k_size] */
+    double *k;
+    double *log_tau;
+    double *redshift;
+    double *D_growth;
+    double *f_growth;
+    double *H_Hubble;
+    char **titles;
+    double *Omega;
+};
+
+/* include/perturb_spline.h:27-36 */
+struct perturb_spline {
+    const struct perturb_data *ptdat;
+    double *k_acc_table;
+    int k_acc_table_size;
+};
+
+/* include/fft_kernels.h:123-128 */
+struct spline_params {
+    const struct perturb_spline *spline;
+    int index_src;
+    int tau_index;
+    double u_tau;
+};
+
+/* include/fft_kernels.h:189-193 */
+struct Hermite_kern_params {
+    int order;
+    int N;
+    double boxlen;
+};
+
+/* ---- grids: replaces src/distributed_grid.c (include/distributed_grid.h:74-77) -------- */
+int alloc_local_grid(struct distributed_grid *dg, int N, double boxlen, MPI_Comm comm);
+int free_local_grid(struct distributed_grid *dg);
+int free_local_real_grid(struct distributed_grid *dg);
+int free_local_complex_grid(struct distributed_grid *dg);
+
+/* ---- FFT + k-space kernels: replaces src/fft.c:29-35,219-302 (include/fft.h:92-116) --- */
+void fft_wavevector(int x, int y, int z, int N, double delta_k, double *kx, double *ky,
+                    double *kz, double *k);
+int fft_r2c_dg(struct distributed_grid *dg);
+int fft_c2r_dg(struct distributed_grid *dg);
+int fft_apply_kernel_dg(struct distributed_grid *dg_write, const struct distributed_grid *dg_read,
+                        void (*compute)(struct kernel *the_kernel), const void *params);
+
+/* Kernel callbacks of include/fft_kernels.h:28-219.  The reference defines them static inline
+ * in a header, so their addresses differ per translation unit; here they are defined once in
+ * the library (host functions with the reference arithmetic) and fft_apply_kernel_dg
+ * recognises them by address.  Any other callback returns status 3 (there is no CPU path). */
+void kernel_constant(struct kernel *the_kernel);
+void kernel_lowpass(struct kernel *the_kernel);
+void kernel_hipass(struct kernel *the_kernel);
+void kernel_tophat(struct kernel *the_kernel);
+void kernel_elliptic_tophat(struct kernel *the_kernel);
+void kernel_translate(struct kernel *the_kernel);
+void kernel_gaussian(struct kernel *the_kernel);
+void kernel_gaussian_inv(struct kernel *the_kernel);
+void kernel_inv_poisson(struct kernel *the_kernel);
+void kernel_dx(struct kernel *the_kernel);
+void kernel_dy(struct kernel *the_kernel);
+void kernel_dz(struct kernel *the_kernel);
+void kernel_power_no_transfer(struct kernel *the_kernel);
+void kernel_transfer_function(struct kernel *the_kernel);
+void kernel_inv_transfer_function(struct kernel *the_kernel);
+void kernel_undo_Hermite_window(struct kernel *the_kernel);
+
+/* ---- white noise: replaces src/grf.c:26-175 (include/grf.h:30-31) --------------------- */
+/* Advances *state past every draw, as the sequential reference does. */
+int generate_complex_grf(struct distributed_grid *dg, rng_state *state);
+int enforce_hermiticity(struct distributed_grid *dg);
+
+/* ---- perturbation grid, Poisson, 2LPT, Monge-Ampere ----------------------------------- */
+/* src/generate_grids.c:28-67 (include/generate_grids.h:29-34).  fname is not written: field
+ * files are host I/O outside this library; copy the grid out with dg_copy_to_host. */
+int generatePerturbationGrid(const struct cosmology *cosmo, const struct perturb_spline *spline,
+                             struct distributed_grid *grf, struct distributed_grid *grid,
+                             const char *transfer_func_title, const char *fname,
+                             const double rescale_factor);
+/* src/poisson.c:58-70 (include/poisson.h:30) */
+int solvePoisson_dg(struct distributed_grid *dg);
+/* src/2lpt.c:38-143 (include/2lpt.h:27-29) */
+int solve2LPT(struct distributed_grid *potential, struct distributed_grid *density,
+              struct distributed_grid *workspace, double factor1, double factor2);
+/* src/monge_ampere.c:50-183 (include/monge_ampere.h:27-29) */
+int solveMongeAmpere(struct distributed_grid *potential, struct distributed_grid *density,
+                     struct distributed_grid *workspace, int cycles);
+
+/* ---- power spectra: replaces src/calc_powerspec.c:32-217 (include/calc_powerspec.h:26-36) */
+/* box1/box2 may be host or device pointers; bins are host arrays. */
+void calc_cross_powerspec(int N, double boxlen, const mitos_c128 *box1, const mitos_c128 *box2,
+                          int bins, double *k_in_bins, double *power_in_bins, int *obs_in_bins);
+void calc_cross_powerspec_float(int N, double boxlen, const mitos_c64 *box1,
+                                const mitos_c64 *box2, int bins, double *k_in_bins,
+                                double *power_in_bins, int *obs_in_bins);
+void calc_cross_powerspec_float_mpi(long int N, long int X0, long int NX, double boxlen,
+                                    const mitos_c64 *box1, const mitos_c64 *box2, int bins,
+                                    double *k_in_bins, double *power_in_bins,
+                                    long int *obs_in_bins);
+
+/* ==== entry points with no reference counterpart ====================================== */
+
+/* Precision used by alloc_local_grid (MITOS_FP64 by default). */
+int mitos_set_precision(int precision);
+int mitos_get_precision(void);
+int alloc_local_grid_prec(struct distributed_grid *dg, int N, double boxlen, MPI_Comm comm,
+                          int precision);
+
+/* Copy a grid between host and device.  which = 0: fbox (N*N*(N/2+1) complex),
+ * which = 1: box (N*N*(N+2) reals).  Element type follows dg->precision. */
+int dg_copy_to_host(const struct distributed_grid *dg, int which, void *host);
+int dg_copy_from_host(struct distributed_grid *dg, int which, const void *host);
+
+/* Description of the last failure (empty when none), and the number of kernels launched. */
+const char *mitos_last_error(void);
+long mitos_launch_count(void);
+/* Release every cached plan, table and workspace. */
+int mitos_release_all(void);
+/* Timing on the library stream: CUDA events around everything launched in between. */
+int mitos_timer_start(void);
+double mitos_timer_stop(void);
+int mitos_sync(void);
+/* Per-launch timing (off by default): on = 1 clears and starts recording; mitos_kernel_times
+ * returns up to max (name, milliseconds) pairs of the launches since. */
+int mitos_kernel_timing(int on);
+int mitos_kernel_times(const char **names, double *ms, int max);
+/* Stage times (ms) of the last ic_pipeline_run made with MITOS_PROFILE set in the environment. */
+int mitos_stage_times(double *ms, int max);
+/* Per-cycle reference eps and relative rms residual of the last solveMongeAmpere. */
+int mitos_ma_history(double *eps, double *rel, int max);
+/* Host-only helpers (no GPU work): the xoshiro256** state n draws after s (jump-ahead), and
+ * the start state of noise column c of an N grid. */
+int mitos_rng_jump(uint64_t s[4], unsigned long long n);
+int mitos_noise_column_state(int N, long c, const uint64_t s0[4], uint64_t out[4]);
+
+/* CIC mass assignment of n particles (float x,y,z triples, host or device pointer) onto the
+ * real part of rho (padded layout), accumulated on top of its contents:
+ * analyse/src/mitos_read.c:278-334 as a library call.  Returns the summed mass in *total. */
+int cic_deposit_dg(struct distributed_grid *rho, const float *pos, long n, double mass,
+                   double *total_mass);
+
+/* Fused initial-condition pipeline on the device: white noise -> primordial power and
+ * transfer function -> Zel'dovich / 2LPT / Monge-Ampere potential -> TSC window undo ->
+ * displacement grids -> lattice displacement (TSC gather) -> CIC -> overdensity -> r2c ->
+ * CIC window undo -> P(k).  Follows src/mitos.c:205-422,794-863,1072-1077 and
+ * analyse/src/mitos_read.c:278-419 with z_source = z_ini. */
+#define MITOS_METHOD_ZELDOVICH 1
+#define MITOS_METHOD_2LPT 2
+#define MITOS_METHOD_MONGE_AMPERE 3
+struct ic_config {
+    int N;              /* grid size */
+    int M;              /* cube root of the particle number */
+    double boxlen;
+    uint64_t seed;      /* Seed (+ rank 0), src/mitos.c:148 */
+    double A_s, n_s, k_pivot;
+    double z_ini;
+    int index_src;      /* transfer function index (findTitle of the density title) */
+    int method;
+    int ma_cycles;      /* Monge-Ampere: maximum cycles */
+    double ma_tol;      /* Monge-Ampere: stop when sqrt(sum res^2 / sum rho^2) <= ma_tol (0: run all cycles) */
+    int pk_bins;
+    int pk_linear;      /* 1: linear shells to k_Nyquist; 0: the reference log bins */
+    int precision;      /* MITOS_FP32 or MITOS_FP64 */
+    int keep_outputs;   /* 1: keep the displacement grids, positions and density on the device */
+};
+struct ic_result {
+    double *pk_k;       /* host [pk_bins] */
+    double *pk_p;       /* host [pk_bins] */
+    long *pk_obs;       /* host [pk_bins] */
+    float *pos;         /* optional host [M^3 * 3]: positions after the wrap */
+    int ma_iterations;  /* Monge-Ampere cycles run */
+    double ma_residual; /* last sqrt(sum res^2 / sum rho^2) */
+};
+int ic_pipeline_run(const struct ic_config *cfg, const struct perturb_spline *spline,
+                    struct ic_result *res);
+/* The same on caller-provided host table arrays (convenience for bindings without structs). */
+int ic_pipeline_run_table(const struct ic_config *cfg, int k_size, int tau_size,
+                          int n_functions, const double *k, const double *log_tau,
+                          const double *redshift, const double *D_growth, const double *delta,
+                          struct ic_result *res);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MITOS_GB300_H */

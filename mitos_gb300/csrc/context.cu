@@ -1,0 +1,302 @@
+// context.cu -- error state, the library stream, cached per-size geometry (FFT plans, twiddle,
+// window and bin tables) and the device workspace.
+#include <math.h>
+#include <stdarg.h>
+#include <string.h>
+
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <vector>
+
+#include "context.cuh"
+
+namespace mitos {
+
+static char g_err[512];
+static std::mutex g_mu;
+static cudaStream_t g_stream = nullptr;
+static long g_launches = 0;
+
+void set_error(int code, const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    int n = snprintf(g_err, sizeof g_err, "[%d] ", code);
+    vsnprintf(g_err + n, sizeof g_err - n, fmt, ap);
+    va_end(ap);
+}
+
+int check_cuda(cudaError_t e, const char *what) {
+    if (e == cudaErrorMemoryAllocation) {
+        set_error(5, "out of device memory in %s", what);
+        cudaGetLastError();
+        return 5;
+    }
+    set_error(4, "CUDA error in %s: %s", what, cudaGetErrorString(e));
+    return 4;
+}
+
+cudaStream_t stream() {
+    if (!g_stream) cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking);
+    return g_stream;
+}
+
+// optional per-launch timing: events recorded on the library stream around every launch
+static bool g_ktime = false;
+static std::vector<std::pair<const char *, std::pair<cudaEvent_t, cudaEvent_t>>> g_kev;
+static cudaEvent_t g_kprev = nullptr;
+static const char *g_kname = nullptr;
+
+void launch_begin(const char *name) {
+    if (!g_ktime) return;
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, stream());
+    g_kprev = e;
+    g_kname = name;
+}
+
+void count_launch(int n) {
+    g_launches += n;
+    if (g_ktime && g_kprev) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        cudaEventRecord(e, stream());
+        g_kev.push_back({g_kname, {g_kprev, e}});
+        g_kprev = nullptr;
+    }
+}
+
+bool make_plan(int n, int E, int tw_len, FFTPlan *pl) {
+    if (n < E || n % E) return false;
+    int rem = n, ns = 0;
+    int rad[MITOS_MAX_STAGES];
+    auto push = [&](int r) { if (ns < MITOS_MAX_STAGES) rad[ns++] = r; };
+    if (E % 8 == 0) {
+        while (rem % 8 == 0) { push(8); rem /= 8; }
+    }
+    while (rem % 4 == 0 && E % 4 == 0) { push(4); rem /= 4; }
+    while (rem % 2 == 0 && E % 2 == 0) { push(2); rem /= 2; }
+    while (rem % 3 == 0 && E % 3 == 0) { push(3); rem /= 3; }
+    if (rem != 1 || ns == 0 || ns >= MITOS_MAX_STAGES) return false;
+    pl->n = n;
+    pl->nst = ns;
+    for (int i = 0; i < ns; i++) pl->rad[i] = rad[i];
+    pl->tw_scale = tw_len / n;
+    return true;
+}
+
+static int elems_for(int N) {
+    int m = N;
+    while (m % 2 == 0) m /= 2;
+    if (m == 1) return 8;
+    if (m == 3) return 12;
+    return 0;
+}
+
+struct GeomEntry {
+    GridGeom g;
+    void *tw = nullptr;
+};
+static std::map<std::pair<int, int>, GeomEntry *> g_geoms;
+
+const GridGeom *geom(int N, int precision) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto key = std::make_pair(N, precision);
+    auto it = g_geoms.find(key);
+    if (it != g_geoms.end()) return &it->second->g;
+    int E = elems_for(N);
+    if (N < 16 || N > 4096 || E == 0 || (N / 2) % E) {
+        set_error(3, "grid size N = %d is not supported (2^k or 3*2^k, 16 <= N <= 4096)", N);
+        return nullptr;
+    }
+    GeomEntry *ge = new GeomEntry;
+    GridGeom &g = ge->g;
+    g.N = N;
+    g.H = N / 2 + 1;
+    g.plane = (long)N * g.H;
+    g.cells = (long)N * g.plane;
+    g.E = E;
+    if (!make_plan(N, E, N, &g.plN) || !make_plan(N / 2, E, N, &g.plH)) {
+        delete ge;
+        set_error(3, "no FFT schedule for N = %d", N);
+        return nullptr;
+    }
+    int tpp = N / E;
+    int P = 512 / tpp;
+    if (P < 1) P = 1;
+    if (P > 64) P = 64;
+    const size_t csz = precision == MITOS_FP32 ? 8 : 16;
+    while (P > 1 && (size_t)P * spad_len(N) * csz > 96 * 1024) P /= 2;
+    g.P_xy = P;
+    int tz = (N / 2) / E;
+    g.P_z = 256 / tz < 1 ? 1 : 256 / tz;
+    // twiddles exp(-2 pi i m / N) from the host libm in double
+    std::vector<double> tw(2 * N);
+    for (int m = 0; m < N; m++) {
+        double a = 2.0 * M_PI * (double)m / (double)N;
+        tw[2 * m] = cos(a);
+        tw[2 * m + 1] = -sin(a);
+    }
+    if (precision == MITOS_FP32) {
+        std::vector<float> twf(2 * N);
+        for (int i = 0; i < 2 * N; i++) twf[i] = (float)tw[i];
+        if (cudaMalloc(&ge->tw, sizeof(float) * 2 * N) != cudaSuccess) { delete ge; set_error(5, "twiddles"); return nullptr; }
+        cudaMemcpy(ge->tw, twf.data(), sizeof(float) * 2 * N, cudaMemcpyHostToDevice);
+    } else {
+        if (cudaMalloc(&ge->tw, sizeof(double) * 2 * N) != cudaSuccess) { delete ge; set_error(5, "twiddles"); return nullptr; }
+        cudaMemcpy(ge->tw, tw.data(), sizeof(double) * 2 * N, cudaMemcpyHostToDevice);
+    }
+    g.twN = ge->tw;
+    g_geoms[key] = ge;
+    return &ge->g;
+}
+
+// 1 / sinc(pi m / N)^order, m = -N/2 .. N/2, stored at m + N/2
+// (include/fft_kernels.h:187,198-219 factorised per axis)
+static std::map<std::tuple<int, int, int>, void *> g_windows;
+const void *window_table(int N, int order, int precision) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto key = std::make_tuple(N, order, precision);
+    auto it = g_windows.find(key);
+    if (it != g_windows.end()) return it->second;
+    std::vector<double> w(N + 1);
+    for (int m = -N / 2; m <= N / 2; m++) {
+        double x = M_PI * (double)m / (double)N;
+        double s = (m == 0) ? 1.0 : sin(x) / x;
+        w[m + N / 2] = 1.0 / pow(s, order);
+    }
+    void *d = nullptr;
+    if (precision == MITOS_FP32) {
+        std::vector<float> wf(w.begin(), w.end());
+        if (cudaMalloc(&d, sizeof(float) * (N + 1)) != cudaSuccess) return nullptr;
+        cudaMemcpy(d, wf.data(), sizeof(float) * (N + 1), cudaMemcpyHostToDevice);
+    } else {
+        if (cudaMalloc(&d, sizeof(double) * (N + 1)) != cudaSuccess) return nullptr;
+        cudaMemcpy(d, w.data(), sizeof(double) * (N + 1), cudaMemcpyHostToDevice);
+    }
+    g_windows[key] = d;
+    return d;
+}
+
+// bin of each squared integer wavevector norm n2 in [0, 3 (N/2)^2]; -1 skips the mode
+static long isqrt_l(long a) {
+    long r = (long)sqrt((double)a);
+    while (r * r > a) r--;
+    while ((r + 1) * (r + 1) <= a) r++;
+    return r;
+}
+static std::map<std::tuple<int, int, int, double>, int *> g_bins;
+const int *bin_table(int N, int bins, int linear, double boxlen) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto key = std::make_tuple(N, bins, linear, linear ? 0.0 : boxlen);
+    auto it = g_bins.find(key);
+    if (it != g_bins.end()) return it->second;
+    const long n2max = 3L * (N / 2) * (N / 2);
+    std::vector<int> tab(n2max + 1, -1);
+    const double dk = 2 * M_PI / boxlen;
+    const double max_k = sqrt(3) * dk * N / 2, min_k = dk;
+    const double lmax = log(max_k), lmin = log(min_k);
+    for (long n2 = 1; n2 <= n2max; n2++) {
+        int b;
+        if (linear) {
+            // linear shells of width k_Nyquist / bins: b = isqrt(n2 bins^2) / (N/2)
+            b = (int)(isqrt_l(n2 * (long)bins * bins) / (N / 2));
+        } else {
+            // src/calc_powerspec.c:61-63 with k = dk sqrt(n2)
+            const double k = sqrt((double)n2) * dk;
+            const float u = (log(k) - lmin) / (lmax - lmin);
+            b = (int)floor((bins - 1) * u);
+        }
+        tab[n2] = (b >= 0 && b < bins) ? b : -1;
+    }
+    int *d = nullptr;
+    if (cudaMalloc(&d, sizeof(int) * (n2max + 1)) != cudaSuccess) return nullptr;
+    cudaMemcpy(d, tab.data(), sizeof(int) * (n2max + 1), cudaMemcpyHostToDevice);
+    g_bins[key] = d;
+    return d;
+}
+
+// ---- workspace: grid-sized device buffers reused across calls --------------------------
+static std::map<std::pair<size_t, int>, std::vector<void *>> g_ws;
+void *workspace(size_t bytes, int slot) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto &v = g_ws[std::make_pair(bytes, 0)];
+    while ((int)v.size() <= slot) v.push_back(nullptr);
+    if (!v[slot]) {
+        if (cudaMalloc(&v[slot], bytes) != cudaSuccess) {
+            cudaGetLastError();
+            v[slot] = nullptr;
+            set_error(5, "out of device memory allocating a %zu-byte workspace", bytes);
+        }
+    }
+    return v[slot];
+}
+
+void release_all() {
+    std::lock_guard<std::mutex> lk(g_mu);
+    for (auto &kv : g_ws)
+        for (void *p : kv.second) if (p) cudaFree(p);
+    g_ws.clear();
+    for (auto &kv : g_geoms) { cudaFree(kv.second->tw); delete kv.second; }
+    g_geoms.clear();
+    for (auto &kv : g_windows) cudaFree(kv.second);
+    g_windows.clear();
+    for (auto &kv : g_bins) cudaFree(kv.second);
+    g_bins.clear();
+}
+
+}  // namespace mitos
+
+extern "C" const char *mitos_last_error(void) { return mitos::g_err; }
+
+// per-launch timing (off by default): enable, run, then read name / milliseconds pairs
+extern "C" int mitos_kernel_timing(int on) {
+    cudaStreamSynchronize(mitos::stream());
+    for (auto &k : mitos::g_kev) {
+        cudaEventDestroy(k.second.first);
+        cudaEventDestroy(k.second.second);
+    }
+    mitos::g_kev.clear();
+    mitos::g_ktime = on != 0;
+    return 0;
+}
+extern "C" int mitos_kernel_times(const char **names, double *ms, int max) {
+    cudaStreamSynchronize(mitos::stream());
+    int n = 0;
+    for (auto &k : mitos::g_kev) {
+        if (n >= max) break;
+        float m = 0;
+        cudaEventElapsedTime(&m, k.second.first, k.second.second);
+        names[n] = k.first;
+        ms[n] = m;
+        n++;
+    }
+    return n;
+}
+extern "C" long mitos_launch_count(void) { return mitos::g_launches; }
+extern "C" int mitos_release_all(void) {
+    cudaDeviceSynchronize();
+    mitos::release_all();
+    return 0;
+}
+
+// CUDA-event timer on the library stream (the stream every kernel of the library runs on)
+static cudaEvent_t g_t0 = nullptr, g_t1 = nullptr;
+extern "C" int mitos_timer_start(void) {
+    if (!g_t0) {
+        cudaEventCreate(&g_t0);
+        cudaEventCreate(&g_t1);
+    }
+    return cudaEventRecord(g_t0, mitos::stream()) == cudaSuccess ? 0 : 4;
+}
+extern "C" double mitos_timer_stop(void) {
+    cudaEventRecord(g_t1, mitos::stream());
+    cudaEventSynchronize(g_t1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, g_t0, g_t1);
+    return ms;
+}
+extern "C" int mitos_sync(void) {
+    return cudaStreamSynchronize(mitos::stream()) == cudaSuccess ? 0 : 4;
+}

@@ -1,0 +1,23 @@
+// context.cuh -- cached device tables and workspace.
+#pragma once
+
+#include "fft_passes.cuh"
+
+namespace mitos {
+
+const void *window_table(int N, int order, int precision);
+const int *bin_table(int N, int bins, int linear, double boxlen);
+// grid-sized scratch buffer number `slot` of `bytes` bytes (kept until mitos_release_all)
+void *workspace(size_t bytes, int slot);
+void release_all();
+
+// white noise (noise.cu)
+struct NoiseFilter {
+    const void *table;  // device, filter value per n2 (precision of the grid), or NULL
+};
+int noise_generate(const GridGeom &g, int precision, double boxlen, uint64_t st[4],
+                   const void *filter_by_n2, void *fbox);
+int hermitian_planes(const GridGeom &g, int precision, void *fbox);
+void rng_jump(uint64_t st[4], unsigned long long n);
+
+}  // namespace mitos

@@ -1,0 +1,73 @@
+// fft_passes.cuh -- the pass kernels of the 3D real FFT and their fused k-space epilogues.
+//
+// Layouts (one rank, reference layout of struct distributed_grid):
+//   complex grid  element (x, y, kz) at (x*N + y)*H + kz,    H = N/2 + 1
+//   real grid     element (x, y, z)  at (x*N + y)*rp + z,    rp = N + 2 (padded) or N
+// c2r = X pass (complex, along x) -> Y pass (complex, along y) -> Z pass (half-complex -> real)
+// r2c = Z pass (real -> half-complex) -> Y pass -> X pass.  The Z c2r uses only the real parts
+// of the kz = 0 and kz = N/2 elements, as FFTW's c2r does.
+#pragma once
+
+#include "fft_core.cuh"
+
+namespace mitos {
+
+// shared description of one grid size / precision
+struct GridGeom {
+    int N, H;
+    long plane;   // N*H complex elements per x-plane
+    long cells;   // N*N*H complex elements
+    int E;        // elements per thread (8 for 2^k, 12 for 3*2^k)
+    FFTPlan plN;  // length-N plan (X and Y passes)
+    FFTPlan plH;  // length-N/2 plan (Z passes)
+    int P_xy;     // pencils per block in X/Y passes
+    int P_z;      // rows per block in Z passes
+    const void *twN;  // device table exp(-2 pi i m / N), m < N, in the grid precision
+};
+
+const GridGeom *geom(int N, int precision);  // cached; NULL if N unsupported
+
+// ---- the fused operations a pass can carry -----------------------------------------------
+enum XOp {
+    XOP_PLAIN = 0,    // out = FFT(in) * scale
+    XOP_HESS,         // out0..2 = FFT(phi), FFT(i kx phi), FFT(-kx^2 phi)            (inverse)
+    XOP_DISP,         // out0..1 = FFT(phi), FFT(i kx phi)                           (inverse)
+    XOP_COMBINE_2LPT, // out = [f1 * in2 + f2 * G(k) * FFT(in) * scale] * W(k)       (forward)
+    XOP_ADD_POISSON,  // out = in2 + G(k) * FFT(in) * scale                          (forward)
+    XOP_PK            // P(k) binning of |FFT(in) * scale * W(k)|^2 (+ optional out)  (forward)
+};
+enum YOp {
+    YOP_PLAIN = 0,    // out = FFT(in) * scale
+    YOP_HESS,         // 3 in -> 6 out: A2, i ky A1, A1, -ky^2 A0, i ky A0, A0
+    YOP_DISP          // 2 in -> 3 out: C1, i ky C0, C0
+};
+enum ZOp {
+    ZOP_C2R = 0,      // real out = c2r(in) * scale
+    ZOP_HESS_2LPT,    // 6 in (kz factors 1, 1, i kz, 1, i kz, -kz^2) -> S = sum_{i<j} (p_ii p_jj - p_ij^2)
+    ZOP_HESS_MA,      // same 6 in -> residual (1 + rho) - det(I + H), sums of res^2 and rho^2
+    ZOP_DISP          // 3 in (kz factors 1, 1, i kz) -> 3 real out
+};
+
+struct PassArgs {
+    const void *in[6];
+    void *out[6];
+    const void *in2;      // second input (XOP_COMBINE_2LPT / XOP_ADD_POISSON) or rho (ZOP_HESS_MA)
+    double scale;         // multiplies the transform result
+    double dk;            // 2 pi / boxlen
+    double f1, f2;        // combination factors
+    int window_order;     // 0: none, else 1 / W(k)^order with W = prod sinc(k_i L / 2N)
+    int rp_in, rp_out;    // real row pitch for Z passes
+    double rho_a, rho_b;  // Z r2c transform on load: x -> x * rho_a + rho_b
+    // P(k) binning (XOP_PK)
+    const int *bin_of_n2; // bin per squared integer wavevector norm (-1: skip)
+    int nbins;
+    double *bin_k, *bin_p; long long *bin_n;  // device accumulators
+    double *red;          // device FP64 reductions (ZOP_HESS_MA: [0] += res^2, [1] += rho^2)
+};
+
+template <typename T> int launch_x(const GridGeom &g, XOp op, int sign, const PassArgs &a);
+template <typename T> int launch_y(const GridGeom &g, YOp op, int sign, const PassArgs &a);
+template <typename T> int launch_z_c2r(const GridGeom &g, ZOp op, const PassArgs &a);
+template <typename T> int launch_z_r2c(const GridGeom &g, const PassArgs &a);
+
+}  // namespace mitos

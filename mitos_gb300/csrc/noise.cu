@@ -1,0 +1,394 @@
+// noise.cu -- white noise with the reference's sequential xoshiro256** stream, generated one
+// (x, y) column per thread on the GPU.
+//
+// src/grf.c:47-63 draws, on one rank, the modes in x -> y -> z order (z fastest) from one
+// stream; each mode with k > 0 takes two sampleNorm calls (four 64-bit draws, real part
+// first, src/random.c:34-49) and the DC mode takes none.  Column c = x N + y therefore starts
+// at draw offset 0 (c = 0) or 4 (c (N/2+1) - 1) (c > 0).
+//
+// xoshiro256** is linear over GF(2) on its 256-bit state, so the state after J steps is
+// q_J(A) s0, with A the one-step transition and q_J(x) = x^J mod p(x), p the characteristic
+// polynomial of A.  p is recovered once with Berlekamp-Massey from 512 output bits; the
+// polynomials of all column offsets are computed on the host (cached per N) and each thread
+// evaluates q_c(A) s0 by Horner's rule with 256 transition steps.
+#include <math.h>
+#include <string.h>
+
+#include <map>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "context.cuh"
+
+namespace mitos {
+
+// ---- GF(2) polynomial arithmetic modulo p(x) = x^256 + plow(x) ------------------------------
+struct Poly {
+    uint64_t w[4];
+};
+static Poly g_plow;
+static bool g_pready = false;
+static std::mutex g_nmu;
+
+static inline uint64_t rotl64h(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+static inline void xo_step(uint64_t s[4]) {
+    const uint64_t t = s[1] << 17;
+    s[2] ^= s[0];
+    s[3] ^= s[1];
+    s[1] ^= s[2];
+    s[0] ^= s[3];
+    s[2] ^= t;
+    s[3] = rotl64h(s[3], 45);
+}
+
+static void pmulmod(const Poly &a, const Poly &b, Poly &out) {
+    uint64_t r[9] = {0};
+    for (int i = 0; i < 256; i++) {
+        if (!((a.w[i >> 6] >> (i & 63)) & 1)) continue;
+        const int ws = i >> 6, bs = i & 63;
+        for (int j = 0; j < 4; j++) {
+            r[j + ws] ^= b.w[j] << bs;
+            if (bs) r[j + ws + 1] ^= b.w[j] >> (64 - bs);
+        }
+    }
+    for (int i = 511; i >= 256; i--) {
+        if (!((r[i >> 6] >> (i & 63)) & 1)) continue;
+        r[i >> 6] ^= 1ULL << (i & 63);
+        const int sh = i - 256, ws = sh >> 6, bs = sh & 63;
+        for (int j = 0; j < 4; j++) {
+            r[j + ws] ^= g_plow.w[j] << bs;
+            if (bs) r[j + ws + 1] ^= g_plow.w[j] >> (64 - bs);
+        }
+    }
+    memcpy(out.w, r, sizeof out.w);
+}
+
+static void pmulx(Poly &a) {
+    const uint64_t top = a.w[3] >> 63;
+    a.w[3] = (a.w[3] << 1) | (a.w[2] >> 63);
+    a.w[2] = (a.w[2] << 1) | (a.w[1] >> 63);
+    a.w[1] = (a.w[1] << 1) | (a.w[0] >> 63);
+    a.w[0] <<= 1;
+    if (top)
+        for (int j = 0; j < 4; j++) a.w[j] ^= g_plow.w[j];
+}
+
+static Poly ppow_x(unsigned long long e) {  // x^e mod p
+    Poly r = {{1, 0, 0, 0}};
+    Poly b = {{2, 0, 0, 0}};  // x
+    while (e) {
+        if (e & 1) pmulmod(r, b, r);
+        e >>= 1;
+        if (e) pmulmod(b, b, b);
+    }
+    return r;
+}
+
+// Horner evaluation q(A) s0 on the host
+static void horner(const Poly &q, const uint64_t s0[4], uint64_t out[4]) {
+    uint64_t r[4] = {0, 0, 0, 0};
+    for (int i = 255; i >= 0; i--) {
+        xo_step(r);
+        if ((q.w[i >> 6] >> (i & 63)) & 1)
+            for (int j = 0; j < 4; j++) r[j] ^= s0[j];
+    }
+    memcpy(out, r, 4 * sizeof(uint64_t));
+}
+
+// Berlekamp-Massey on bit 0 of s[0]; p(x) is the reciprocal of the connection polynomial
+static bool charpoly_init() {
+    if (g_pready) return true;
+    uint64_t s[4] = {0x9E3779B97f4A7C15ULL, 0xBF58476D1CE4E5B9ULL, 0x94D049BB133111EBULL, 1ULL};
+    const int NB = 512;
+    std::vector<uint8_t> b(NB);
+    for (int n = 0; n < NB; n++) {
+        b[n] = (uint8_t)(s[0] & 1);
+        xo_step(s);
+    }
+    std::vector<uint8_t> C(NB + 1, 0), B(NB + 1, 0), T;
+    C[0] = B[0] = 1;
+    int L = 0, m = 1;
+    for (int n = 0; n < NB; n++) {
+        uint8_t d = b[n];
+        for (int i = 1; i <= L; i++) d ^= C[i] & b[n - i];
+        if (!d) {
+            m++;
+        } else if (2 * L <= n) {
+            T = C;
+            for (int i = 0; i + m <= NB; i++) C[i + m] ^= B[i];
+            L = n + 1 - L;
+            B = T;
+            m = 1;
+        } else {
+            for (int i = 0; i + m <= NB; i++) C[i + m] ^= B[i];
+            m++;
+        }
+    }
+    if (L != 256) return false;
+    memset(&g_plow, 0, sizeof g_plow);
+    for (int j = 0; j < 256; j++)
+        if (C[256 - j]) g_plow.w[j >> 6] |= 1ULL << (j & 63);
+    // self-check: a jump of 1000 steps must equal 1000 sequential steps
+    uint64_t s0[4] = {1, 2, 3, 4}, seq[4] = {1, 2, 3, 4}, jmp[4];
+    for (int i = 0; i < 1000; i++) xo_step(seq);
+    g_pready = true;
+    horner(ppow_x(1000), s0, jmp);
+    if (memcmp(seq, jmp, sizeof seq) != 0) {
+        g_pready = false;
+        return false;
+    }
+    return true;
+}
+
+void rng_jump(uint64_t st[4], unsigned long long n) {
+    std::lock_guard<std::mutex> lk(g_nmu);
+    if (!charpoly_init()) return;
+    uint64_t out[4];
+    horner(ppow_x(n), st, out);
+    memcpy(st, out, sizeof out);
+}
+
+// per-N table of column polynomials (device), 4 x uint64 per column
+static std::map<int, uint64_t *> g_ptabs;
+static const uint64_t *column_polys(int N) {
+    std::lock_guard<std::mutex> lk(g_nmu);
+    auto it = g_ptabs.find(N);
+    if (it != g_ptabs.end()) return it->second;
+    if (!charpoly_init()) {
+        set_error(4, "xoshiro256** characteristic polynomial check failed");
+        return nullptr;
+    }
+    const long ncol = (long)N * N;
+    const unsigned long long T = 4ULL * (N / 2 + 1);
+    std::vector<uint64_t> tab(4 * ncol);
+    // columns of multiplication by x^T: MT[i] = x^(T + i) mod p
+    std::vector<Poly> MT(256);
+    MT[0] = ppow_x(T);
+    for (int i = 1; i < 256; i++) {
+        MT[i] = MT[i - 1];
+        pmulx(MT[i]);
+    }
+    unsigned nth = std::thread::hardware_concurrency();
+    if (nth < 1) nth = 1;
+    if (nth > 32) nth = 32;
+    if (ncol < 4096) nth = 1;
+    std::vector<std::thread> th;
+    for (unsigned w = 0; w < nth; w++) {
+        th.emplace_back([&, w]() {
+            long c0 = ncol * w / nth, c1 = ncol * (w + 1) / nth;
+            Poly q;
+            for (long c = c0; c < c1; c++) {
+                if (c == 0) {
+                    q = Poly{{1, 0, 0, 0}};
+                } else if (c == c0 || c == 1) {
+                    q = ppow_x(T * (unsigned long long)c - 4);
+                } else {
+                    Poly r = {{0, 0, 0, 0}};
+                    for (int i = 0; i < 256; i++)
+                        if ((q.w[i >> 6] >> (i & 63)) & 1)
+                            for (int j = 0; j < 4; j++) r.w[j] ^= MT[i].w[j];
+                    q = r;
+                }
+                memcpy(&tab[4 * c], q.w, sizeof q.w);
+            }
+        });
+    }
+    for (auto &t : th) t.join();
+    uint64_t *d = nullptr;
+    if (cudaMalloc(&d, sizeof(uint64_t) * 4 * ncol) != cudaSuccess) {
+        cudaGetLastError();
+        set_error(5, "out of device memory for the noise column table");
+        return nullptr;
+    }
+    cudaMemcpy(d, tab.data(), sizeof(uint64_t) * 4 * ncol, cudaMemcpyHostToDevice);
+    g_ptabs[N] = d;
+    return d;
+}
+
+// ---- device -----------------------------------------------------------------------------
+struct RngState {
+    uint64_t s[4];
+};
+
+__device__ __forceinline__ uint64_t drotl(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+
+__device__ __forceinline__ uint64_t dnext(uint64_t &s0, uint64_t &s1, uint64_t &s2, uint64_t &s3) {
+    const uint64_t result = drotl(s1 * 5, 7) * 9;  // include/random_xorshift.h:17
+    const uint64_t t = s1 << 17;
+    s2 ^= s0;
+    s3 ^= s1;
+    s1 ^= s2;
+    s0 ^= s3;
+    s2 ^= t;
+    s3 = drotl(s3, 45);
+    return result;
+}
+
+// sampleNorm in FP64: src/random.c:34-49 (2^64 = (double)UINT64_MAX + 1)
+__device__ __forceinline__ double gauss64(uint64_t A, uint64_t B) {
+    const double RMax = 18446744073709551616.0;
+    const double u = (__ull2double_rn(A) + 0.5) / RMax;
+    const double v = (__ull2double_rn(B) + 0.5) / RMax;
+    return sqrt(-2 * log(u)) * cos(2 * 3.14159265358979323846 * v);
+}
+
+// the same Box-Muller transform in FP32; ln u of u >= 1/2 goes through log1p of the exact
+// complement so that no precision is lost near u = 1
+__device__ __forceinline__ float gauss32(uint64_t A, uint64_t B) {
+    const float inv64 = 5.42101086242752217e-20f;  // 2^-64
+    float lnu;
+    if (A >> 63) {
+        const float t = (__ull2float_rn(~A) + 0.5f) * inv64;
+        lnu = log1pf(-t);
+    } else {
+        lnu = logf((__ull2float_rn(A) + 0.5f) * inv64);
+    }
+    const float v = (__ull2float_rn(B) + 0.5f) * inv64;
+    return sqrtf(-2.f * lnu) * cospif(2.f * v);
+}
+
+template <typename T> __device__ __forceinline__ T gauss(uint64_t A, uint64_t B);
+template <> __device__ __forceinline__ float gauss<float>(uint64_t A, uint64_t B) { return gauss32(A, B); }
+template <> __device__ __forceinline__ double gauss<double>(uint64_t A, uint64_t B) { return gauss64(A, B); }
+
+#define NOISE_THREADS 128
+#define NOISE_CHUNK 16
+
+template <typename T>
+__global__ void __launch_bounds__(NOISE_THREADS)
+k_noise(int N, const uint64_t *__restrict__ polys, RngState s0, T factor, const T *__restrict__ filt,
+        cplx<T> *__restrict__ out) {
+    __shared__ cplx<T> stage[NOISE_THREADS][NOISE_CHUNK + 1];
+    const int H = N / 2 + 1;
+    const long ncol = (long)N * N;
+    const long c = (long)blockIdx.x * NOISE_THREADS + threadIdx.x;
+    const bool valid = c < ncol;
+    uint64_t r0 = 0, r1 = 0, r2 = 0, r3 = 0;
+    int ky = 0, kx = 0;
+    if (valid) {
+        const uint64_t q0 = polys[4 * c], q1 = polys[4 * c + 1], q2 = polys[4 * c + 2], q3 = polys[4 * c + 3];
+        // Horner: r = sum_i q_i A^i s0
+#pragma unroll 4
+        for (int i = 255; i >= 0; i--) {
+            const uint64_t t = r1 << 17;
+            r2 ^= r0;
+            r3 ^= r1;
+            r1 ^= r2;
+            r0 ^= r3;
+            r2 ^= t;
+            r3 = drotl(r3, 45);
+            const uint64_t w = (i >= 192) ? q3 : (i >= 128) ? q2 : (i >= 64) ? q1 : q0;
+            const uint64_t m = 0ULL - ((w >> (i & 63)) & 1ULL);
+            r0 ^= s0.s[0] & m;
+            r1 ^= s0.s[1] & m;
+            r2 ^= s0.s[2] & m;
+            r3 ^= s0.s[3] & m;
+        }
+        kx = kint((int)(c / N), N);
+        ky = kint((int)(c % N), N);
+    }
+    const long rowbase0 = ((long)blockIdx.x * NOISE_THREADS) * H;
+    for (int z0 = 0; z0 < H; z0 += NOISE_CHUNK) {
+        const int cz = (H - z0) < NOISE_CHUNK ? (H - z0) : NOISE_CHUNK;
+        if (valid) {
+            for (int j = 0; j < cz; j++) {
+                const int z = z0 + j;
+                cplx<T> val = mk<T>(0, 0);
+                const long n2 = (long)kx * kx + (long)ky * ky + (long)z * z;
+                if (n2 > 0) {
+                    const uint64_t A = dnext(r0, r1, r2, r3), B = dnext(r0, r1, r2, r3);
+                    const uint64_t C2 = dnext(r0, r1, r2, r3), D = dnext(r0, r1, r2, r3);
+                    T a = gauss<T>(A, B) * factor;
+                    T b = gauss<T>(C2, D) * factor;
+                    if (filt) {
+                        const T f = filt[n2];
+                        a *= f;
+                        b *= f;
+                    }
+                    val = mk<T>(a, b);
+                }
+                stage[threadIdx.x][j] = val;
+            }
+        }
+        __syncthreads();
+        // coalesced write-out: the block's rows are contiguous in memory
+        for (int idx = threadIdx.x; idx < NOISE_THREADS * cz; idx += NOISE_THREADS) {
+            const int rr = idx / cz, j = idx % cz;
+            if ((long)blockIdx.x * NOISE_THREADS + rr < ncol)
+                out[rowbase0 + (long)rr * H + z0 + j] = stage[rr][j];
+        }
+        __syncthreads();
+    }
+}
+
+// enforce_hermiticity on the kz = 0 and kz = N/2 planes (src/grf.c:103-137): targets are never
+// sources, so the planes are fixed in place
+template <typename T>
+__global__ void k_hermitian(int N, cplx<T> *fbox) {
+    const int H = N / 2 + 1;
+    const int x = blockIdx.y;  // 0 .. N/2
+    const int zsel = blockIdx.z;
+    const int z = zsel ? N / 2 : 0;
+    for (int y = blockIdx.x * blockDim.x + threadIdx.x; y < N; y += gridDim.x * blockDim.x) {
+        if ((x == 0 || x == N / 2) && y > N / 2) continue;
+        const int invx = (x > 0) ? N - x : 0;
+        const int invy = (y > 0) ? N - y : 0;
+        const long id = ((long)x * N + y) * H + z;
+        if (invx == x && invy == y) {
+            fbox[id].y = 0;
+        } else {
+            const cplx<T> s = fbox[((long)invx * N + invy) * H + z];
+            fbox[id] = mk<T>(s.x, -s.y);
+        }
+    }
+}
+
+int noise_generate(const GridGeom &g, int precision, double boxlen, uint64_t st[4],
+                   const void *filter_by_n2, void *fbox) {
+    const uint64_t *polys = column_polys(g.N);
+    if (!polys) return 5;
+    RngState s0;
+    memcpy(s0.s, st, sizeof s0.s);
+    const double boxvol = boxlen * boxlen * boxlen;
+    const double factor = sqrt(boxvol / 2);  // src/grf.c:33
+    const long ncol = (long)g.N * g.N;
+    const unsigned blocks = (unsigned)((ncol + NOISE_THREADS - 1) / NOISE_THREADS);
+    launch_begin("noise");
+    if (precision == MITOS_FP32)
+        k_noise<float><<<blocks, NOISE_THREADS, 0, stream()>>>(g.N, polys, s0, (float)factor,
+                                                               (const float *)filter_by_n2, (float2 *)fbox);
+    else
+        k_noise<double><<<blocks, NOISE_THREADS, 0, stream()>>>(g.N, polys, s0, factor,
+                                                                (const double *)filter_by_n2, (double2 *)fbox);
+    count_launch();
+    MITOS_LAUNCH_CHECK("noise");
+    return 0;
+}
+
+int hermitian_planes(const GridGeom &g, int precision, void *fbox) {
+    dim3 grid((g.N + 255) / 256, g.N / 2 + 1, 2);
+    launch_begin("hermitian");
+    if (precision == MITOS_FP32) k_hermitian<float><<<grid, 256, 0, stream()>>>(g.N, (float2 *)fbox);
+    else k_hermitian<double><<<grid, 256, 0, stream()>>>(g.N, (double2 *)fbox);
+    count_launch();
+    MITOS_LAUNCH_CHECK("hermitian planes");
+    return 0;
+}
+
+}  // namespace mitos
+
+// ---- host-only entry points for checking the jump-ahead without a GPU ---------------------
+// state after n draws from s0 (polynomial jump)
+extern "C" int mitos_rng_jump(uint64_t s[4], unsigned long long n) {
+    mitos::rng_jump(s, n);
+    return 0;
+}
+// start state of noise column c of an N grid (the state the GPU thread of column c uses)
+extern "C" int mitos_noise_column_state(int N, long c, const uint64_t s0[4], uint64_t out[4]) {
+    uint64_t s[4] = {s0[0], s0[1], s0[2], s0[3]};
+    const unsigned long long T = 4ULL * (N / 2 + 1);
+    mitos::rng_jump(s, c == 0 ? 0ULL : T * (unsigned long long)c - 4ULL);
+    for (int i = 0; i < 4; i++) out[i] = s[i];
+    return 0;
+}

@@ -1,0 +1,13 @@
+// particles.cuh -- particle stage launchers.
+#pragma once
+
+namespace mitos {
+
+// lattice of M^3 particles, TSC displacement by the three padded displacement grids, wrap,
+// CIC into rho (padded real grid, accumulated, in units of the mean density); pos_out optional
+int displace_and_deposit(int N, int M, double boxlen, int precision, const void *d0, const void *d1,
+                         const void *d2, void *rho, float *pos_out);
+// CIC of n given positions with per-particle value val
+int cic_positions(long n, int N, double boxlen, int precision, const float *pos, double val, void *rho);
+
+}  // namespace mitos

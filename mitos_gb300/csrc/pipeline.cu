@@ -1,0 +1,354 @@
+// pipeline.cu -- the fused initial-condition pipeline (ic_pipeline_run).
+//
+// Stage order (src/mitos.c:205-422,794-863,1072-1077 then analyse/src/mitos_read.c:278-419), with
+// the reference's redundant c2r -> r2c round trips removed (exact in exact arithmetic):
+//   S1  noise x sqrt(P_prim) x T(k, tau_src) x rescale x (-1/k^2)  -> phi1(k)   [+ Hermitian planes]
+//   S2  six Hessians of phi1 (X, Y, Z passes) with the 2LPT source fused into the Z pass -> S(x)
+//   S3  S r2c; the last X pass forms phi = f1 phi1 - f2 S/k^2 and undoes the TSC window
+//       (Monge-Ampere: S2/S3 iterate residual -> phi += -res/k^2 until the tolerance)
+//   S4  three displacement grids (X, Y, Z passes)
+//   S5  lattice + TSC displacement + wrap + CIC deposit
+//   S6  density r2c; the last X pass undoes the CIC window and bins P(k)
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <vector>
+
+#include "context.cuh"
+#include "kspace.cuh"
+#include "particles.cuh"
+
+namespace mitos {
+int grid_c2r(const GridGeom &g, int prec, double boxlen, void *fbox, void *box);
+int grid_hessian(const GridGeom &g, int prec, double boxlen, const void *phi, int zop, const void *rho,
+                 void *out, double *red, int window_order);
+}  // namespace mitos
+
+using namespace mitos;
+
+// filter per squared integer wavevector norm: include/fft_kernels.h:116-155 (power, transfer),
+// rescale, and optionally the inverse Poisson kernel (:96-99)
+template <typename T>
+__global__ void k_filter(long n2max, double dk, double A_s, double n_s, double k_pivot,
+                         const double *__restrict__ tab, int k_size, double u_tau, double rescale,
+                         int poisson, T *__restrict__ out) {
+    for (long n2 = (long)blockIdx.x * blockDim.x + threadIdx.x; n2 <= n2max; n2 += (long)gridDim.x * blockDim.x) {
+        if (n2 == 0) { out[0] = 0; continue; }
+        const double k = sqrt((double)n2) * dk;
+        double v = sqrt(A_s * pow(k / k_pivot, n_s - 1.) * k * (2. * M_PI * M_PI));
+        v *= transfer_at<double>(tab, tab + k_size, tab + 2 * k_size, k_size, k, u_tau);
+        v *= rescale;
+        if (poisson) v *= -1.0 / k / k;
+        out[n2] = (T)v;
+    }
+}
+
+static double g_stage_ms[16];
+static int g_nstages = 0;
+
+extern "C" int mitos_stage_times(double *ms, int max) {
+    for (int i = 0; i < g_nstages && i < max; i++) ms[i] = g_stage_ms[i];
+    return g_nstages;
+}
+
+struct StageTimer {
+    bool on;
+    std::vector<cudaEvent_t> ev;
+    explicit StageTimer(bool enable) : on(enable) {}
+    void mark() {
+        if (!on) return;
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        cudaEventRecord(e, stream());
+        ev.push_back(e);
+    }
+    void finish() {
+        if (!on) return;
+        cudaEventSynchronize(ev.back());
+        g_nstages = 0;
+        for (size_t i = 1; i < ev.size() && i <= 16; i++) {
+            float m = 0;
+            cudaEventElapsedTime(&m, ev[i - 1], ev[i]);
+            g_stage_ms[g_nstages++] = m;
+        }
+        for (auto e : ev) cudaEventDestroy(e);
+    }
+};
+
+template <typename T>
+static int run_pipeline(const struct ic_config *cfg, const double *ktab, const double *tlo, const double *thi,
+                        int k_size, double u_tau, struct ic_result *res) {
+    const int prec = cfg->precision;
+    const int N = cfg->N, M = cfg->M;
+    const double L = cfg->boxlen;
+    const GridGeom *gp = geom(N, prec);
+    if (!gp) return 3;
+    const GridGeom &g = *gp;
+    const size_t gb = (size_t)g.cells * sizeof(cplx<T>);
+    const double V = L * L * L;
+    const double dk = 2 * M_PI / L;
+    StageTimer tim(getenv("MITOS_PROFILE") != nullptr);
+    tim.mark();
+
+    void *phi = workspace(gb, 0), *S = workspace(gb, 10), *Sk = workspace(gb, 11), *rho = workspace(gb, 12);
+    void *A0 = workspace(gb, 1), *A1 = workspace(gb, 2);
+    void *B0 = workspace(gb, 4), *B1 = workspace(gb, 5), *B2 = workspace(gb, 6);
+    void *D0 = workspace(gb, 7), *D1 = workspace(gb, 8), *D2 = workspace(gb, 9);
+    if (!phi || !S || !Sk || !rho || !A0 || !A1 || !B0 || !B1 || !B2 || !D0 || !D1 || !D2) return 5;
+    const long n2max = 3L * (N / 2) * (N / 2);
+    T *filt = (T *)workspace(sizeof(T) * (n2max + 1), 106);
+    double *dtab = (double *)workspace(sizeof(double) * 3 * k_size, 107);
+    double *acc = (double *)workspace(sizeof(double) * 3 * (size_t)cfg->pk_bins + 2 * sizeof(double), 104);
+    if (!filt || !dtab || !acc) return 5;
+    double *red = acc + 3 * cfg->pk_bins;
+
+    // inputs: the transfer table rows of the source time (host -> device)
+    MITOS_CUDA(cudaMemcpyAsync(dtab, ktab, sizeof(double) * k_size, cudaMemcpyHostToDevice, stream()));
+    MITOS_CUDA(cudaMemcpyAsync(dtab + k_size, tlo, sizeof(double) * k_size, cudaMemcpyHostToDevice, stream()));
+    MITOS_CUDA(cudaMemcpyAsync(dtab + 2 * k_size, thi, sizeof(double) * k_size, cudaMemcpyHostToDevice, stream()));
+    const bool ma = cfg->method == MITOS_METHOD_MONGE_AMPERE;
+    {
+        int blocks = (int)((n2max + 256) / 256);
+        if (blocks > 4096) blocks = 4096;
+        launch_begin("filter");
+        k_filter<T><<<blocks, 256, 0, stream()>>>(n2max, dk, cfg->A_s, cfg->n_s, cfg->k_pivot, dtab, k_size, u_tau,
+                                                  1.0, ma ? 0 : 1, filt);
+        count_launch();
+        MITOS_LAUNCH_CHECK("filter table");
+    }
+    tim.mark();
+
+    // S1: noise (src/mitos.c:148,220-224 + generatePerturbationGrid)
+    uint64_t st[4];
+    {
+        // splitmix64 seeding (include/random_xorshift.h:38-59) of Seed + rank 0
+        uint64_t s = cfg->seed;
+        for (int i = 0; i < 4; i++) {
+            uint64_t r = s;
+            s = r + 0x9E3779B97f4A7C15ULL;
+            r = (r ^ (r >> 30)) * 0xBF58476D1CE4E5B9ULL;
+            r = (r ^ (r >> 27)) * 0x94D049BB133111EBULL;
+            st[i] = r ^ (r >> 31);
+        }
+    }
+    int e;
+    void *dens_k = ma ? Sk : phi;  // Monge-Ampere keeps delta(k) to build rho(x)
+    e = noise_generate(g, prec, L, st, filt, dens_k);
+    if (!e) e = hermitian_planes(g, prec, dens_k);
+    if (e) return e;
+    tim.mark();
+
+    PassArgs a;
+    int win_disp = 3;
+    int iters = 0;
+    double last_rel = 0;
+    if (cfg->method == MITOS_METHOD_2LPT) {
+        // S2: Hessians + source
+        e = grid_hessian(g, prec, L, phi, ZOP_HESS_2LPT, nullptr, S, nullptr, 0);
+        if (e) return e;
+        tim.mark();
+        // S3: S r2c -> phi = f1 phi1 + f2 (-1/k^2) S, TSC window undone (src/2lpt.c:125-136)
+        memset(&a, 0, sizeof a);
+        a.dk = dk;
+        a.scale = 1.0;
+        a.in[0] = S;
+        a.out[0] = Sk;
+        a.rp_in = N + 2;
+        a.rho_a = 1.0;
+        e = launch_z_r2c<T>(g, a);
+        a.in[0] = Sk;
+        if (!e) e = launch_y<T>(g, YOP_PLAIN, -1, a);
+        a.in2 = phi;
+        a.out[0] = phi;
+        a.scale = V / ((double)N * N * N);
+        a.f1 = 1.0;
+        a.f2 = -3. / 7.;  // src/mitos.c:385
+        a.window_order = 3;
+        if (!e) e = launch_x<T>(g, XOP_COMBINE_2LPT, -1, a);
+        if (e) return e;
+        win_disp = 0;
+        tim.mark();
+    } else if (ma) {
+        // rho(x) = c2r(delta(k)) and phi = -delta/k^2 (src/monge_ampere.c:87-90)
+        void *rhoR = workspace(gb, 13);
+        void *tmp = workspace(gb, 14);
+        if (!rhoR || !tmp) return 5;
+        KernelParams kp;
+        memset(&kp, 0, sizeof kp);
+        kp.id = KID_INV_POISSON;
+        e = apply_kernel_launch(N, L, prec, kp, Sk, phi);
+        if (!e) { MITOS_CUDA(cudaMemcpyAsync(tmp, Sk, gb, cudaMemcpyDeviceToDevice, stream())); }
+        if (!e) e = grid_c2r(g, prec, L, tmp, rhoR);
+        if (e) return e;
+        tim.mark();
+        const int maxc = cfg->ma_cycles > 0 ? cfg->ma_cycles : 1;
+        for (int it = 0; it < maxc; it++) {
+            MITOS_CUDA(cudaMemsetAsync(red, 0, 2 * sizeof(double), stream()));
+            e = grid_hessian(g, prec, L, phi, ZOP_HESS_MA, rhoR, S, red, 0);
+            if (e) return e;
+            memset(&a, 0, sizeof a);
+            a.dk = dk;
+            a.scale = 1.0;
+            a.in[0] = S;
+            a.out[0] = Sk;
+            a.rp_in = N + 2;
+            a.rho_a = 1.0;
+            e = launch_z_r2c<T>(g, a);
+            a.in[0] = Sk;
+            if (!e) e = launch_y<T>(g, YOP_PLAIN, -1, a);
+            a.in2 = phi;
+            a.out[0] = phi;
+            a.scale = V / ((double)N * N * N);
+            if (!e) e = launch_x<T>(g, XOP_ADD_POISSON, -1, a);
+            if (e) return e;
+            double h[2];
+            MITOS_CUDA(cudaMemcpyAsync(h, red, sizeof h, cudaMemcpyDeviceToHost, stream()));
+            MITOS_CUDA(cudaStreamSynchronize(stream()));
+            iters = it + 1;
+            last_rel = sqrt(h[0] / h[1]);
+            if (cfg->ma_tol > 0 && last_rel <= cfg->ma_tol) break;
+        }
+        tim.mark();
+    } else {
+        tim.mark();
+        tim.mark();
+    }
+
+    // S4: displacement grids d_i = c2r(i k_i phi W^-3) (src/mitos.c:395-416)
+    memset(&a, 0, sizeof a);
+    a.dk = dk;
+    a.scale = 1.0;
+    a.window_order = win_disp;
+    a.in[0] = phi;
+    a.out[0] = A0;
+    a.out[1] = A1;
+    e = launch_x<T>(g, XOP_DISP, +1, a);
+    if (e) return e;
+    a.window_order = 0;
+    a.in[0] = A0;
+    a.in[1] = A1;
+    a.out[0] = B0;
+    a.out[1] = B1;
+    a.out[2] = B2;
+    e = launch_y<T>(g, YOP_DISP, +1, a);
+    if (e) return e;
+    a.in[0] = B0;
+    a.in[1] = B1;
+    a.in[2] = B2;
+    a.out[0] = D0;
+    a.out[1] = D1;
+    a.out[2] = D2;
+    a.rp_out = N + 2;
+    a.scale = 1.0 / V;
+    e = launch_z_c2r<T>(g, ZOP_DISP, a);
+    if (e) return e;
+    tim.mark();
+
+    // S5: particles + CIC
+    float *dpos = nullptr;
+    if (res && res->pos) {
+        dpos = (float *)workspace(sizeof(float) * 3 * (size_t)M * M * M, 108);
+        if (!dpos) return 5;
+    }
+    MITOS_CUDA(cudaMemsetAsync(rho, 0, gb, stream()));
+    e = displace_and_deposit(N, M, L, prec, D0, D1, D2, rho, dpos);
+    if (e) return e;
+    tim.mark();
+
+    // S6: overdensity r2c, CIC window undo, P(k) (analyse/src/mitos_read.c:364-419)
+    const int *bins = bin_table(N, cfg->pk_bins, cfg->pk_linear, L);
+    if (!bins) return 5;
+    MITOS_CUDA(cudaMemsetAsync(acc, 0, sizeof(double) * 3 * cfg->pk_bins, stream()));
+    memset(&a, 0, sizeof a);
+    a.dk = dk;
+    a.scale = 1.0;
+    a.in[0] = rho;
+    a.out[0] = Sk;
+    a.rp_in = N + 2;
+    a.rho_a = 1.0;
+    a.rho_b = -1.0;
+    e = launch_z_r2c<T>(g, a);
+    a.in[0] = Sk;
+    if (!e) e = launch_y<T>(g, YOP_PLAIN, -1, a);
+    a.rho_a = 1.0;
+    a.rho_b = 0.0;
+    a.out[0] = nullptr;
+    a.scale = V / ((double)N * N * N);
+    a.window_order = 2;
+    a.bin_of_n2 = bins;
+    a.nbins = cfg->pk_bins;
+    a.bin_k = acc;
+    a.bin_p = acc + cfg->pk_bins;
+    a.bin_n = (long long *)(acc + 2 * cfg->pk_bins);
+    if (!e) e = launch_x<T>(g, XOP_PK, -1, a);
+    if (e) return e;
+    tim.mark();
+
+    if (res) {
+        std::vector<double> h(3 * cfg->pk_bins);
+        MITOS_CUDA(cudaMemcpyAsync(h.data(), acc, sizeof(double) * 3 * cfg->pk_bins, cudaMemcpyDeviceToHost, stream()));
+        if (dpos)
+            MITOS_CUDA(cudaMemcpyAsync(res->pos, dpos, sizeof(float) * 3 * (size_t)M * M * M, cudaMemcpyDeviceToHost,
+                                       stream()));
+        MITOS_CUDA(cudaStreamSynchronize(stream()));
+        for (int i = 0; i < cfg->pk_bins; i++) {
+            long long n;
+            memcpy(&n, &h[2 * cfg->pk_bins + i], sizeof n);
+            if (res->pk_obs) res->pk_obs[i] = (long)n;
+            if (res->pk_k) res->pk_k[i] = h[i] / (double)n;
+            if (res->pk_p) res->pk_p[i] = h[cfg->pk_bins + i] / (double)n / V;
+        }
+        res->ma_iterations = iters;
+        res->ma_residual = last_rel;
+    } else {
+        MITOS_CUDA(cudaStreamSynchronize(stream()));
+    }
+    tim.finish();
+    return 0;
+}
+
+extern "C" int ic_pipeline_run_table(const struct ic_config *cfg, int k_size, int tau_size, int n_functions,
+                                     const double *k, const double *log_tau, const double *redshift,
+                                     const double *D_growth, const double *delta, struct ic_result *res) {
+    if (!cfg || cfg->N < 16 || cfg->M < 1 || cfg->boxlen <= 0 || cfg->pk_bins < 1) {
+        set_error(1, "invalid ic_config");
+        return 1;
+    }
+    if (cfg->index_src < 0 || cfg->index_src >= n_functions) {
+        set_error(1, "transfer function index %d out of range", cfg->index_src);
+        return 1;
+    }
+    struct perturb_data pd;
+    memset(&pd, 0, sizeof pd);
+    pd.k_size = k_size;
+    pd.tau_size = tau_size;
+    pd.n_functions = n_functions;
+    pd.k = (double *)k;
+    pd.log_tau = (double *)log_tau;
+    pd.redshift = (double *)redshift;
+    pd.D_growth = (double *)D_growth;
+    pd.delta = (double *)delta;
+    // src/mitos.c:151-153 with z_source = z_ini (rescale factor 1, :357-362)
+    const double lt = log_tau_at_z_h(&pd, cfg->z_ini);
+    int tau_index;
+    double u_tau;
+    find_tau_h(&pd, lt, &tau_index, &u_tau);
+    const double *arr = delta + (long)cfg->index_src * k_size * tau_size;
+    const double *tlo = arr + (long)k_size * tau_index, *thi = arr + (long)k_size * (tau_index + 1);
+    if (cfg->precision == MITOS_FP32) return run_pipeline<float>(cfg, k, tlo, thi, k_size, u_tau, res);
+    if (cfg->precision == MITOS_FP64) return run_pipeline<double>(cfg, k, tlo, thi, k_size, u_tau, res);
+    set_error(3, "unknown precision %d", cfg->precision);
+    return 3;
+}
+
+extern "C" int ic_pipeline_run(const struct ic_config *cfg, const struct perturb_spline *spline,
+                               struct ic_result *res) {
+    if (!spline || !spline->ptdat) {
+        set_error(1, "missing perturbation spline");
+        return 1;
+    }
+    const struct perturb_data *pd = spline->ptdat;
+    return ic_pipeline_run_table(cfg, pd->k_size, pd->tau_size, pd->n_functions, pd->k, pd->log_tau, pd->redshift,
+                                 pd->D_growth, pd->delta, res);
+}

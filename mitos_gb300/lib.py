@@ -1,0 +1,369 @@
+"""ctypes mirror of the C ABI in include/mitos_gb300.h.
+
+The names and argument meanings follow the reference entry points (alloc_local_grid,
+fft_r2c_dg, fft_c2r_dg, fft_apply_kernel_dg, generate_complex_grf, enforce_hermiticity,
+solvePoisson_dg, solve2LPT, solveMongeAmpere, calc_cross_powerspec, ...).  A non-zero status
+raises MitosError with the library's description.  The CUDA library is required: importing
+this module on a machine without it, or calling into it without a GPU, fails loudly.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+FP64 = 0
+FP32 = 1
+METHOD_ZELDOVICH = 1
+METHOD_2LPT = 2
+METHOD_MONGE_AMPERE = 3
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_fp = ctypes.POINTER(ctypes.c_float)
+_lp = ctypes.POINTER(ctypes.c_long)
+_ip = ctypes.POINTER(ctypes.c_int)
+
+
+class MitosError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"mitos_gb300 status {code}: {msg}")
+        self.code = code
+
+
+class DistributedGrid(ctypes.Structure):
+    _fields_ = [("N", ctypes.c_int), ("boxlen", ctypes.c_double), ("comm", ctypes.c_void_p),
+                ("momentum_space", ctypes.c_char), ("NX", ctypes.c_long), ("X0", ctypes.c_long),
+                ("local_size", ctypes.c_long), ("fbox", ctypes.c_void_p), ("box", ctypes.c_void_p),
+                ("precision", ctypes.c_int), ("flags", ctypes.c_int), ("priv", ctypes.c_void_p)]
+
+
+class RngState(ctypes.Structure):
+    _fields_ = [("s", ctypes.c_uint64 * 4)]
+
+
+class Kernel(ctypes.Structure):
+    _fields_ = [("kx", ctypes.c_double), ("ky", ctypes.c_double), ("kz", ctypes.c_double),
+                ("k", ctypes.c_double), ("kern", ctypes.c_double * 2), ("params", ctypes.c_void_p)]
+
+
+class Cosmology(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in
+                ("h", "n_s", "A_s", "k_pivot", "z_ini", "log_tau_ini", "rho_crit", "z_source",
+                 "log_tau_source")]
+
+
+class PerturbData(ctypes.Structure):
+    _fields_ = [("k_size", ctypes.c_int), ("tau_size", ctypes.c_int), ("n_functions", ctypes.c_int),
+                ("delta", _dp), ("k", _dp), ("log_tau", _dp), ("redshift", _dp), ("D_growth", _dp),
+                ("f_growth", _dp), ("H_Hubble", _dp), ("titles", ctypes.POINTER(ctypes.c_char_p)),
+                ("Omega", _dp)]
+
+
+class PerturbSpline(ctypes.Structure):
+    _fields_ = [("ptdat", ctypes.POINTER(PerturbData)), ("k_acc_table", _dp),
+                ("k_acc_table_size", ctypes.c_int)]
+
+
+class SplineParams(ctypes.Structure):
+    _fields_ = [("spline", ctypes.POINTER(PerturbSpline)), ("index_src", ctypes.c_int),
+                ("tau_index", ctypes.c_int), ("u_tau", ctypes.c_double)]
+
+
+class HermiteParams(ctypes.Structure):
+    _fields_ = [("order", ctypes.c_int), ("N", ctypes.c_int), ("boxlen", ctypes.c_double)]
+
+
+class ICConfig(ctypes.Structure):
+    _fields_ = [("N", ctypes.c_int), ("M", ctypes.c_int), ("boxlen", ctypes.c_double),
+                ("seed", ctypes.c_uint64), ("A_s", ctypes.c_double), ("n_s", ctypes.c_double),
+                ("k_pivot", ctypes.c_double), ("z_ini", ctypes.c_double), ("index_src", ctypes.c_int),
+                ("method", ctypes.c_int), ("ma_cycles", ctypes.c_int), ("ma_tol", ctypes.c_double),
+                ("pk_bins", ctypes.c_int), ("pk_linear", ctypes.c_int), ("precision", ctypes.c_int),
+                ("keep_outputs", ctypes.c_int)]
+
+
+class ICResult(ctypes.Structure):
+    _fields_ = [("pk_k", _dp), ("pk_p", _dp), ("pk_obs", _lp), ("pos", _fp),
+                ("ma_iterations", ctypes.c_int), ("ma_residual", ctypes.c_double)]
+
+
+_lib = None
+
+KERNEL_NAMES = ["constant", "lowpass", "hipass", "tophat", "elliptic_tophat", "translate",
+                "gaussian", "gaussian_inv", "inv_poisson", "dx", "dy", "dz", "power_no_transfer",
+                "transfer_function", "inv_transfer_function", "undo_Hermite_window"]
+
+# every symbol include/mitos_gb300.h declares
+EXPORTS = ["alloc_local_grid", "free_local_grid", "free_local_real_grid", "free_local_complex_grid",
+           "fft_wavevector", "fft_r2c_dg", "fft_c2r_dg", "fft_apply_kernel_dg",
+           "generate_complex_grf", "enforce_hermiticity", "generatePerturbationGrid",
+           "solvePoisson_dg", "solve2LPT", "solveMongeAmpere", "calc_cross_powerspec",
+           "calc_cross_powerspec_float", "calc_cross_powerspec_float_mpi", "mitos_set_precision",
+           "mitos_get_precision", "alloc_local_grid_prec", "dg_copy_to_host", "dg_copy_from_host",
+           "mitos_last_error", "mitos_launch_count", "mitos_release_all", "cic_deposit_dg",
+           "ic_pipeline_run", "ic_pipeline_run_table", "mitos_timer_start", "mitos_timer_stop",
+           "mitos_sync", "mitos_kernel_timing", "mitos_kernel_times", "mitos_stage_times",
+           "mitos_ma_history", "mitos_rng_jump", "mitos_noise_column_state"] + \
+          ["kernel_" + k for k in KERNEL_NAMES]
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load the CUDA library (building it first when missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise MitosError(4, f"{path} is missing; run mitos_gb300.build.build()")
+        _build.build()
+    L = ctypes.CDLL(path)
+    L.mitos_last_error.restype = ctypes.c_char_p
+    L.mitos_timer_stop.restype = ctypes.c_double
+    L.mitos_launch_count.restype = ctypes.c_long
+    _lib = L
+    return L
+
+
+def _check(status: int) -> None:
+    if status != 0:
+        raise MitosError(status, load().mitos_last_error().decode())
+
+
+def last_error() -> str:
+    return load().mitos_last_error().decode()
+
+
+def launch_count() -> int:
+    return int(load().mitos_launch_count())
+
+
+def set_precision(p: int) -> None:
+    _check(load().mitos_set_precision(p))
+
+
+# ---- grids ---------------------------------------------------------------------------------
+def alloc_local_grid(N: int, boxlen: float, precision: int = FP64) -> DistributedGrid:
+    dg = DistributedGrid()
+    _check(load().alloc_local_grid_prec(ctypes.byref(dg), N, ctypes.c_double(boxlen), None, precision))
+    return dg
+
+
+def free_local_grid(dg: DistributedGrid) -> None:
+    _check(load().free_local_grid(ctypes.byref(dg)))
+
+
+def _ctype(dg):
+    return (np.complex64, np.float32) if dg.precision == FP32 else (np.complex128, np.float64)
+
+
+def get_fbox(dg: DistributedGrid) -> np.ndarray:
+    c, _ = _ctype(dg)
+    out = np.empty((dg.N, dg.N, dg.N // 2 + 1), c)
+    _check(load().dg_copy_to_host(ctypes.byref(dg), 0, out.ctypes.data_as(ctypes.c_void_p)))
+    return out
+
+
+def get_box(dg: DistributedGrid) -> np.ndarray:
+    _, r = _ctype(dg)
+    out = np.empty((dg.N, dg.N, dg.N + 2), r)
+    _check(load().dg_copy_to_host(ctypes.byref(dg), 1, out.ctypes.data_as(ctypes.c_void_p)))
+    return out
+
+
+def set_fbox(dg: DistributedGrid, a: np.ndarray, momentum_space: bool = True) -> None:
+    c, _ = _ctype(dg)
+    a = np.ascontiguousarray(a, dtype=c).reshape(dg.N, dg.N, dg.N // 2 + 1)
+    _check(load().dg_copy_from_host(ctypes.byref(dg), 0, a.ctypes.data_as(ctypes.c_void_p)))
+    dg.momentum_space = b"\x01" if momentum_space else b"\x00"
+
+
+def set_box(dg: DistributedGrid, a: np.ndarray) -> None:
+    _, r = _ctype(dg)
+    a = np.ascontiguousarray(a, dtype=r)
+    if a.shape[-1] == dg.N:
+        a = np.concatenate([a, np.zeros(a.shape[:-1] + (2,), r)], axis=-1)
+    a = np.ascontiguousarray(a).reshape(dg.N, dg.N, dg.N + 2)
+    _check(load().dg_copy_from_host(ctypes.byref(dg), 1, a.ctypes.data_as(ctypes.c_void_p)))
+    dg.momentum_space = b"\x00"
+
+
+# ---- FFT and kernels -----------------------------------------------------------------------
+def fft_r2c_dg(dg):
+    _check(load().fft_r2c_dg(ctypes.byref(dg)))
+
+
+def fft_c2r_dg(dg):
+    _check(load().fft_c2r_dg(ctypes.byref(dg)))
+
+
+def kernel_fn(name: str):
+    return ctypes.cast(getattr(load(), "kernel_" + name), ctypes.c_void_p)
+
+
+def fft_apply_kernel_dg(w, r, kernel: str, params=None) -> int:
+    """Returns the status (does not raise) so that the error paths can be tested."""
+    L = load()
+    if params is None:
+        pp = None
+    elif isinstance(params, ctypes.Structure):
+        pp = ctypes.cast(ctypes.byref(params), ctypes.c_void_p)
+    else:
+        arr = (ctypes.c_double * len(np.atleast_1d(params)))(*np.atleast_1d(params).tolist())
+        pp = ctypes.cast(arr, ctypes.c_void_p)
+        fft_apply_kernel_dg._keep = arr
+    fn = kernel_fn(kernel) if isinstance(kernel, str) else kernel
+    return L.fft_apply_kernel_dg(ctypes.byref(w), ctypes.byref(r), fn, pp)
+
+
+def rng_init(seed: int) -> RngState:
+    """splitmix64 seeding of xoshiro256** (include/random_xorshift.h:49-59), host side."""
+    s = RngState()
+    st = seed & 0xFFFFFFFFFFFFFFFF
+    for i in range(4):
+        r = st
+        st = (r + 0x9E3779B97F4A7C15) & 0xFFFFFFFFFFFFFFFF
+        r = ((r ^ (r >> 30)) * 0xBF58476D1CE4E5B9) & 0xFFFFFFFFFFFFFFFF
+        r = ((r ^ (r >> 27)) * 0x94D049BB133111EB) & 0xFFFFFFFFFFFFFFFF
+        s.s[i] = r ^ (r >> 31)
+    return s
+
+
+def generate_complex_grf(dg, state: RngState):
+    _check(load().generate_complex_grf(ctypes.byref(dg), ctypes.byref(state)))
+
+
+def enforce_hermiticity(dg):
+    _check(load().enforce_hermiticity(ctypes.byref(dg)))
+
+
+def solvePoisson_dg(dg):
+    _check(load().solvePoisson_dg(ctypes.byref(dg)))
+
+
+def solve2LPT(pot, dens, work, f1=1.0, f2=-3.0 / 7.0):
+    _check(load().solve2LPT(ctypes.byref(pot), ctypes.byref(dens), ctypes.byref(work),
+                            ctypes.c_double(f1), ctypes.c_double(f2)))
+
+
+def solveMongeAmpere(pot, dens, work, cycles: int):
+    _check(load().solveMongeAmpere(ctypes.byref(pot), ctypes.byref(dens), ctypes.byref(work), cycles))
+
+
+def ma_history(max_cycles: int = 256):
+    eps = np.zeros(max_cycles)
+    rel = np.zeros(max_cycles)
+    n = load().mitos_ma_history(eps.ctypes.data_as(_dp), rel.ctypes.data_as(_dp), max_cycles)
+    return eps[:n], rel[:n]
+
+
+def calc_cross_powerspec(N, boxlen, f1, f2, bins, precision=FP64):
+    """f1, f2: host numpy complex arrays or DistributedGrid (device fbox)."""
+    L = load()
+    k = np.zeros(bins)
+    p = np.zeros(bins)
+    o = np.zeros(bins, np.int32)
+
+    def ptr(x, c):
+        if isinstance(x, DistributedGrid):
+            return ctypes.c_void_p(x.fbox)
+        x = np.ascontiguousarray(x, dtype=c)
+        ptr._keep.append(x)
+        return x.ctypes.data_as(ctypes.c_void_p)
+    ptr._keep = []
+    c = np.complex64 if precision == FP32 else np.complex128
+    fn = L.calc_cross_powerspec_float if precision == FP32 else L.calc_cross_powerspec
+    fn(N, ctypes.c_double(boxlen), ptr(f1, c), ptr(f2, c), bins, k.ctypes.data_as(_dp),
+       p.ctypes.data_as(_dp), o.ctypes.data_as(_ip))
+    return k, p, o
+
+
+# ---- perturbation table ----------------------------------------------------------------------
+class Spline:
+    """struct perturb_data + struct perturb_spline over a PerturbTable (arrays kept alive)."""
+
+    def __init__(self, table):
+        self.arrays = [np.ascontiguousarray(a, np.float64) for a in
+                       (table.delta, table.k, table.log_tau, table.redshift, table.D_growth,
+                        table.f_growth, table.H_Hubble)]
+        self.titles = (ctypes.c_char_p * table.n_functions)(*[t.encode() for t in table.titles])
+        d, k, lt, z, D, f, H = [a.ctypes.data_as(_dp) for a in self.arrays]
+        self.pd = PerturbData(table.k_size, table.tau_size, table.n_functions, d, k, lt, z, D, f, H,
+                              self.titles, None)
+        self.sp = PerturbSpline(ctypes.pointer(self.pd), None, 0)
+        self.table = table
+
+    def tau_params(self, z: float):
+        t = self.table
+        lt = np.interp(z, t.redshift[::-1], t.log_tau[::-1])
+        return lt
+
+
+def generatePerturbationGrid(cosmo: Cosmology, spline: Spline, grf, grid, title: str,
+                             rescale: float = 1.0):
+    _check(load().generatePerturbationGrid(ctypes.byref(cosmo), ctypes.byref(spline.sp),
+                                           ctypes.byref(grf), ctypes.byref(grid), title.encode(),
+                                           b"", ctypes.c_double(rescale)))
+
+
+def cic_deposit_dg(rho, pos: np.ndarray, mass: float) -> float:
+    pos = np.ascontiguousarray(pos, np.float32)
+    tot = ctypes.c_double()
+    _check(load().cic_deposit_dg(ctypes.byref(rho), pos.ctypes.data_as(_fp), ctypes.c_long(len(pos)),
+                                 ctypes.c_double(mass), ctypes.byref(tot)))
+    return tot.value
+
+
+# ---- fused pipeline --------------------------------------------------------------------------
+def ic_config(N, M, boxlen, seed, table, method=METHOD_2LPT, pk_bins=32, pk_linear=True,
+              precision=FP32, z_ini=31.0, ma_cycles=0, ma_tol=0.0, index_src=0) -> ICConfig:
+    return ICConfig(N, M, boxlen, seed, table.A_s, table.n_s, table.k_pivot, z_ini, index_src,
+                    method, ma_cycles, ma_tol, pk_bins, int(pk_linear), precision, 0)
+
+
+def ic_pipeline_run(cfg: ICConfig, spline: Spline, want_pos: bool = False) -> dict:
+    bins = cfg.pk_bins
+    k = np.zeros(bins)
+    p = np.zeros(bins)
+    o = np.zeros(bins, np.int64)
+    pos = np.zeros((cfg.M ** 3, 3), np.float32) if want_pos else None
+    res = ICResult(k.ctypes.data_as(_dp), p.ctypes.data_as(_dp), o.ctypes.data_as(_lp),
+                   pos.ctypes.data_as(_fp) if pos is not None else None, 0, 0.0)
+    _check(load().ic_pipeline_run(ctypes.byref(cfg), ctypes.byref(spline.sp), ctypes.byref(res)))
+    out = {"pk_k": k, "pk_p": p, "pk_obs": o, "ma_iterations": res.ma_iterations,
+           "ma_residual": res.ma_residual}
+    if pos is not None:
+        out["pos"] = pos
+    return out
+
+
+def stage_times() -> np.ndarray:
+    ms = np.zeros(16)
+    n = load().mitos_stage_times(ms.ctypes.data_as(_dp), 16)
+    return ms[:n]
+
+
+def timer_start() -> None:
+    _check(load().mitos_timer_start())
+
+
+def timer_stop() -> float:
+    return float(load().mitos_timer_stop())
+
+
+def kernel_timing(on: bool) -> None:
+    load().mitos_kernel_timing(int(on))
+
+
+def kernel_times(max_n: int = 4096):
+    names = (ctypes.c_char_p * max_n)()
+    ms = np.zeros(max_n)
+    n = load().mitos_kernel_times(names, ms.ctypes.data_as(_dp), max_n)
+    return [(names[i].decode(), float(ms[i])) for i in range(n)]

@@ -1,0 +1,50 @@
+"""Generate the golden vectors in tests/golden/ from the reference's own code.
+
+Runs the reference hot-path sources compiled by oracle/Makefile (`make -C oracle ref`,
+needs the reference tree) through oracle.ref_* and stores small fixtures:
+  xoshiro_draws.npz  rand_uint64 streams (include/random.h:27-33) for seeds 42, 7, 1000..1002
+  sample_norm.npz    sampleNorm streams (src/random.c:34-49)
+  grf.npz            generate_complex_grf + enforce_hermiticity at 16^3 and 32^3
+  pipeline.npz       positions and P(k) of src/mitos.c + analyse/src/mitos_read.c at 16^3 / 32^3
+Usage: python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import oracle  # noqa: E402
+from mitos_gb300.perturb import load_table  # noqa: E402
+
+
+def main():
+    oracle.build(ref=True)
+    assert oracle.ref_lib() is not None, "the reference build is required"
+    np.savez_compressed(os.path.join(HERE, "xoshiro_draws.npz"),
+                        **{f"seed_{s}": oracle.ref_draws(s, 4096) for s in (42, 7, 1000, 1001, 1002)})
+    np.savez_compressed(os.path.join(HERE, "sample_norm.npz"),
+                        **{f"seed_{s}": oracle.ref_norms(s, 4096) for s in (42, 7, 100)})
+    np.savez_compressed(os.path.join(HERE, "grf.npz"),
+                        **{f"grf_{N}_{s}": oracle.ref_grf(N, 256.0 * N / 64, s)
+                           for N, s in ((16, 42), (32, 7))})
+    table = load_table()
+    fx = {}
+    for N, seed, lpt, ma, lin in ((16, 42, 2, 0, 1), (32, 7, 2, 0, 0), (16, 42, 1, 0, 1),
+                                  (16, 42, 2, 3, 1)):
+        prm = oracle.ic_params(N, N, 256.0 * N / 64, seed, table, lpt_order=lpt, ma_cycles=ma,
+                               pk_bins=8, pk_linear=bool(lin))
+        out = oracle.ref_ic_pipeline(prm, want=("pos", "pk"))
+        name = f"p_{N}_{seed}_{lpt}_{ma}_{lin}"
+        fx[name + "_pos"] = out["pos"]
+        fx[name + "_obs"] = out["pk_obs"]
+        fx[name + "_pk"] = out["pk_p"]
+    np.savez_compressed(os.path.join(HERE, "pipeline.npz"), **fx)
+    print("golden vectors written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,66 @@
+"""GPU parity of the fused initial-condition pipeline against the oracle (the reference restated)
+and the FP32 precision study against the FP64 GPU path."""
+import numpy as np
+import pytest
+
+import oracle
+import mitos_gb300.lib as ml
+from conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _wrapdiff(a, b, L):
+    d = np.asarray(a, np.float64) - np.asarray(b, np.float64)
+    return d - L * np.round(d / L)
+
+
+@pytest.mark.parametrize("N,method,lin", [(32, ml.METHOD_2LPT, True), (32, ml.METHOD_ZELDOVICH, False),
+                                          (48, ml.METHOD_2LPT, True), (64, ml.METHOD_2LPT, True)])
+def test_pipeline_fp64_vs_oracle(N, method, lin, table, spline):
+    """64^3 / L = 256 / seed 42 / z = 31 / 32 linear shells is the reference CPU configuration."""
+    L = 256.0 * N / 64
+    bins = 32 if N == 64 else 12
+    cfg = ml.ic_config(N, N, L, 42, table, method=method, pk_bins=bins, pk_linear=lin, precision=ml.FP64)
+    out = ml.ic_pipeline_run(cfg, spline, want_pos=True)
+    ref = oracle.ic_pipeline(oracle.ic_params(N, N, L, 42, table, lpt_order=2 if method == ml.METHOD_2LPT else 1,
+                                              pk_bins=bins, pk_linear=lin), want=("pos", "pk"))
+    assert np.array_equal(out["pk_obs"], ref["pk_obs"])
+    ok = ref["pk_obs"] > 0
+    assert np.abs(out["pk_p"][ok] / ref["pk_p"][ok] - 1).max() < 1e-9
+    assert np.abs(out["pk_k"][ok] / ref["pk_k"][ok] - 1).max() < 1e-12
+    assert np.abs(_wrapdiff(out["pos"], ref["pos"], L)).max() < 1e-4
+
+
+def test_pipeline_ma_fp64_vs_oracle(table, spline):
+    N, L = 32, 128.0
+    cfg = ml.ic_config(N, N, L, 42, table, method=ml.METHOD_MONGE_AMPERE, pk_bins=12, pk_linear=True,
+                       precision=ml.FP64, ma_cycles=3)
+    out = ml.ic_pipeline_run(cfg, spline, want_pos=True)
+    ref = oracle.ic_pipeline(oracle.ic_params(N, N, L, 42, table, ma_cycles=3, pk_bins=12, pk_linear=True),
+                             want=("pos", "pk"))
+    assert out["ma_iterations"] == 3
+    ok = ref["pk_obs"] > 0
+    assert np.abs(out["pk_p"][ok] / ref["pk_p"][ok] - 1).max() < 1e-9
+    assert np.abs(_wrapdiff(out["pos"], ref["pos"], L)).max() < 1e-4
+
+
+@pytest.mark.parametrize("N,L,seed,bins", [(128, 250.0, 7, 64), (256, 500.0, 7, 128)])
+def test_precision_study_fp32_vs_fp64(N, L, seed, bins, table, spline):
+    """FP32 pipeline against the FP64 GPU path: P(k) per bin within 1e-4, displacement rms
+    relative error within 1e-5 (256^3, L = 500, seed 7, 128 shells is the precision-study config)."""
+    c64 = ml.ic_config(N, N, L, seed, table, pk_bins=bins, pk_linear=True, precision=ml.FP64)
+    c32 = ml.ic_config(N, N, L, seed, table, pk_bins=bins, pk_linear=True, precision=ml.FP32)
+    o64 = ml.ic_pipeline_run(c64, spline, want_pos=True)
+    o32 = ml.ic_pipeline_run(c32, spline, want_pos=True)
+    assert np.array_equal(o32["pk_obs"], o64["pk_obs"])
+    ok = o64["pk_obs"] > 0
+    perbin = np.abs(o32["pk_p"][ok] / o64["pk_p"][ok] - 1)
+    assert perbin.max() < 1e-4, perbin.max()
+    # displacement = lattice - position (mod L)
+    M = N
+    q = (np.indices((M, M, M)).reshape(3, -1).T * np.float32(L / M)).astype(np.float64)
+    d64 = _wrapdiff(q, o64["pos"], L)
+    d32 = _wrapdiff(q, o32["pos"], L)
+    rms = np.sqrt(np.mean((d32 - d64) ** 2)) / np.sqrt(np.mean(d64 ** 2))
+    assert rms < 1e-5, rms
