@@ -180,6 +180,8 @@ def main():
     ap.add_argument("--seed", type=int, default=42)
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--quick", action="store_true",
+                    help="timed steps only (no e2e, per-kernel timing or CPU baseline): the profiling run")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -242,6 +244,11 @@ def main():
         ms = float(t.item())
     ms_per_step = ms / args.steps
     value = ws * args.steps / (ms / 1e3)
+    if args.quick:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "ms_per_step": ms_per_step,
+                              "config": config(args), "clocks": clk, "quick": True}), flush=True)
+        return 0
 
     # e2e: positions to pinned host memory every step (the IC product), table up, P(k) down
     import torch
