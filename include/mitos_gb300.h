@@ -271,6 +271,18 @@ struct ic_result {
 int ic_pipeline_run(const struct ic_config *cfg, const struct perturb_spline *spline,
                     struct ic_result *res);
 /* The same on caller-provided host table arrays (convenience for bindings without structs). */
+/* P(k) binning that allocates no device memory.  No counterpart in the reference: for callers
+ * that must not allocate device memory in their loop, because another allocator already holds
+ * the device's memory or because cudaMalloc / cudaFree would synchronise a streaming pipeline.
+ * dev_box1 / dev_box2 are device complex grids (N*N*(N/2+1), FP64 or FP32 per `precision`);
+ * linear = 0 gives the reference log bins of calc_cross_powerspec, 1 linear shells to k_Nyquist.
+ * Scratch: a fixed device array for at most 4096 bins (96 KB, held by every GPU that loads the
+ * library until exit); more bins return status 3.  The array is shared by all calls and cleared
+ * by each: calls whose GPU work overlaps race.  The first call on a device looks up the array's
+ * address (cudaGetSymbolAddress); make it before any stream capture.  Outputs are host arrays. */
+int calc_cross_powerspec_noalloc(int N, double boxlen, const void *dev_box1, const void *dev_box2,
+                                 int precision, int bins, int linear, double *k_in_bins,
+                                 double *power_in_bins, long *obs_in_bins);
 int ic_pipeline_run_table(const struct ic_config *cfg, int k_size, int tau_size,
                           int n_functions, const double *k, const double *log_tau,
                           const double *redshift, const double *D_growth, const double *delta,
