@@ -81,8 +81,17 @@ bool make_plan(int n, int E, int tw_len, FFTPlan *pl) {
     if (rem != 1 || ns == 0 || ns >= MITOS_MAX_STAGES) return false;
     pl->n = n;
     pl->nst = ns;
-    for (int i = 0; i < ns; i++) pl->rad[i] = rad[i];
     pl->tw_scale = tw_len / n;
+    int Ns = 1;
+    for (int i = 0; i < ns; i++) {
+        pl->rad[i] = rad[i];
+        int lg = -1;
+        for (int b = 0; b < 31; b++)
+            if ((1 << b) == Ns) lg = b;
+        pl->lgNs[i] = lg;
+        pl->twstep[i] = n / (Ns * rad[i]) * pl->tw_scale;
+        Ns *= rad[i];
+    }
     return true;
 }
 
@@ -179,6 +188,29 @@ const void *window_table(int N, int order, int precision) {
     return d;
 }
 
+// Fourier transfer of the on-node TSC stencil (1/8, 3/4, 1/8): 3/4 + cos(2 pi m / N) / 4,
+// m = -N/2 .. N/2 stored at m + N/2
+static std::map<std::pair<int, int>, void *> g_stencils;
+const void *stencil_table(int N, int precision) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto key = std::make_pair(N, precision);
+    auto it = g_stencils.find(key);
+    if (it != g_stencils.end()) return it->second;
+    std::vector<double> w(N + 1);
+    for (int m = -N / 2; m <= N / 2; m++) w[m + N / 2] = 0.75 + 0.25 * cos(2.0 * M_PI * (double)m / (double)N);
+    void *d = nullptr;
+    if (precision == MITOS_FP32) {
+        std::vector<float> wf(w.begin(), w.end());
+        if (cudaMalloc(&d, sizeof(float) * (N + 1)) != cudaSuccess) return nullptr;
+        cudaMemcpy(d, wf.data(), sizeof(float) * (N + 1), cudaMemcpyHostToDevice);
+    } else {
+        if (cudaMalloc(&d, sizeof(double) * (N + 1)) != cudaSuccess) return nullptr;
+        cudaMemcpy(d, w.data(), sizeof(double) * (N + 1), cudaMemcpyHostToDevice);
+    }
+    g_stencils[key] = d;
+    return d;
+}
+
 // bin of each squared integer wavevector norm n2 in [0, 3 (N/2)^2]; -1 skips the mode
 static long isqrt_l(long a) {
     long r = (long)sqrt((double)a);
@@ -186,14 +218,23 @@ static long isqrt_l(long a) {
     while ((r + 1) * (r + 1) <= a) r++;
     return r;
 }
-static std::map<std::tuple<int, int, int, double>, int *> g_bins;
-const int *bin_table(int N, int bins, int linear, double boxlen) {
-    std::lock_guard<std::mutex> lk(g_mu);
-    auto key = std::make_tuple(N, bins, linear, linear ? 0.0 : boxlen);
+struct BinEntry {
+    int *dev = nullptr;
+    std::vector<int> host;
+    std::vector<double> ksum;        // sum over modes of multiplicity * |k| per bin
+    std::vector<long long> count;    // sum over modes of multiplicity per bin
+};
+static std::map<std::tuple<int, int, int, double>, BinEntry *> g_bins;
+static std::map<int, std::vector<long long>> g_n2hist;
+
+static BinEntry *bin_entry(int N, int bins, int linear, double boxlen) {
+    auto key = std::make_tuple(N, bins, linear, boxlen);
     auto it = g_bins.find(key);
     if (it != g_bins.end()) return it->second;
     const long n2max = 3L * (N / 2) * (N / 2);
-    std::vector<int> tab(n2max + 1, -1);
+    BinEntry *be = new BinEntry;
+    std::vector<int> &tab = be->host;
+    tab.assign(n2max + 1, -1);
     const double dk = 2 * M_PI / boxlen;
     const double max_k = sqrt(3) * dk * N / 2, min_k = dk;
     const double lmax = log(max_k), lmin = log(min_k);
@@ -210,11 +251,51 @@ const int *bin_table(int N, int bins, int linear, double boxlen) {
         }
         tab[n2] = (b >= 0 && b < bins) ? b : -1;
     }
-    int *d = nullptr;
-    if (cudaMalloc(&d, sizeof(int) * (n2max + 1)) != cudaSuccess) return nullptr;
-    cudaMemcpy(d, tab.data(), sizeof(int) * (n2max + 1), cudaMemcpyHostToDevice);
-    g_bins[key] = d;
-    return d;
+    if (cudaMalloc(&be->dev, sizeof(int) * (n2max + 1)) != cudaSuccess) {
+        cudaGetLastError();
+        delete be;
+        return nullptr;
+    }
+    cudaMemcpy(be->dev, tab.data(), sizeof(int) * (n2max + 1), cudaMemcpyHostToDevice);
+    // multiplicity-weighted mode count per n2 over the half-complex grid (weight 2 except on the
+    // kz = 0 and kz = N/2 planes, src/calc_powerspec.c:73-79), then per bin
+    auto &hist = g_n2hist[N];
+    if (hist.empty()) {
+        hist.assign(n2max + 1, 0);
+        for (int x = 0; x < N; x++) {
+            const long jx = x > N / 2 ? x - N : x;
+            for (int y = 0; y < N; y++) {
+                const long jy = y > N / 2 ? y - N : y;
+                const long b2 = jx * jx + jy * jy;
+                for (int z = 0; z <= N / 2; z++) hist[b2 + (long)z * z] += (z == 0 || z == N / 2) ? 1 : 2;
+            }
+        }
+    }
+    be->ksum.assign(bins, 0.0);
+    be->count.assign(bins, 0);
+    for (long n2 = 1; n2 <= n2max; n2++) {
+        const int b = tab[n2];
+        if (b < 0 || !hist[n2]) continue;
+        be->count[b] += hist[n2];
+        be->ksum[b] += (double)hist[n2] * sqrt((double)n2) * dk;
+    }
+    g_bins[key] = be;
+    return be;
+}
+
+const int *bin_table(int N, int bins, int linear, double boxlen) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    BinEntry *be = bin_entry(N, bins, linear, boxlen);
+    return be ? be->dev : nullptr;
+}
+
+int bin_geometry(int N, int bins, int linear, double boxlen, const double **ksum, const long long **count) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    BinEntry *be = bin_entry(N, bins, linear, boxlen);
+    if (!be) return 5;
+    *ksum = be->ksum.data();
+    *count = be->count.data();
+    return 0;
 }
 
 // ---- workspace: grid-sized device buffers reused across calls --------------------------
@@ -242,7 +323,9 @@ void release_all() {
     g_geoms.clear();
     for (auto &kv : g_windows) cudaFree(kv.second);
     g_windows.clear();
-    for (auto &kv : g_bins) cudaFree(kv.second);
+    for (auto &kv : g_stencils) cudaFree(kv.second);
+    g_stencils.clear();
+    for (auto &kv : g_bins) { cudaFree(kv.second->dev); delete kv.second; }
     g_bins.clear();
 }
 

@@ -6,7 +6,10 @@
 namespace mitos {
 
 const void *window_table(int N, int order, int precision);
+const void *stencil_table(int N, int precision);
 const int *bin_table(int N, int bins, int linear, double boxlen);
+// per-bin multiplicity-weighted mode counts and |k| sums of the half-complex grid (host arrays)
+int bin_geometry(int N, int bins, int linear, double boxlen, const double **ksum, const long long **count);
 // grid-sized scratch buffer number `slot` of `bytes` bytes (kept until mitos_release_all)
 void *workspace(size_t bytes, int slot);
 void release_all();

@@ -25,7 +25,20 @@ struct FFTPlan {
     int nst;                       // number of stages
     int rad[MITOS_MAX_STAGES];     // radices, first to last
     int tw_scale;                  // twiddle table length / n
+    int lgNs[MITOS_MAX_STAGES];    // log2 of the combined length before stage s, -1 if not 2^k
+    int twstep[MITOS_MAX_STAGES];  // n / (Ns R) * tw_scale: table stride of stage s
 };
+
+// j / Ns and j % Ns, by shifts when Ns is a power of two
+__device__ __forceinline__ void divmod_ns(int j, int Ns, int lg, int &q, int &r) {
+    if (lg >= 0) {
+        q = j >> lg;
+        r = j & (Ns - 1);
+    } else {
+        q = j / Ns;
+        r = j - q * Ns;
+    }
+}
 
 // unnormalised R-point DFT in registers; SIGN = -1 forward, +1 backward
 template <typename T, int SIGN> __device__ __forceinline__ void dft2(cplx<T> &a, cplx<T> &b) {
@@ -101,12 +114,13 @@ __device__ __forceinline__ void stage_first(cplx<T> *v) {
 // write stage outputs to shared memory (layout: element n of pencil at sm[spad(n)*sn])
 template <typename T, int E, int R>
 __device__ __forceinline__ void stage_write(const cplx<T> *v, cplx<T> *sm, int sn, int n, int t,
-                                            int Ns) {
+                                            int Ns, int lg) {
 #pragma unroll
     for (int b = 0; b < E / R; b++) {
         int j = t + b * (n / E);
-        int jm = j % Ns;
-        int idxD = (j / Ns) * Ns * R + jm;
+        int jd, jm;
+        divmod_ns(j, Ns, lg, jd, jm);
+        int idxD = jd * Ns * R + jm;
 #pragma unroll
         for (int r = 0; r < R; r++) sm[spad(idxD + r * Ns) * sn] = v[b * R + r];
     }
@@ -115,13 +129,14 @@ __device__ __forceinline__ void stage_write(const cplx<T> *v, cplx<T> *sm, int s
 // read stage inputs from shared memory, apply twiddles and the radix-R DFT
 template <typename T, int E, int R, int SIGN>
 __device__ __forceinline__ void stage_read_dft(cplx<T> *v, const cplx<T> *sm, int sn, int n, int t,
-                                               int Ns, const cplx<T> *__restrict__ tw,
-                                               int tw_scale) {
+                                               int Ns, int lg, const cplx<T> *__restrict__ tw,
+                                               int twstep) {
 #pragma unroll
     for (int b = 0; b < E / R; b++) {
         int j = t + b * (n / E);
-        int jm = j % Ns;
-        int step = jm * (n / (Ns * R)) * tw_scale;
+        int jd, jm;
+        divmod_ns(j, Ns, lg, jd, jm);
+        int step = jm * twstep;
 #pragma unroll
         for (int r = 0; r < R; r++) {
             cplx<T> x = sm[spad(j + r * (n / R)) * sn];
@@ -146,20 +161,20 @@ __device__ __forceinline__ void first_dispatch(int R, cplx<T> *v) {
 
 template <typename T, int E>
 __device__ __forceinline__ void write_dispatch(int R, const cplx<T> *v, cplx<T> *sm, int sn, int n,
-                                               int t, int Ns) {
-    if constexpr (E % 8 == 0) { if (R == 8) { stage_write<T, E, 8>(v, sm, sn, n, t, Ns); return; } }
-    if constexpr (E % 4 == 0) { if (R == 4) { stage_write<T, E, 4>(v, sm, sn, n, t, Ns); return; } }
-    if constexpr (E % 3 == 0) { if (R == 3) { stage_write<T, E, 3>(v, sm, sn, n, t, Ns); return; } }
-    if constexpr (E % 2 == 0) { if (R == 2) { stage_write<T, E, 2>(v, sm, sn, n, t, Ns); return; } }
+                                               int t, int Ns, int lg) {
+    if constexpr (E % 8 == 0) { if (R == 8) { stage_write<T, E, 8>(v, sm, sn, n, t, Ns, lg); return; } }
+    if constexpr (E % 4 == 0) { if (R == 4) { stage_write<T, E, 4>(v, sm, sn, n, t, Ns, lg); return; } }
+    if constexpr (E % 3 == 0) { if (R == 3) { stage_write<T, E, 3>(v, sm, sn, n, t, Ns, lg); return; } }
+    if constexpr (E % 2 == 0) { if (R == 2) { stage_write<T, E, 2>(v, sm, sn, n, t, Ns, lg); return; } }
 }
 
 template <typename T, int E, int SIGN>
 __device__ __forceinline__ void read_dispatch(int R, cplx<T> *v, const cplx<T> *sm, int sn, int n,
-                                              int t, int Ns, const cplx<T> *tw, int tws) {
-    if constexpr (E % 8 == 0) { if (R == 8) { stage_read_dft<T, E, 8, SIGN>(v, sm, sn, n, t, Ns, tw, tws); return; } }
-    if constexpr (E % 4 == 0) { if (R == 4) { stage_read_dft<T, E, 4, SIGN>(v, sm, sn, n, t, Ns, tw, tws); return; } }
-    if constexpr (E % 3 == 0) { if (R == 3) { stage_read_dft<T, E, 3, SIGN>(v, sm, sn, n, t, Ns, tw, tws); return; } }
-    if constexpr (E % 2 == 0) { if (R == 2) { stage_read_dft<T, E, 2, SIGN>(v, sm, sn, n, t, Ns, tw, tws); return; } }
+                                              int t, int Ns, int lg, const cplx<T> *tw, int tws) {
+    if constexpr (E % 8 == 0) { if (R == 8) { stage_read_dft<T, E, 8, SIGN>(v, sm, sn, n, t, Ns, lg, tw, tws); return; } }
+    if constexpr (E % 4 == 0) { if (R == 4) { stage_read_dft<T, E, 4, SIGN>(v, sm, sn, n, t, Ns, lg, tw, tws); return; } }
+    if constexpr (E % 3 == 0) { if (R == 3) { stage_read_dft<T, E, 3, SIGN>(v, sm, sn, n, t, Ns, lg, tw, tws); return; } }
+    if constexpr (E % 2 == 0) { if (R == 2) { stage_read_dft<T, E, 2, SIGN>(v, sm, sn, n, t, Ns, lg, tw, tws); return; } }
 }
 
 // Transform the pencils of a thread block.  v holds the stage-1 inputs on entry and the
@@ -171,11 +186,13 @@ __device__ __forceinline__ void fft_regs(const FFTPlan &pl, cplx<T> *v, cplx<T> 
     const int n = pl.n;
     first_dispatch<T, E, SIGN>(pl.rad[0], v);
     int Ns = pl.rad[0];
+    int Nsp = 1;
     for (int s = 1; s < pl.nst; s++) {
-        write_dispatch<T, E>(pl.rad[s - 1], v, sm, sn, n, t, Ns / pl.rad[s - 1]);
+        write_dispatch<T, E>(pl.rad[s - 1], v, sm, sn, n, t, Nsp, pl.lgNs[s - 1]);
         __syncthreads();
-        read_dispatch<T, E, SIGN>(pl.rad[s], v, sm, sn, n, t, Ns, tw, pl.tw_scale);
+        read_dispatch<T, E, SIGN>(pl.rad[s], v, sm, sn, n, t, Ns, pl.lgNs[s], tw, pl.twstep[s]);
         __syncthreads();
+        Nsp = Ns;
         Ns *= pl.rad[s];
     }
 }

@@ -12,7 +12,7 @@ template <> __device__ __forceinline__ double dev_sqrt<double>(double x) { retur
 // p fastest so that a warp reads P consecutive columns of each row.
 // ------------------------------------------------------------------------------------------
 template <typename T, int E, int SIGN, int AXIS, int OP>
-__global__ void __launch_bounds__(512) k_strided(GridGeom g, PassArgs a, const T *__restrict__ win) {
+__global__ void __launch_bounds__(512, 2) k_strided(GridGeom g, PassArgs a, const T *__restrict__ win) {
     extern __shared__ __align__(16) unsigned char smraw[];
     cplx<T> *sm = reinterpret_cast<cplx<T> *>(smraw);
     const FFTPlan &pl = g.plN;
@@ -46,19 +46,15 @@ __global__ void __launch_bounds__(512) k_strided(GridGeom g, PassArgs a, const T
     const T scale = (T)a.scale;
     cplx<T> *psm = sm + p;
 
-    // per-block P(k) accumulators live behind the FFT exchange buffer
-    T *hk = nullptr, *hp = nullptr;
-    int *hn = nullptr;
+    // P(k): one power histogram per warp behind the FFT exchange buffer (the counts and the
+    // wavenumber sums of the bins depend only on the geometry and are tabulated on the host)
+    T *hp = nullptr;
     if constexpr (OP == XOP_PK) {
         size_t off = (size_t)P * spad_len(N) * sizeof(cplx<T>);
-        hk = reinterpret_cast<T *>(smraw + off);
-        hp = hk + a.nbins;
-        hn = reinterpret_cast<int *>(hp + a.nbins);
-        for (int i = tid; i < a.nbins; i += blockDim.x) {
-            hk[i] = 0;
-            hp[i] = 0;
-            hn[i] = 0;
-        }
+        T *hist = reinterpret_cast<T *>(smraw + off);
+        const int nw = blockDim.x >> 5;
+        for (int i = tid; i < a.nbins * nw; i += blockDim.x) hist[i] = 0;
+        hp = hist + (tid >> 5) * a.nbins;
         __syncthreads();
     }
 
@@ -94,6 +90,13 @@ __global__ void __launch_bounds__(512) k_strided(GridGeom g, PassArgs a, const T
 #pragma unroll 1
         for (int m = 0; m < nout; m++) {
             const int fac = facs[m];
+            // on-node TSC stencil of the displacement passes, applied to the k-space input:
+            // x for the d_x chain (X output 1), y for the d_x and d_y chains (Y outputs 0, 1)
+            const T *stn = nullptr;
+            if constexpr ((AXIS == 0 && OP == XOP_DISP) || (AXIS == 1 && OP == YOP_DISP)) {
+                if ((AXIS == 0 && outs[m] == 1) || (AXIS == 1 && outs[m] <= 1))
+                    stn = reinterpret_cast<const T *>(a.stencil);
+            }
 #pragma unroll
             for (int e = 0; e < E; e++) {
                 cplx<T> x = raw[e];
@@ -101,6 +104,7 @@ __global__ void __launch_bounds__(512) k_strided(GridGeom g, PassArgs a, const T
                     T kk = (T)kint(n_in(pl, E, t, e), N) * dk;
                     x = (fac == 1) ? cmul_is<T>(x, kk) : cscale<T>(x, -kk * kk);
                 }
+                if (stn) x = cscale<T>(x, stn[kint(n_in(pl, E, t, e), N) + N / 2]);
                 v[e] = x;
             }
             fft_regs<T, E, SIGN>(pl, v, psm, P, t, tw);
@@ -119,10 +123,8 @@ __global__ void __launch_bounds__(512) k_strided(GridGeom g, PassArgs a, const T
                         if (win) r = cscale<T>(r, win[jx + N / 2] * win[iy + N / 2] * win[iz + N / 2]);
                         int bin = a.bin_of_n2[n2];
                         if (bin >= 0) {
-                            const int mult = (iz == 0 || iz == N / 2) ? 1 : 2;
-                            atomicAdd(hk + bin, (T)mult * dev_sqrt<T>((T)n2) * dk);
-                            atomicAdd(hp + bin, (T)mult * (r.x * r.x + r.y * r.y));
-                            atomicAdd(hn + bin, mult);
+                            const T mult = (iz == 0 || iz == N / 2) ? (T)1 : (T)2;
+                            atomicAdd(hp + bin, mult * (r.x * r.x + r.y * r.y));
                         }
                         if (a.out[0]) dst[idx] = r;
                     } else {
@@ -147,16 +149,83 @@ __global__ void __launch_bounds__(512) k_strided(GridGeom g, PassArgs a, const T
     }
     if constexpr (OP == XOP_PK) {
         __syncthreads();
+        const size_t off = (size_t)P * spad_len(N) * sizeof(cplx<T>);
+        const T *hist = reinterpret_cast<const T *>(smraw + off);
+        const int nw = blockDim.x >> 5;
         for (int i = tid; i < a.nbins; i += blockDim.x) {
-            if (hn[i]) {
-                atomicAdd(a.bin_k + i, (double)hk[i]);
-                atomicAdd(a.bin_p + i, (double)hp[i]);
-                atomicAdd((unsigned long long *)a.bin_n + i, (unsigned long long)hn[i]);
-            }
+            double sum = 0;
+            for (int w = 0; w < nw; w++) sum += (double)hist[w * a.nbins + i];
+            if (sum != 0) atomicAdd(a.bin_p + i, sum);
         }
     }
 }
 
+
+// ------------------------------------------------------------------------------------------
+// X pass that closes the 2LPT potential and opens the displacement grids in one sweep:
+// forward FFT of the source spectrum, phi = (f1 phi1 - f2 S/k^2) / W_TSC, then the inverse
+// FFTs of phi and i kx phi (with the on-node stencil of the d_x chain when requested).
+// ------------------------------------------------------------------------------------------
+template <typename T, int E>
+__global__ void __launch_bounds__(512, 2) k_x_combine_disp(GridGeom g, PassArgs a, const T *__restrict__ win) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    cplx<T> *sm = reinterpret_cast<cplx<T> *>(smraw);
+    const FFTPlan &pl = g.plN;
+    const int P = g.P_xy;
+    const int tid = threadIdx.x, p = tid % P, t = tid / P;
+    const int N = g.N, H = g.H;
+    long col = (long)blockIdx.x * P + p;
+    const bool valid = col < g.plane;
+    if (!valid) col = 0;
+    const int iy = kint((int)(col / H), N), iz = (int)(col % H);
+    const cplx<T> *tw = reinterpret_cast<const cplx<T> *>(g.twN);
+    const T dk = (T)a.dk, scale = (T)a.scale, f1 = (T)a.f1, f2 = (T)a.f2;
+    const T *stn = reinterpret_cast<const T *>(a.stencil);
+    cplx<T> *psm = sm + p;
+    const cplx<T> *src = reinterpret_cast<const cplx<T> *>(a.in[0]);
+    const cplx<T> *phi1 = reinterpret_cast<const cplx<T> *>(a.in2);
+    cplx<T> v[E];
+#pragma unroll
+    for (int e = 0; e < E; e++) v[e] = valid ? src[col + (long)n_in(pl, E, t, e) * g.plane] : mk<T>(0, 0);
+    fft_regs<T, E, -1>(pl, v, psm, P, t, tw);
+    const T wyz = win ? win[iy + N / 2] * win[iz + N / 2] : (T)1;
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+        const int n = n_out(pl, E, t, e);
+        const int jx = kint(n, N);
+        const long n2 = (long)jx * jx + (long)iy * iy + (long)iz * iz;
+        const T G = (n2 > 0) ? (T)-1 / ((T)n2 * dk * dk) : (T)1;
+        const cplx<T> q = valid ? phi1[col + (long)n * g.plane] : mk<T>(0, 0);
+        const cplx<T> r = cscale<T>(v[e], scale);
+        cplx<T> o = mk<T>(f1 * q.x + f2 * G * r.x, f1 * q.y + f2 * G * r.y);
+        if (win) o = cscale<T>(o, win[jx + N / 2] * wyz);
+        psm[spad(n) * P] = o;
+    }
+    __syncthreads();
+    cplx<T> phi[E];
+#pragma unroll
+    for (int e = 0; e < E; e++) phi[e] = psm[spad(n_in(pl, E, t, e)) * P];
+    __syncthreads();
+#pragma unroll 1
+    for (int m = 0; m < 2; m++) {
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+            cplx<T> x = phi[e];
+            if (m == 1) {
+                const int jx = kint(n_in(pl, E, t, e), N);
+                x = cmul_is<T>(x, (T)jx * dk);
+                if (stn) x = cscale<T>(x, stn[jx + N / 2]);
+            }
+            v[e] = x;
+        }
+        fft_regs<T, E, 1>(pl, v, psm, P, t, tw);
+        if (valid) {
+            cplx<T> *dst = reinterpret_cast<cplx<T> *>(a.out[m]);
+#pragma unroll
+            for (int e = 0; e < E; e++) dst[col + (long)n_out(pl, E, t, e) * g.plane] = v[e];
+        }
+    }
+}
 // ------------------------------------------------------------------------------------------
 // Z c2r: rows of N/2+1 complex -> N reals via an N/2-point complex inverse FFT.
 // ------------------------------------------------------------------------------------------
@@ -177,14 +246,22 @@ __global__ void __launch_bounds__(256) k_z_c2r(GridGeom g, PassArgs a) {
     cplx<T> *psm = sm + (long)p * spad_len(h);
 
     constexpr int NIN = (OP == ZOP_C2R) ? 1 : (OP == ZOP_DISP) ? 3 : 6;
-    cplx<T> o[NIN][E];
+    // inputs of the Hessian passes are [xx, xy, xz, yy, yz, zz]; the 2LPT source is accumulated
+    // in the reference's term order (src/2lpt.c:111-112): zz yy + zz xx + yy xx - xy^2 - yz^2 - xz^2
+    constexpr int ORDER_2LPT[6] = {0, 3, 5, 1, 4, 2};
+    constexpr int NKEEP = (OP == ZOP_HESS_MA) ? 6 : (OP == ZOP_HESS_2LPT) ? 2 : 1;
+    cplx<T> o[NKEEP][E];
+    cplx<T> acc[E];
+    T *dst_row = nullptr;
 #pragma unroll
-    for (int f = 0; f < NIN; f++) {
+    for (int q = 0; q < NIN; q++) {
+        const int f = (OP == ZOP_HESS_2LPT) ? ORDER_2LPT[q] : q;
         // kz factor of input f: 0 -> 1, 1 -> i kz, 2 -> -kz^2
         int fac = 0;
         if (OP == ZOP_HESS_2LPT || OP == ZOP_HESS_MA) fac = (f == 2 || f == 4) ? 1 : (f == 5 ? 2 : 0);
         if (OP == ZOP_DISP) fac = (f == 2) ? 1 : 0;
         const cplx<T> *src = reinterpret_cast<const cplx<T> *>(a.in[f]) + row * H;
+        cplx<T> v[E];
 #pragma unroll
         for (int e = 0; e < E; e++) {
             const int k = n_in(pl, E, t, e);
@@ -194,29 +271,60 @@ __global__ void __launch_bounds__(256) k_z_c2r(GridGeom g, PassArgs a) {
                 if (fac == 1) { X = cmul_is<T>(X, k1); Y = cmul_is<T>(Y, k2); }
                 else { X = cscale<T>(X, -k1 * k1); Y = cscale<T>(Y, -k2 * k2); }
             }
+            if constexpr (OP == ZOP_DISP) {
+                const T *stn = reinterpret_cast<const T *>(a.stencil);
+                if (stn) { X = cscale<T>(X, stn[k + N / 2]); Y = cscale<T>(Y, stn[h - k + N / 2]); }
+            }
             if (k == 0) { X.y = 0; Y.y = 0; }
             // E' = X + conj(Y), O' = (X - conj(Y)) e^{+2 pi i k / N}, Z = E' + i O'
             const cplx<T> w = __ldg(tw + k);  // exp(-2 pi i k / N)
             const cplx<T> Ep = mk<T>(X.x + Y.x, X.y - Y.y);
             const cplx<T> D = mk<T>(X.x - Y.x, X.y + Y.y);
             const cplx<T> Op = mk<T>(D.x * w.x + D.y * w.y, D.y * w.x - D.x * w.y);
-            o[f][e] = mk<T>(Ep.x - Op.y, Ep.y + Op.x);
+            v[e] = mk<T>(Ep.x - Op.y, Ep.y + Op.x);
         }
-        fft_regs<T, E, 1>(pl, o[f], psm, 1, t, tw);
-    }
-    if (!valid) return;
-    if constexpr (OP == ZOP_C2R || OP == ZOP_DISP) {
+        fft_regs<T, E, 1>(pl, v, psm, 1, t, tw);
+        if constexpr (OP == ZOP_C2R || OP == ZOP_DISP) {
+            if (valid) {
+                T *dst = reinterpret_cast<T *>(a.out[f]) + row * a.rp_out;
 #pragma unroll
-        for (int f = 0; f < NIN; f++) {
-            T *dst = reinterpret_cast<T *>(a.out[f]) + row * a.rp_out;
+                for (int e = 0; e < E; e++) {
+                    const int n = n_out(pl, E, t, e);
+                    *reinterpret_cast<cplx<T> *>(dst + 2 * n) = cscale<T>(v[e], scale);
+                }
+                if (t == 0 && a.rp_out > N) { dst[N] = 0; dst[N + 1] = 0; }
+            }
+        } else if constexpr (OP == ZOP_HESS_2LPT) {
 #pragma unroll
             for (int e = 0; e < E; e++) {
-                const int n = n_out(pl, E, t, e);
-                *reinterpret_cast<cplx<T> *>(dst + 2 * n) = cscale<T>(o[f][e], scale);
+                const cplx<T> x = cscale<T>(v[e], scale);
+                if (q == 0) o[0][e] = x;  // xx
+                else if (q == 1) o[1][e] = x;  // yy
+                else if (q == 2) {  // zz: zz yy + zz xx + yy xx
+                    acc[e] = mk<T>(x.x * o[1][e].x + x.x * o[0][e].x + o[1][e].x * o[0][e].x,
+                                   x.y * o[1][e].y + x.y * o[0][e].y + o[1][e].y * o[0][e].y);
+                } else {  // - xy^2, - yz^2, - xz^2
+                    acc[e] = mk<T>(acc[e].x - x.x * x.x, acc[e].y - x.y * x.y);
+                }
             }
-            if (t == 0 && a.rp_out > N) { dst[N] = 0; dst[N + 1] = 0; }
+        } else {
+#pragma unroll
+            for (int e = 0; e < E; e++) o[f][e] = v[e];
         }
-    } else {
+    }
+    (void)dst_row;
+    if (!valid) return;
+    if constexpr (OP == ZOP_HESS_2LPT) {
+        T *dst = reinterpret_cast<T *>(a.out[0]) + row * a.rp_out;
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+            const int n = n_out(pl, E, t, e);
+            *reinterpret_cast<cplx<T> *>(dst + 2 * n) = acc[e];
+        }
+        if (t == 0 && a.rp_out > N) { dst[N] = 0; dst[N + 1] = 0; }
+        return;
+    }
+    if constexpr (OP == ZOP_HESS_MA) {
         T *dst = reinterpret_cast<T *>(a.out[0]) + row * a.rp_out;
         double sres = 0, srho = 0;
         const T *rho = (OP == ZOP_HESS_MA) ? reinterpret_cast<const T *>(a.in2) + row * a.rp_in : nullptr;
@@ -313,7 +421,7 @@ static int launch_strided_e(const GridGeom &g, const PassArgs &a, const T *win) 
     const int P = g.P_xy;
     const int threads = P * (g.N / E);
     size_t smem = (size_t)P * spad_len(g.N) * sizeof(cplx<T>);
-    if (OP == XOP_PK && AXIS == 0) smem += (size_t)a.nbins * (2 * sizeof(T) + sizeof(int));
+    if (OP == XOP_PK && AXIS == 0) smem += (size_t)a.nbins * (threads / 32) * sizeof(T);
     long blocks = (AXIS == 0) ? (g.plane + P - 1) / P : (long)g.N * ((g.H + P - 1) / P);
     auto kern = k_strided<T, E, SIGN, AXIS, OP>;
     if (smem > 48 * 1024) MITOS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -343,6 +451,25 @@ template <typename T> int launch_x(const GridGeom &g, XOp op, int sign, const Pa
     case XOP_COMBINE_2LPT: return launch_strided<T, -1, 0, XOP_COMBINE_2LPT>(g, a, win);
     case XOP_ADD_POISSON: return launch_strided<T, -1, 0, XOP_ADD_POISSON>(g, a, win);
     case XOP_PK: return launch_strided<T, -1, 0, XOP_PK>(g, a, win);
+    case XOP_COMBINE_DISP: {
+        const int P = g.P_xy;
+        const int threads = P * (g.N / g.E);
+        const size_t smem = (size_t)P * spad_len(g.N) * sizeof(cplx<T>);
+        const long blocks = (g.plane + P - 1) / P;
+        launch_begin("x_combine_disp");
+        if (g.E == 8) {
+            auto kern = k_x_combine_disp<T, 8>;
+            if (smem > 48 * 1024) MITOS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            kern<<<(unsigned)blocks, threads, smem, stream()>>>(g, a, win);
+        } else {
+            auto kern = k_x_combine_disp<T, 12>;
+            if (smem > 48 * 1024) MITOS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            kern<<<(unsigned)blocks, threads, smem, stream()>>>(g, a, win);
+        }
+        count_launch();
+        MITOS_LAUNCH_CHECK("x combine + displacement pass");
+        return 0;
+    }
     }
     return 3;
 }

@@ -34,7 +34,10 @@ enum XOp {
     XOP_DISP,         // out0..1 = FFT(phi), FFT(i kx phi)                           (inverse)
     XOP_COMBINE_2LPT, // out = [f1 * in2 + f2 * G(k) * FFT(in) * scale] * W(k)       (forward)
     XOP_ADD_POISSON,  // out = in2 + G(k) * FFT(in) * scale                          (forward)
-    XOP_PK            // P(k) binning of |FFT(in) * scale * W(k)|^2 (+ optional out)  (forward)
+    XOP_PK,           // P(k) binning of |FFT(in) * scale * W(k)|^2 (+ optional out)  (forward)
+    XOP_COMBINE_DISP  // phi = [f1 * in2 + f2 * G(k) * FFT(in) * scale] * W(k) (forward), then
+                      // out0..1 = FFT^-1(phi), FFT^-1(i kx phi) (inverse): the 2LPT potential never
+                      // leaves the block
 };
 enum YOp {
     YOP_PLAIN = 0,    // out = FFT(in) * scale
@@ -63,6 +66,10 @@ struct PassArgs {
     int nbins;
     double *bin_k, *bin_p; long long *bin_n;  // device accumulators
     double *red;          // device FP64 reductions (ZOP_HESS_MA: [0] += res^2, [1] += rho^2)
+    // displacement passes: fold the on-node TSC interpolation stencil (1/8, 3/4, 1/8) into the
+    // axes along which the later gather sits on grid nodes (x for d_x, y for d_x and d_y, z for
+    // all three); table of 3/4 + cos(2 pi m / N)/4 at m + N/2
+    const void *stencil;
 };
 
 template <typename T> int launch_x(const GridGeom &g, XOp op, int sign, const PassArgs &a);

@@ -242,10 +242,12 @@ __device__ __forceinline__ float gauss32(uint64_t A, uint64_t B) {
         const float t = (__ull2float_rn(~A) + 0.5f) * inv64;
         lnu = log1pf(-t);
     } else {
-        lnu = logf((__ull2float_rn(A) + 0.5f) * inv64);
+        // u < 1/2: |ln u| >= ln 2, so the hardware log2 keeps full relative precision
+        lnu = __logf((__ull2float_rn(A) + 0.5f) * inv64);
     }
-    const float v = (__ull2float_rn(B) + 0.5f) * inv64;
-    return sqrtf(-2.f * lnu) * cospif(2.f * v);
+    // cos(2 pi v) = -cos(2 pi (v - 1/2)), argument in (-pi, pi) for the hardware cosine
+    const float w = ((float)(long long)(B - 0x8000000000000000ULL) + 0.5f) * inv64;
+    return -sqrtf(-2.f * lnu) * __cosf(6.28318530717958647692f * w);
 }
 
 template <typename T> __device__ __forceinline__ T gauss(uint64_t A, uint64_t B);

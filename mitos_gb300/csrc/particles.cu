@@ -16,10 +16,36 @@ namespace mitos {
 template <typename T> __device__ __forceinline__ T dfloor(T x);
 template <> __device__ __forceinline__ float dfloor<float>(float x) { return floorf(x); }
 template <> __device__ __forceinline__ double dfloor<double>(double x) { return floor(x); }
+template <typename T> __device__ __forceinline__ int ifloor(T x);
+template <> __device__ __forceinline__ int ifloor<float>(float x) { return __float2int_rd(x); }
+template <> __device__ __forceinline__ int ifloor<double>(double x) { return __double2int_rd(x); }
+
+// CIC region accumulators: 32-bit fixed point with 2^23 per mean density in FP32 (native
+// integer shared atomics; exact, order independent), doubles in FP64
+template <typename T> struct RegAcc;
+template <> struct RegAcc<float> {
+    using type = unsigned int;
+    static __device__ __forceinline__ void add(unsigned int *c, float w) { atomicAdd(c, (unsigned int)__float2uint_rn(w * 8388608.f)); }
+    static __device__ __forceinline__ float value(unsigned int c) { return (float)c * (1.f / 8388608.f); }
+};
+template <> struct RegAcc<double> {
+    using type = double;
+    static __device__ __forceinline__ void add(double *c, double w) { atomicAdd(c, w); }
+    static __device__ __forceinline__ double value(double c) { return c; }
+};
 
 __device__ __forceinline__ int wrapi(int i, int N) {
     i %= N;
     return i < 0 ? i + N : i;
+}
+
+// periodic index for the small offsets of the interpolation stencils, with the general
+// modulo kept for anything further out (non-finite positions included)
+__device__ __forceinline__ int wrapn(int i, int N) {
+    i += (i < 0) ? N : 0;
+    i -= (i >= N) ? N : 0;
+    if ((unsigned)i >= (unsigned)N) i = wrapi(i, N);
+    return i;
 }
 
 // TSC interpolation at grid coordinates (Xg, Yg, Zg) of a padded real grid:
@@ -33,18 +59,22 @@ __device__ __forceinline__ T tsc_gather(const T *__restrict__ box, int N, T Xg, 
     wx[0] = half * (half - dx) * (half - dx); wx[1] = (T)0.75 - dx * dx; wx[2] = half * (half + dx) * (half + dx);
     wy[0] = half * (half - dy) * (half - dy); wy[1] = (T)0.75 - dy * dy; wy[2] = half * (half + dy) * (half + dy);
     wz[0] = half * (half - dz) * (half - dz); wz[1] = (T)0.75 - dz * dz; wz[2] = half * (half + dz) * (half + dz);
-    int zi[3];
+    int zi[3], yi[3], xi[3];
 #pragma unroll
-    for (int k = 0; k < 3; k++) zi[k] = wrapi(nz - 1 + k, N);
+    for (int k = 0; k < 3; k++) {
+        zi[k] = wrapn(nz - 1 + k, N);
+        yi[k] = wrapn(ny - 1 + k, N);
+        xi[k] = wrapn(nx - 1 + k, N);
+    }
     const long rp = N + 2;
     T sum = 0;
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-        const long xo = (long)wrapi(nx - 1 + i, N) * N;
+        const long xo = (long)xi[i] * N;
         T sy = 0;
 #pragma unroll
         for (int j = 0; j < 3; j++) {
-            const T *row = box + (xo + wrapi(ny - 1 + j, N)) * rp;
+            const T *row = box + (xo + yi[j]) * rp;
             const T sz = wz[0] * __ldg(row + zi[0]) + wz[1] * __ldg(row + zi[1]) + wz[2] * __ldg(row + zi[2]);
             sy += wy[j] * sz;
         }
@@ -99,9 +129,9 @@ k_displace_cic(int N, int M, float spacing, T boxlen, T gfac, T val,
     const T dx = X - iX, dy = Y - iY, dz = Z - iZ;
     const T tx = 1 - dx, ty = 1 - dy, tz = 1 - dz;
     const long rp = N + 2;
-    const int x0 = wrapi(iX, N), x1 = wrapi(iX + 1, N);
-    const int y0 = wrapi(iY, N), y1 = wrapi(iY + 1, N);
-    const int z0 = wrapi(iZ, N), z1 = wrapi(iZ + 1, N);
+    const int x0 = wrapn(iX, N), x1 = wrapn(iX + 1, N);
+    const int y0 = wrapn(iY, N), y1 = wrapn(iY + 1, N);
+    const int z0 = wrapn(iZ, N), z1 = wrapn(iZ + 1, N);
     atomicAdd(rho + ((long)x0 * N + y0) * rp + z0, val * tx * ty * tz);
     atomicAdd(rho + ((long)x1 * N + y0) * rp + z0, val * dx * ty * tz);
     atomicAdd(rho + ((long)x0 * N + y1) * rp + z0, val * tx * dy * tz);
@@ -110,6 +140,251 @@ k_displace_cic(int N, int M, float spacing, T boxlen, T gfac, T val,
     atomicAdd(rho + ((long)x1 * N + y0) * rp + z1, val * dx * ty * dz);
     atomicAdd(rho + ((long)x0 * N + y1) * rp + z1, val * tx * dy * dz);
     atomicAdd(rho + ((long)x1 * N + y1) * rp + z1, val * dx * dy * dz);
+}
+
+// ---- lattice-aligned fast path ------------------------------------------------------------
+// When M = N and every lattice coordinate i * spacing maps exactly onto grid node i, the TSC
+// gather of direction 0 sits on nodes in x, y, z; direction 1 on nodes in y, z; direction 2 on
+// nodes in z.  The displacement passes fold the stencil of those axes into the grids (exact in
+// exact arithmetic), so the gathers read 1, 3 and 9 values.  The CIC deposit of a brick of
+// particles accumulates in shared memory (one halo cell each side) and is flushed with
+// atomics; deposits that land outside the brick's region go straight to global memory.
+#define LB_X 8
+#define LB_Y 8
+#define LB_Z 32
+#define LB_THREADS 512
+#define LR_X (LB_X + 2)
+#define LR_Y (LB_Y + 2)
+#define LR_Z (LB_Z + 8)   // z halo of 4 each side keeps the flushed rows 16-byte aligned
+#define LR_Z0 4           // region z index of the brick's first cell
+
+template <typename T>
+__device__ __forceinline__ void tsc_w(T d, T *w) {
+    const T half = (T)0.5;
+    w[0] = half * (half - d) * (half - d);
+    w[1] = (T)0.75 - d * d;
+    w[2] = half * (half + d) * (half + d);
+}
+
+// deposit of one particle outside its brick's shared region (rare): straight to global memory
+template <typename T>
+__device__ __noinline__ void cic_global(T *rho, int N, int rp, int iX, int iY, int iZ, T dx, T dy, T dz) {
+    const T wx[2] = {1 - dx, dx}, wy[2] = {1 - dy, dy}, wz[2] = {1 - dz, dz};
+#pragma unroll 1
+    for (int a = 0; a < 2; a++)
+        for (int b = 0; b < 2; b++)
+            for (int c = 0; c < 2; c++)
+                atomicAdd(rho + ((long)wrapn(iX + a, N) * N + wrapn(iY + b, N)) * rp + wrapn(iZ + c, N),
+                          wx[a] * wy[b] * wz[c]);
+}
+
+// red.global.add.v4.f32: four consecutive floats in one reduction (sm_90 and later)
+__device__ __forceinline__ void red_add_v4(float *p, float a, float b, float c, float d) {
+    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(a), "f"(b), "f"(c), "f"(d)
+                 : "memory");
+}
+
+// gather of the three displacement grids from global memory for a particle that moved too far
+// for the brick's shared tiles (rare); same arithmetic as the tiled path
+template <typename T>
+__device__ __noinline__ void displace_global(int N, T Nf, T boxlen, const T *d1, const T *d2, int y, int z,
+                                             float &p0, float &p1, float &p2) {
+    const long rp = N + 2;
+    const long yz = (long)y * rp + z;
+    const T Xg = (T)p0 * Nf / boxlen;
+    const int nx = (int)dfloor<T>(Xg + (T)0.5);
+    T wx[3];
+    tsc_w<T>(Xg - (T)nx, wx);
+    long xo[3];
+    for (int i = 0; i < 3; i++) xo[i] = (long)wrapn(nx - 1 + i, N) * N * rp;
+    p1 = (float)((T)p1 - (wx[0] * d1[xo[0] + yz] + wx[1] * d1[xo[1] + yz] + wx[2] * d1[xo[2] + yz]));
+    const T Yg = (T)p1 * Nf / boxlen;
+    const int ny = (int)dfloor<T>(Yg + (T)0.5);
+    T wy[3];
+    tsc_w<T>(Yg - (T)ny, wy);
+    T sv = 0;
+    for (int j = 0; j < 3; j++) {
+        const long yo = (long)wrapn(ny - 1 + j, N) * rp + z;
+        sv += wy[j] * (wx[0] * d2[xo[0] + yo] + wx[1] * d2[xo[1] + yo] + wx[2] * d2[xo[2] + yo]);
+    }
+    p2 = (float)((T)p2 - sv);
+}
+
+// tiles of the brick: d0 on the brick, d1 with an x halo of 2, d2 with x and y halos of 2
+#define TH 2
+#define T1X (LB_X + 2 * TH)
+#define T2Y (LB_Y + 2 * TH)
+
+template <typename T>
+__global__ void __launch_bounds__(LB_THREADS, 2)
+k_lattice_cic(int N, int rpo, float spacing, T boxlen, T gfac, T ginv, const T *__restrict__ d0,
+              const T *__restrict__ d1, const T *__restrict__ d2, T *__restrict__ rho, float *__restrict__ pos_out) {
+    using A = typename RegAcc<T>::type;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    A *reg = reinterpret_cast<A *>(smraw);                                  // LR_X * LR_Y * LR_Z
+    T *t0 = reinterpret_cast<T *>(smraw + sizeof(A) * LR_X * LR_Y * LR_Z); // LB_X * LB_Y * LB_Z
+    T *t1 = t0 + LB_X * LB_Y * LB_Z;                                        // T1X * LB_Y * LB_Z
+    T *t2 = t1 + T1X * LB_Y * LB_Z;                                         // T1X * T2Y * LB_Z
+    const int bz_n = N / LB_Z, by_n = N / LB_Y;
+    const int bz = blockIdx.x % bz_n, by = (blockIdx.x / bz_n) % by_n, bx = blockIdx.x / (bz_n * by_n);
+    const int x0 = bx * LB_X, y0 = by * LB_Y, z0 = bz * LB_Z;
+    const long rp = N + 2;  // displacement grids: padded reference layout
+    for (int i = threadIdx.x; i < LR_X * LR_Y * LR_Z; i += blockDim.x) reg[i] = 0;
+    // cooperative, independent loads of the three tiles (rows of LB_Z contiguous values)
+    for (int i = threadIdx.x; i < LB_X * LB_Y * LB_Z; i += blockDim.x) {
+        const int lz = i % LB_Z, ly = (i / LB_Z) % LB_Y, lx = i / (LB_Z * LB_Y);
+        t0[i] = __ldg(d0 + ((long)(x0 + lx) * N + y0 + ly) * rp + z0 + lz);
+    }
+    for (int i = threadIdx.x; i < T1X * LB_Y * LB_Z; i += blockDim.x) {
+        const int lz = i % LB_Z, ly = (i / LB_Z) % LB_Y, lx = i / (LB_Z * LB_Y);
+        t1[i] = __ldg(d1 + ((long)wrapn(x0 - TH + lx, N) * N + y0 + ly) * rp + z0 + lz);
+    }
+    for (int i = threadIdx.x; i < T1X * T2Y * LB_Z; i += blockDim.x) {
+        const int lz = i % LB_Z, ly = (i / LB_Z) % T2Y, lx = i / (LB_Z * T2Y);
+        t2[i] = __ldg(d2 + ((long)wrapn(x0 - TH + lx, N) * N + wrapn(y0 - TH + ly, N)) * rp + z0 + lz);
+    }
+    __syncthreads();
+    const T Nf = (T)N;
+    const float Lf = (float)boxlen;
+    const int lz = threadIdx.x % LB_Z, ly = (threadIdx.x / LB_Z) % LB_Y, lxb = threadIdx.x / (LB_Z * LB_Y);
+#pragma unroll 1
+    for (int rep = 0; rep < (LB_X * LB_Y * LB_Z) / LB_THREADS; rep++) {
+        const int lx = lxb + rep * (LB_THREADS / (LB_Z * LB_Y));
+        const int x = x0 + lx, y = y0 + ly, z = z0 + lz;
+        float p0 = x * spacing, p1 = y * spacing, p2 = z * spacing;  // src/particle.c:114-116
+        // direction 0: on nodes (stencil folded into d0)
+        p0 = (float)((T)p0 - t0[(lx * LB_Y + ly) * LB_Z + lz]);
+        // direction 1: x off node (src/grids_interp.c:269-306), y and z on nodes (folded into d1)
+        const T Xg = (T)p0 * ginv;
+        const int nx = ifloor<T>(Xg + (T)0.5);
+        const int ix = nx - 1 - (x0 - TH);  // tile x index of the first stencil node
+        bool tiled = ix >= 0 && ix + 2 < T1X;
+        T wx[3], wy[3];
+        if (tiled) {
+            tsc_w<T>(Xg - (T)nx, wx);
+            const T *r1 = t1 + (ix * LB_Y + ly) * LB_Z + lz;
+            p1 = (float)((T)p1 - (wx[0] * r1[0] + wx[1] * r1[LB_Y * LB_Z] + wx[2] * r1[2 * LB_Y * LB_Z]));
+            // direction 2: x and y off nodes, z on nodes (folded into d2)
+            const T Yg = (T)p1 * ginv;
+            const int ny = ifloor<T>(Yg + (T)0.5);
+            const int iy = ny - 1 - (y0 - TH);
+            tiled = iy >= 0 && iy + 2 < T2Y;
+            if (tiled) {
+                tsc_w<T>(Yg - (T)ny, wy);
+                T sv = 0;
+#pragma unroll
+                for (int i = 0; i < 3; i++) {
+                    const T *r2 = t2 + ((ix + i) * T2Y + iy) * LB_Z + lz;
+                    sv += wx[i] * (wy[0] * r2[0] + wy[1] * r2[LB_Z] + wy[2] * r2[2 * LB_Z]);
+                }
+                p2 = (float)((T)p2 - sv);
+            }
+        }
+        if (!tiled) {
+            // restart the off-node gathers from global memory
+            p1 = y * spacing;
+            p2 = z * spacing;
+            displace_global<T>(N, Nf, boxlen, d1, d2, y, z, p0, p1, p2);
+        }
+        p0 = fwrapf(p0, Lf);
+        p1 = fwrapf(p1, Lf);
+        p2 = fwrapf(p2, Lf);
+        if (pos_out) {
+            const long id = ((long)x * N + y) * N + z;
+            pos_out[3 * id] = p0;
+            pos_out[3 * id + 1] = p1;
+            pos_out[3 * id + 2] = p2;
+        }
+        // CIC (analyse/src/mitos_read.c:288-333), one unit of mean density per particle (M = N)
+        const T X = (T)p0 * ginv, Y = (T)p1 * ginv, Z = (T)p2 * ginv;
+        const int iX = ifloor<T>(X), iY = ifloor<T>(Y), iZ = ifloor<T>(Z);
+        const T dx = X - iX, dy = Y - iY, dz = Z - iZ;
+        const int rx = wrapn(iX - x0 + 1, N), ry = wrapn(iY - y0 + 1, N), rz = wrapn(iZ - z0 + LR_Z0, N);
+        if (rx < LR_X - 1 && ry < LR_Y - 1 && rz < LR_Z - 1) {
+            A *c = reg + (rx * LR_Y + ry) * LR_Z + rz;
+            const T tx = 1 - dx, ty = 1 - dy, tz = 1 - dz;
+            RegAcc<T>::add(c, tx * ty * tz);
+            RegAcc<T>::add(c + 1, tx * ty * dz);
+            RegAcc<T>::add(c + LR_Z, tx * dy * tz);
+            RegAcc<T>::add(c + LR_Z + 1, tx * dy * dz);
+            RegAcc<T>::add(c + LR_Y * LR_Z, dx * ty * tz);
+            RegAcc<T>::add(c + LR_Y * LR_Z + 1, dx * ty * dz);
+            RegAcc<T>::add(c + LR_Y * LR_Z + LR_Z, dx * dy * tz);
+            RegAcc<T>::add(c + LR_Y * LR_Z + LR_Z + 1, dx * dy * dz);
+        } else {
+            cic_global<T>(rho, N, rpo, iX, iY, iZ, dx, dy, dz);
+        }
+    }
+    __syncthreads();
+    // flush: rows of LR_Z cells starting at z0 - 4 (a multiple of 4, so 16-byte aligned with the
+    // 16-byte aligned row pitch rpo)
+    constexpr int Q = LR_Z / 4;
+    for (int i = threadIdx.x; i < LR_X * LR_Y * Q; i += blockDim.x) {
+        const int qz = i % Q, qy = (i / Q) % LR_Y, qx = i / (Q * LR_Y);
+        const A *c = reg + (qx * LR_Y + qy) * LR_Z + 4 * qz;
+        if (c[0] == (A)0 && c[1] == (A)0 && c[2] == (A)0 && c[3] == (A)0) continue;
+        T v[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) v[k] = RegAcc<T>::value(c[k]);
+        const long row = ((long)wrapn(x0 - 1 + qx, N) * N + wrapn(y0 - 1 + qy, N)) * rpo;
+        const int gz = z0 - LR_Z0 + 4 * qz;
+        if constexpr (sizeof(T) == 4) {
+            if (gz >= 0 && gz + 3 < N) {
+                red_add_v4((float *)rho + row + gz, (float)v[0], (float)v[1], (float)v[2], (float)v[3]);
+                continue;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            if (v[k] != (T)0) atomicAdd(rho + row + wrapn(gz + k, N), v[k]);
+    }
+}
+
+static size_t lattice_smem(size_t elem) {
+    // the region accumulators have the size of one element in either precision
+    return elem * ((size_t)LR_X * LR_Y * LR_Z + LB_X * LB_Y * LB_Z + (size_t)T1X * LB_Y * LB_Z +
+                   (size_t)T1X * T2Y * LB_Z);
+}
+
+int lattice_deposit(int N, double boxlen, int precision, const void *d0, const void *d1, const void *d2,
+                    void *rho, int rho_pitch, float *pos_out) {
+    if (N % LB_Z || N % LB_Y || N % LB_X || (rho_pitch * (precision == MITOS_FP32 ? 4 : 8)) % 16) return 3;
+    const float Lf = (float)boxlen;
+    const float spacing = Lf / N;  // src/particle.c:102-103 with M = N
+    const double gfac = boxlen / N;
+    const unsigned blocks = (unsigned)((N / LB_X) * (N / LB_Y) * (N / LB_Z));
+    launch_begin("lattice_cic");
+    if (precision == MITOS_FP32) {
+        const size_t smem = lattice_smem(sizeof(float));
+        MITOS_CUDA(cudaFuncSetAttribute(k_lattice_cic<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_lattice_cic<float><<<blocks, LB_THREADS, smem, stream()>>>(N, rho_pitch, spacing, (float)boxlen, (float)gfac,
+                                                                     (float)(N / boxlen), (const float *)d0, (const float *)d1,
+                                                                     (const float *)d2, (float *)rho, pos_out);
+    } else {
+        const size_t smem = lattice_smem(sizeof(double));
+        MITOS_CUDA(cudaFuncSetAttribute(k_lattice_cic<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_lattice_cic<double><<<blocks, LB_THREADS, smem, stream()>>>(N, rho_pitch, spacing, boxlen, gfac,
+                                                                      (double)N / boxlen, (const double *)d0, (const double *)d1,
+                                                                      (const double *)d2, (double *)rho, pos_out);
+    }
+    count_launch();
+    MITOS_LAUNCH_CHECK("lattice CIC");
+    return 0;
+}
+
+// whether lattice coordinate i * spacing lands exactly on grid node i for every i, in the
+// arithmetic of both the reference (double, x N / boxlen) and the FP32 path
+bool lattice_aligned(int N, int M, double boxlen) {
+    if (M != N || N % LB_Z || N % LB_Y || N % LB_X) return false;
+    const float Lf = (float)boxlen;
+    const float spacing = Lf / M;
+    for (int i = 0; i < M; i++) {
+        const float x = i * spacing;
+        if ((double)x * N / boxlen != (double)i) return false;
+        if ((float)x * (float)N / Lf != (float)i) return false;
+        if ((double)x / (boxlen / N) != (double)i) return false;
+    }
+    return true;
 }
 
 // CIC of given positions (cic_deposit_dg)
@@ -125,9 +400,9 @@ __global__ void k_cic(long n, int N, T gfac, T val, const float *__restrict__ po
     const T dx = X - iX, dy = Y - iY, dz = Z - iZ;
     const T tx = 1 - dx, ty = 1 - dy, tz = 1 - dz;
     const long rp = N + 2;
-    const int x0 = wrapi(iX, N), x1 = wrapi(iX + 1, N);
-    const int y0 = wrapi(iY, N), y1 = wrapi(iY + 1, N);
-    const int z0 = wrapi(iZ, N), z1 = wrapi(iZ + 1, N);
+    const int x0 = wrapn(iX, N), x1 = wrapn(iX + 1, N);
+    const int y0 = wrapn(iY, N), y1 = wrapn(iY + 1, N);
+    const int z0 = wrapn(iZ, N), z1 = wrapn(iZ + 1, N);
     atomicAdd(rho + ((long)x0 * N + y0) * rp + z0, val * tx * ty * tz);
     atomicAdd(rho + ((long)x1 * N + y0) * rp + z0, val * dx * ty * tz);
     atomicAdd(rho + ((long)x0 * N + y1) * rp + z0, val * tx * dy * tz);

@@ -7,6 +7,11 @@ namespace mitos {
 // CIC into rho (padded real grid, accumulated, in units of the mean density); pos_out optional
 int displace_and_deposit(int N, int M, double boxlen, int precision, const void *d0, const void *d1,
                          const void *d2, void *rho, float *pos_out);
+// lattice-aligned fast path (M = N, exact nodes); the displacement grids must carry the folded
+// on-node TSC stencils (PassArgs::stencil in the displacement passes)
+int lattice_deposit(int N, double boxlen, int precision, const void *d0, const void *d1, const void *d2,
+                    void *rho, int rho_pitch, float *pos_out);
+bool lattice_aligned(int N, int M, double boxlen);
 // CIC of n given positions with per-particle value val
 int cic_positions(long n, int N, double boxlen, int precision, const float *pos, double val, void *rho);
 

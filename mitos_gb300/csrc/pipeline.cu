@@ -141,6 +141,7 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
 
     PassArgs a;
     int win_disp = 3;
+    bool fused_disp_x = false;
     int iters = 0;
     double last_rel = 0;
     if (cfg->method == MITOS_METHOD_2LPT) {
@@ -160,12 +161,15 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
         a.in[0] = Sk;
         if (!e) e = launch_y<T>(g, YOP_PLAIN, -1, a);
         a.in2 = phi;
-        a.out[0] = phi;
         a.scale = V / ((double)N * N * N);
         a.f1 = 1.0;
         a.f2 = -3. / 7.;  // src/mitos.c:385
         a.window_order = 3;
-        if (!e) e = launch_x<T>(g, XOP_COMBINE_2LPT, -1, a);
+        fused_disp_x = true;  // the X pass of the displacement grids runs inside this one
+        a.out[0] = A0;
+        a.out[1] = A1;
+        a.stencil = lattice_aligned(N, M, L) ? stencil_table(N, prec) : nullptr;
+        if (!e) e = launch_x<T>(g, XOP_COMBINE_DISP, -1, a);
         if (e) return e;
         win_disp = 0;
         tim.mark();
@@ -216,14 +220,17 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     }
 
     // S4: displacement grids d_i = c2r(i k_i phi W^-3) (src/mitos.c:395-416)
+    const bool aligned = lattice_aligned(N, M, L);
     memset(&a, 0, sizeof a);
     a.dk = dk;
     a.scale = 1.0;
     a.window_order = win_disp;
+    a.stencil = aligned ? stencil_table(N, prec) : nullptr;
+    if (aligned && !a.stencil) return 5;
     a.in[0] = phi;
     a.out[0] = A0;
     a.out[1] = A1;
-    e = launch_x<T>(g, XOP_DISP, +1, a);
+    if (!fused_disp_x) e = launch_x<T>(g, XOP_DISP, +1, a);
     if (e) return e;
     a.window_order = 0;
     a.in[0] = A0;
@@ -251,8 +258,14 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
         dpos = (float *)workspace(sizeof(float) * 3 * (size_t)M * M * M, 108);
         if (!dpos) return 5;
     }
-    MITOS_CUDA(cudaMemsetAsync(rho, 0, gb, stream()));
-    e = displace_and_deposit(N, M, L, prec, D0, D1, D2, rho, dpos);
+    // the aligned deposit uses a row pitch of N + 4 reals (16-byte aligned rows for vector reductions)
+    const int rho_pitch = aligned ? N + 4 : N + 2;
+    const size_t rho_bytes = (size_t)N * N * rho_pitch * (sizeof(T));
+    void *rhoD = aligned ? workspace(rho_bytes, 15) : rho;
+    if (!rhoD) return 5;
+    MITOS_CUDA(cudaMemsetAsync(rhoD, 0, rho_bytes, stream()));
+    e = aligned ? lattice_deposit(N, L, prec, D0, D1, D2, rhoD, rho_pitch, dpos)
+                : displace_and_deposit(N, M, L, prec, D0, D1, D2, rhoD, dpos);
     if (e) return e;
     tim.mark();
 
@@ -263,9 +276,9 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     memset(&a, 0, sizeof a);
     a.dk = dk;
     a.scale = 1.0;
-    a.in[0] = rho;
+    a.in[0] = rhoD;
     a.out[0] = Sk;
-    a.rp_in = N + 2;
+    a.rp_in = rho_pitch;
     a.rho_a = 1.0;
     a.rho_b = -1.0;
     e = launch_z_r2c<T>(g, a);
@@ -286,18 +299,22 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     tim.mark();
 
     if (res) {
-        std::vector<double> h(3 * cfg->pk_bins);
-        MITOS_CUDA(cudaMemcpyAsync(h.data(), acc, sizeof(double) * 3 * cfg->pk_bins, cudaMemcpyDeviceToHost, stream()));
+        const double *ksum;
+        const long long *count;
+        e = bin_geometry(N, cfg->pk_bins, cfg->pk_linear, L, &ksum, &count);
+        if (e) return e;
+        std::vector<double> h(cfg->pk_bins);
+        MITOS_CUDA(cudaMemcpyAsync(h.data(), acc + cfg->pk_bins, sizeof(double) * cfg->pk_bins,
+                                   cudaMemcpyDeviceToHost, stream()));
         if (dpos)
             MITOS_CUDA(cudaMemcpyAsync(res->pos, dpos, sizeof(float) * 3 * (size_t)M * M * M, cudaMemcpyDeviceToHost,
                                        stream()));
         MITOS_CUDA(cudaStreamSynchronize(stream()));
         for (int i = 0; i < cfg->pk_bins; i++) {
-            long long n;
-            memcpy(&n, &h[2 * cfg->pk_bins + i], sizeof n);
-            if (res->pk_obs) res->pk_obs[i] = (long)n;
-            if (res->pk_k) res->pk_k[i] = h[i] / (double)n;
-            if (res->pk_p) res->pk_p[i] = h[cfg->pk_bins + i] / (double)n / V;
+            const double n = (double)count[i];
+            if (res->pk_obs) res->pk_obs[i] = (long)count[i];
+            if (res->pk_k) res->pk_k[i] = ksum[i] / n;
+            if (res->pk_p) res->pk_p[i] = h[i] / n / V;
         }
         res->ma_iterations = iters;
         res->ma_residual = last_rel;
