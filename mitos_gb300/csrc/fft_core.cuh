@@ -209,6 +209,131 @@ __device__ __forceinline__ int n_out(const FFTPlan &pl, int E, int t, int e) {
     return t + b * (pl.n / E) + r * (pl.n / R);
 }
 
+
+// ---- compile-time specialisation (length NL, elements per thread E) ----------------------
+// Same schedule and stage arithmetic as fft_regs with every length, radix and stride a
+// constant, so shared-memory offsets and index splits fold away.
+template <int NL, int E> struct CTSched {
+    static constexpr int radix_at(int s) {
+        int rem = NL, idx = 0;
+        if (E % 8 == 0)
+            while (rem % 8 == 0) { if (idx == s) return 8; rem /= 8; idx++; }
+        while (E % 4 == 0 && rem % 4 == 0) { if (idx == s) return 4; rem /= 4; idx++; }
+        while (E % 2 == 0 && rem % 2 == 0) { if (idx == s) return 2; rem /= 2; idx++; }
+        while (E % 3 == 0 && rem % 3 == 0) { if (idx == s) return 3; rem /= 3; idx++; }
+        return 0;
+    }
+    static constexpr int count() {
+        int n = 0;
+        while (radix_at(n)) n++;
+        return n;
+    }
+    static constexpr int nst = count();
+    static constexpr int ns_before(int s) {
+        int p = 1;
+        for (int i = 0; i < s; i++) p *= radix_at(i);
+        return p;
+    }
+    static constexpr int first = radix_at(0);
+    static constexpr int last = radix_at(nst - 1);
+};
+
+// padded index of i + D from the padded index of i, when D is a multiple of 8 (or i + D stays
+// inside one group of 8)
+template <int D> __device__ __forceinline__ int spad_plus(int i, int si) {
+    if constexpr (D % 8 == 0) return si + D + D / 8;
+    else return spad(i + D);
+}
+
+template <typename T, int E, int SIGN, int NL, int SN, int S>
+struct CTStage {
+    using Sch = CTSched<NL, E>;
+    static __device__ __forceinline__ void run(cplx<T> *v, cplx<T> *sm, int t, const cplx<T> *__restrict__ tw,
+                                               int tw_scale) {
+        if constexpr (S < Sch::nst) {
+            constexpr int Rp = Sch::radix_at(S - 1);
+            constexpr int Nsp = Sch::ns_before(S - 1);
+            constexpr int R = Sch::radix_at(S);
+            constexpr int Ns = Sch::ns_before(S);
+#pragma unroll
+            for (int b = 0; b < E / Rp; b++) {
+                const int j = t + b * (NL / E);
+                const int idxD = (j / Nsp) * Nsp * Rp + (j % Nsp);
+                if constexpr (Nsp == 1 && Rp <= 8) {
+                    // idxD = j Rp and the Rp outputs stay in one padding group when Rp divides 8
+                    const int base = spad(idxD);
+#pragma unroll
+                    for (int r = 0; r < Rp; r++)
+                        sm[(8 % Rp == 0 ? base + r : spad(idxD + r)) * SN] = v[b * Rp + r];
+                } else {
+                    const int base = spad(idxD);
+#pragma unroll
+                    for (int r = 0; r < Rp; r++) {
+                        const int o = (Nsp % 8 == 0) ? base + r * Nsp + (r * Nsp) / 8 : spad(idxD + r * Nsp);
+                        sm[o * SN] = v[b * Rp + r];
+                    }
+                }
+            }
+            __syncthreads();
+#pragma unroll
+            for (int b = 0; b < E / R; b++) {
+                const int j = t + b * (NL / E);
+                const int jm = j % Ns;
+                const int step = jm * (NL / (Ns * R)) * tw_scale;
+                const int base = spad(j);
+#pragma unroll
+                for (int r = 0; r < R; r++) {
+                    constexpr int D = NL / R;
+                    const int o = ((D % 8) == 0) ? base + r * D + (r * D) / 8 : spad(j + r * D);
+                    cplx<T> x = sm[o * SN];
+                    if (r > 0) {
+                        cplx<T> w = __ldg(tw + r * step);
+                        if (SIGN > 0) w.y = -w.y;
+                        x = cmul<T>(x, w);
+                    }
+                    v[b * R + r] = x;
+                }
+                dft<T, R, SIGN>(v + b * R);
+            }
+            __syncthreads();
+            CTStage<T, E, SIGN, NL, SN, S + 1>::run(v, sm, t, tw, tw_scale);
+        }
+    }
+};
+
+// fft_regs with the length, the exchange stride SN and the schedule fixed at compile time
+template <typename T, int E, int SIGN, int NL, int SN>
+__device__ __forceinline__ void fft_regs_ct(cplx<T> *v, cplx<T> *sm, int t, const cplx<T> *__restrict__ tw,
+                                            int tw_scale) {
+    stage_first<T, E, CTSched<NL, E>::first, SIGN>(v);
+    CTStage<T, E, SIGN, NL, SN, 1>::run(v, sm, t, tw, tw_scale);
+}
+
+template <int NL, int E> __device__ __forceinline__ int n_in_ct(int t, int e) {
+    constexpr int R = CTSched<NL, E>::first;
+    return t + (e / R) * (NL / E) + (e % R) * (NL / R);
+}
+template <int NL, int E> __device__ __forceinline__ int n_out_ct(int t, int e) {
+    constexpr int R = CTSched<NL, E>::last;
+    return t + (e / R) * (NL / E) + (e % R) * (NL / R);
+}
+
+// one entry point for both variants: NL = 0 runs the runtime plan
+template <typename T, int E, int SIGN, int NL, int SN>
+__device__ __forceinline__ void fft_any(const FFTPlan &pl, cplx<T> *v, cplx<T> *sm, int sn, int t,
+                                        const cplx<T> *__restrict__ tw) {
+    if constexpr (NL > 0) fft_regs_ct<T, E, SIGN, NL, SN>(v, sm, t, tw, pl.tw_scale);
+    else fft_regs<T, E, SIGN>(pl, v, sm, sn, t, tw);
+}
+template <int NL, int E> __device__ __forceinline__ int nin_any(const FFTPlan &pl, int t, int e) {
+    if constexpr (NL > 0) return n_in_ct<NL, E>(t, e);
+    else return n_in(pl, E, t, e);
+}
+template <int NL, int E> __device__ __forceinline__ int nout_any(const FFTPlan &pl, int t, int e) {
+    if constexpr (NL > 0) return n_out_ct<NL, E>(t, e);
+    else return n_out(pl, E, t, e);
+}
+
 // host: radix schedule of a length for a given E (radices dividing E, largest first)
 bool make_plan(int n, int E, int tw_len, FFTPlan *pl);
 

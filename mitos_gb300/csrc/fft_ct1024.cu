@@ -1,0 +1,10 @@
+// fft_ct1024.cu -- compile-time specialised FP32 FFT passes for N = 1024 (X / Y length 1024,
+// Z length 512, 4 pencils per X / Y block).
+#include "fft_kernels.cuh"
+
+namespace mitos {
+int launch_x_ct1024(const GridGeom &g, XOp op, int sign, const PassArgs &a) { return launch_x_t<float, 1024, 4>(g, op, sign, a); }
+int launch_y_ct1024(const GridGeom &g, YOp op, int sign, const PassArgs &a) { return launch_y_t<float, 1024, 4>(g, op, sign, a); }
+int launch_zc_ct1024(const GridGeom &g, ZOp op, const PassArgs &a) { return launch_zc_t<float, 512>(g, op, a); }
+int launch_zr_ct1024(const GridGeom &g, const PassArgs &a) { return launch_zr_t<float, 512>(g, a); }
+}  // namespace mitos

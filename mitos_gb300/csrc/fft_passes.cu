@@ -1,543 +1,53 @@
-// fft_passes.cu -- X / Y / Z pass kernels of the 3D real FFT with fused k-space operations.
-#include "context.cuh"
+// fft_passes.cu -- dispatch of the FFT passes: compile-time specialised kernels for the FP32
+// sizes 256, 512 and 1024 (instantiated in fft_ct*.cu), runtime-plan kernels otherwise.
+#include "fft_kernels.cuh"
 
 namespace mitos {
 
-template <typename T> __device__ __forceinline__ T dev_sqrt(T x);
-template <> __device__ __forceinline__ float dev_sqrt<float>(float x) { return sqrtf(x); }
-template <> __device__ __forceinline__ double dev_sqrt<double>(double x) { return sqrt(x); }
+// specialised entry points (fft_ct256.cu, fft_ct512.cu, fft_ct1024.cu)
+#define MITOS_CT_DECL(N)                                                                          \
+    int launch_x_ct##N(const GridGeom &g, XOp op, int sign, const PassArgs &a);                  \
+    int launch_y_ct##N(const GridGeom &g, YOp op, int sign, const PassArgs &a);                  \
+    int launch_zc_ct##N(const GridGeom &g, ZOp op, const PassArgs &a);                           \
+    int launch_zr_ct##N(const GridGeom &g, const PassArgs &a);
+MITOS_CT_DECL(256)
+MITOS_CT_DECL(512)
+MITOS_CT_DECL(1024)
 
-// ------------------------------------------------------------------------------------------
-// X and Y passes: complex FFTs along a strided axis.  Block = P pencils; thread (t, p) with
-// p fastest so that a warp reads P consecutive columns of each row.
-// ------------------------------------------------------------------------------------------
-template <typename T, int E, int SIGN, int AXIS, int OP>
-__global__ void __launch_bounds__(512, 2) k_strided(GridGeom g, PassArgs a, const T *__restrict__ win) {
-    extern __shared__ __align__(16) unsigned char smraw[];
-    cplx<T> *sm = reinterpret_cast<cplx<T> *>(smraw);
-    const FFTPlan &pl = g.plN;
-    const int P = g.P_xy;
-    const int tid = threadIdx.x, p = tid % P, t = tid / P;
-    const int N = g.N, H = g.H;
-    long base, stride;
-    bool valid;
-    int ix = 0, iy = 0, iz;
-    if (AXIS == 0) {
-        long col = (long)blockIdx.x * P + p;
-        valid = col < g.plane;
-        if (!valid) col = 0;
-        base = col;
-        stride = g.plane;
-        iy = kint((int)(col / H), N);
-        iz = (int)(col % H);
-    } else {
-        int tiles = (H + P - 1) / P;
-        int x = blockIdx.x / tiles;
-        int kz = (blockIdx.x % tiles) * P + p;
-        valid = kz < H;
-        if (!valid) kz = 0;
-        base = (long)x * g.plane + kz;
-        stride = H;
-        ix = kint(x, N);
-        iz = kz;
-    }
-    const cplx<T> *tw = reinterpret_cast<const cplx<T> *>(g.twN);
-    const T dk = (T)a.dk;
-    const T scale = (T)a.scale;
-    cplx<T> *psm = sm + p;
-
-    // P(k): one power histogram per warp behind the FFT exchange buffer (the counts and the
-    // wavenumber sums of the bins depend only on the geometry and are tabulated on the host)
-    T *hp = nullptr;
-    if constexpr (OP == XOP_PK) {
-        size_t off = (size_t)P * spad_len(N) * sizeof(cplx<T>);
-        T *hist = reinterpret_cast<T *>(smraw + off);
-        const int nw = blockDim.x >> 5;
-        for (int i = tid; i < a.nbins * nw; i += blockDim.x) hist[i] = 0;
-        hp = hist + (tid >> 5) * a.nbins;
-        __syncthreads();
-    }
-
-    constexpr int NIN = (AXIS == 1 && OP == YOP_HESS) ? 3 : (AXIS == 1 && OP == YOP_DISP) ? 2 : 1;
-    cplx<T> raw[E];
-    cplx<T> v[E];
-#pragma unroll 1
-    for (int i = 0; i < NIN; i++) {
-        const cplx<T> *src = reinterpret_cast<const cplx<T> *>(a.in[i]);
-#pragma unroll
-        for (int e = 0; e < E; e++) {
-            int n = n_in(pl, E, t, e);
-            raw[e] = valid ? src[base + (long)n * stride] : mk<T>(0, 0);
-            // window undo applied on load by the inverse X passes (XOP_DISP / XOP_HESS)
-            if constexpr (AXIS == 0 && (OP == XOP_DISP || OP == XOP_HESS)) {
-                if (win) raw[e] = cscale<T>(raw[e], win[kint(n, N) + N / 2] * win[iy + N / 2] * win[iz + N / 2]);
-            }
-        }
-        // outputs produced from input i: (output index, factor) with factor 0: 1, 1: i k, 2: -k^2
-        int nout = 1;
-        int outs[3] = {0, 0, 0}, facs[3] = {0, 0, 0};
-        if (AXIS == 0 && OP == XOP_HESS) { nout = 3; outs[1] = 1; outs[2] = 2; facs[1] = 1; facs[2] = 2; }
-        if (AXIS == 0 && OP == XOP_DISP) { nout = 2; outs[1] = 1; facs[1] = 1; }
-        if (AXIS == 1 && OP == YOP_HESS) {
-            if (i == 0) { nout = 3; outs[0] = 3; facs[0] = 2; outs[1] = 4; facs[1] = 1; outs[2] = 5; }
-            if (i == 1) { nout = 2; outs[0] = 1; facs[0] = 1; outs[1] = 2; }
-            if (i == 2) { nout = 1; outs[0] = 0; }
-        }
-        if (AXIS == 1 && OP == YOP_DISP) {
-            if (i == 0) { nout = 2; outs[0] = 1; facs[0] = 1; outs[1] = 2; }
-            if (i == 1) { nout = 1; outs[0] = 0; }
-        }
-#pragma unroll 1
-        for (int m = 0; m < nout; m++) {
-            const int fac = facs[m];
-            // on-node TSC stencil of the displacement passes, applied to the k-space input:
-            // x for the d_x chain (X output 1), y for the d_x and d_y chains (Y outputs 0, 1)
-            const T *stn = nullptr;
-            if constexpr ((AXIS == 0 && OP == XOP_DISP) || (AXIS == 1 && OP == YOP_DISP)) {
-                if ((AXIS == 0 && outs[m] == 1) || (AXIS == 1 && outs[m] <= 1))
-                    stn = reinterpret_cast<const T *>(a.stencil);
-            }
-#pragma unroll
-            for (int e = 0; e < E; e++) {
-                cplx<T> x = raw[e];
-                if (fac != 0) {
-                    T kk = (T)kint(n_in(pl, E, t, e), N) * dk;
-                    x = (fac == 1) ? cmul_is<T>(x, kk) : cscale<T>(x, -kk * kk);
-                }
-                if (stn) x = cscale<T>(x, stn[kint(n_in(pl, E, t, e), N) + N / 2]);
-                v[e] = x;
-            }
-            fft_regs<T, E, SIGN>(pl, v, psm, P, t, tw);
-            if (!valid) continue;
-            cplx<T> *dst = reinterpret_cast<cplx<T> *>(a.out[outs[m]]);
-#pragma unroll
-            for (int e = 0; e < E; e++) {
-                int n = n_out(pl, E, t, e);
-                long idx = base + (long)n * stride;
-                cplx<T> r = cscale<T>(v[e], scale);
-                if constexpr (AXIS == 0 && (OP == XOP_COMBINE_2LPT || OP == XOP_ADD_POISSON ||
-                                            OP == XOP_PK)) {
-                    const int jx = kint(n, N);
-                    const long n2 = (long)jx * jx + (long)iy * iy + (long)iz * iz;
-                    if constexpr (OP == XOP_PK) {
-                        if (win) r = cscale<T>(r, win[jx + N / 2] * win[iy + N / 2] * win[iz + N / 2]);
-                        int bin = a.bin_of_n2[n2];
-                        if (bin >= 0) {
-                            const T mult = (iz == 0 || iz == N / 2) ? (T)1 : (T)2;
-                            atomicAdd(hp + bin, mult * (r.x * r.x + r.y * r.y));
-                        }
-                        if (a.out[0]) dst[idx] = r;
-                    } else {
-                        const T kk2 = (T)n2 * dk * dk;
-                        const T G = (n2 > 0) ? (T)-1 / kk2 : (T)1;
-                        const cplx<T> q = reinterpret_cast<const cplx<T> *>(a.in2)[idx];
-                        cplx<T> o;
-                        if constexpr (OP == XOP_COMBINE_2LPT) {
-                            const T f1 = (T)a.f1, f2 = (T)a.f2;
-                            o = mk<T>(f1 * q.x + f2 * G * r.x, f1 * q.y + f2 * G * r.y);
-                        } else {
-                            o = mk<T>(q.x + G * r.x, q.y + G * r.y);
-                        }
-                        if (win) o = cscale<T>(o, win[jx + N / 2] * win[iy + N / 2] * win[iz + N / 2]);
-                        dst[idx] = o;
-                    }
-                } else {
-                    dst[idx] = r;
-                }
-            }
-        }
-    }
-    if constexpr (OP == XOP_PK) {
-        __syncthreads();
-        const size_t off = (size_t)P * spad_len(N) * sizeof(cplx<T>);
-        const T *hist = reinterpret_cast<const T *>(smraw + off);
-        const int nw = blockDim.x >> 5;
-        for (int i = tid; i < a.nbins; i += blockDim.x) {
-            double sum = 0;
-            for (int w = 0; w < nw; w++) sum += (double)hist[w * a.nbins + i];
-            if (sum != 0) atomicAdd(a.bin_p + i, sum);
-        }
-    }
-}
-
-
-// ------------------------------------------------------------------------------------------
-// X pass that closes the 2LPT potential and opens the displacement grids in one sweep:
-// forward FFT of the source spectrum, phi = (f1 phi1 - f2 S/k^2) / W_TSC, then the inverse
-// FFTs of phi and i kx phi (with the on-node stencil of the d_x chain when requested).
-// ------------------------------------------------------------------------------------------
-template <typename T, int E>
-__global__ void __launch_bounds__(512, 2) k_x_combine_disp(GridGeom g, PassArgs a, const T *__restrict__ win) {
-    extern __shared__ __align__(16) unsigned char smraw[];
-    cplx<T> *sm = reinterpret_cast<cplx<T> *>(smraw);
-    const FFTPlan &pl = g.plN;
-    const int P = g.P_xy;
-    const int tid = threadIdx.x, p = tid % P, t = tid / P;
-    const int N = g.N, H = g.H;
-    long col = (long)blockIdx.x * P + p;
-    const bool valid = col < g.plane;
-    if (!valid) col = 0;
-    const int iy = kint((int)(col / H), N), iz = (int)(col % H);
-    const cplx<T> *tw = reinterpret_cast<const cplx<T> *>(g.twN);
-    const T dk = (T)a.dk, scale = (T)a.scale, f1 = (T)a.f1, f2 = (T)a.f2;
-    const T *stn = reinterpret_cast<const T *>(a.stencil);
-    cplx<T> *psm = sm + p;
-    const cplx<T> *src = reinterpret_cast<const cplx<T> *>(a.in[0]);
-    const cplx<T> *phi1 = reinterpret_cast<const cplx<T> *>(a.in2);
-    cplx<T> v[E];
-#pragma unroll
-    for (int e = 0; e < E; e++) v[e] = valid ? src[col + (long)n_in(pl, E, t, e) * g.plane] : mk<T>(0, 0);
-    fft_regs<T, E, -1>(pl, v, psm, P, t, tw);
-    const T wyz = win ? win[iy + N / 2] * win[iz + N / 2] : (T)1;
-#pragma unroll
-    for (int e = 0; e < E; e++) {
-        const int n = n_out(pl, E, t, e);
-        const int jx = kint(n, N);
-        const long n2 = (long)jx * jx + (long)iy * iy + (long)iz * iz;
-        const T G = (n2 > 0) ? (T)-1 / ((T)n2 * dk * dk) : (T)1;
-        const cplx<T> q = valid ? phi1[col + (long)n * g.plane] : mk<T>(0, 0);
-        const cplx<T> r = cscale<T>(v[e], scale);
-        cplx<T> o = mk<T>(f1 * q.x + f2 * G * r.x, f1 * q.y + f2 * G * r.y);
-        if (win) o = cscale<T>(o, win[jx + N / 2] * wyz);
-        psm[spad(n) * P] = o;
-    }
-    __syncthreads();
-    cplx<T> phi[E];
-#pragma unroll
-    for (int e = 0; e < E; e++) phi[e] = psm[spad(n_in(pl, E, t, e)) * P];
-    __syncthreads();
-#pragma unroll 1
-    for (int m = 0; m < 2; m++) {
-#pragma unroll
-        for (int e = 0; e < E; e++) {
-            cplx<T> x = phi[e];
-            if (m == 1) {
-                const int jx = kint(n_in(pl, E, t, e), N);
-                x = cmul_is<T>(x, (T)jx * dk);
-                if (stn) x = cscale<T>(x, stn[jx + N / 2]);
-            }
-            v[e] = x;
-        }
-        fft_regs<T, E, 1>(pl, v, psm, P, t, tw);
-        if (valid) {
-            cplx<T> *dst = reinterpret_cast<cplx<T> *>(a.out[m]);
-#pragma unroll
-            for (int e = 0; e < E; e++) dst[col + (long)n_out(pl, E, t, e) * g.plane] = v[e];
-        }
-    }
-}
-// ------------------------------------------------------------------------------------------
-// Z c2r: rows of N/2+1 complex -> N reals via an N/2-point complex inverse FFT.
-// ------------------------------------------------------------------------------------------
-template <typename T, int E, int OP>
-__global__ void __launch_bounds__(256) k_z_c2r(GridGeom g, PassArgs a) {
-    extern __shared__ __align__(16) unsigned char smraw[];
-    cplx<T> *sm = reinterpret_cast<cplx<T> *>(smraw);
-    const FFTPlan &pl = g.plH;
-    const int h = pl.n, N = g.N, H = g.H;
-    const int tpp = h / E;
-    const int tid = threadIdx.x, t = tid % tpp, p = tid / tpp;
-    long row = (long)blockIdx.x * g.P_z + p;
-    const bool valid = row < (long)N * N;
-    if (!valid) row = 0;
-    const cplx<T> *tw = reinterpret_cast<const cplx<T> *>(g.twN);
-    const T dk = (T)a.dk;
-    const T scale = (T)a.scale;
-    cplx<T> *psm = sm + (long)p * spad_len(h);
-
-    constexpr int NIN = (OP == ZOP_C2R) ? 1 : (OP == ZOP_DISP) ? 3 : 6;
-    // inputs of the Hessian passes are [xx, xy, xz, yy, yz, zz]; the 2LPT source is accumulated
-    // in the reference's term order (src/2lpt.c:111-112): zz yy + zz xx + yy xx - xy^2 - yz^2 - xz^2
-    constexpr int ORDER_2LPT[6] = {0, 3, 5, 1, 4, 2};
-    constexpr int NKEEP = (OP == ZOP_HESS_MA) ? 6 : (OP == ZOP_HESS_2LPT) ? 2 : 1;
-    cplx<T> o[NKEEP][E];
-    cplx<T> acc[E];
-    T *dst_row = nullptr;
-#pragma unroll
-    for (int q = 0; q < NIN; q++) {
-        const int f = (OP == ZOP_HESS_2LPT) ? ORDER_2LPT[q] : q;
-        // kz factor of input f: 0 -> 1, 1 -> i kz, 2 -> -kz^2
-        int fac = 0;
-        if (OP == ZOP_HESS_2LPT || OP == ZOP_HESS_MA) fac = (f == 2 || f == 4) ? 1 : (f == 5 ? 2 : 0);
-        if (OP == ZOP_DISP) fac = (f == 2) ? 1 : 0;
-        const cplx<T> *src = reinterpret_cast<const cplx<T> *>(a.in[f]) + row * H;
-        cplx<T> v[E];
-#pragma unroll
-        for (int e = 0; e < E; e++) {
-            const int k = n_in(pl, E, t, e);
-            cplx<T> X = src[k], Y = src[h - k];
-            if (fac != 0) {
-                const T k1 = (T)k * dk, k2 = (T)(h - k) * dk;
-                if (fac == 1) { X = cmul_is<T>(X, k1); Y = cmul_is<T>(Y, k2); }
-                else { X = cscale<T>(X, -k1 * k1); Y = cscale<T>(Y, -k2 * k2); }
-            }
-            if constexpr (OP == ZOP_DISP) {
-                const T *stn = reinterpret_cast<const T *>(a.stencil);
-                if (stn) { X = cscale<T>(X, stn[k + N / 2]); Y = cscale<T>(Y, stn[h - k + N / 2]); }
-            }
-            if (k == 0) { X.y = 0; Y.y = 0; }
-            // E' = X + conj(Y), O' = (X - conj(Y)) e^{+2 pi i k / N}, Z = E' + i O'
-            const cplx<T> w = __ldg(tw + k);  // exp(-2 pi i k / N)
-            const cplx<T> Ep = mk<T>(X.x + Y.x, X.y - Y.y);
-            const cplx<T> D = mk<T>(X.x - Y.x, X.y + Y.y);
-            const cplx<T> Op = mk<T>(D.x * w.x + D.y * w.y, D.y * w.x - D.x * w.y);
-            v[e] = mk<T>(Ep.x - Op.y, Ep.y + Op.x);
-        }
-        fft_regs<T, E, 1>(pl, v, psm, 1, t, tw);
-        if constexpr (OP == ZOP_C2R || OP == ZOP_DISP) {
-            if (valid) {
-                T *dst = reinterpret_cast<T *>(a.out[f]) + row * a.rp_out;
-#pragma unroll
-                for (int e = 0; e < E; e++) {
-                    const int n = n_out(pl, E, t, e);
-                    *reinterpret_cast<cplx<T> *>(dst + 2 * n) = cscale<T>(v[e], scale);
-                }
-                if (t == 0 && a.rp_out > N) { dst[N] = 0; dst[N + 1] = 0; }
-            }
-        } else if constexpr (OP == ZOP_HESS_2LPT) {
-#pragma unroll
-            for (int e = 0; e < E; e++) {
-                const cplx<T> x = cscale<T>(v[e], scale);
-                if (q == 0) o[0][e] = x;  // xx
-                else if (q == 1) o[1][e] = x;  // yy
-                else if (q == 2) {  // zz: zz yy + zz xx + yy xx
-                    acc[e] = mk<T>(x.x * o[1][e].x + x.x * o[0][e].x + o[1][e].x * o[0][e].x,
-                                   x.y * o[1][e].y + x.y * o[0][e].y + o[1][e].y * o[0][e].y);
-                } else {  // - xy^2, - yz^2, - xz^2
-                    acc[e] = mk<T>(acc[e].x - x.x * x.x, acc[e].y - x.y * x.y);
-                }
-            }
-        } else {
-#pragma unroll
-            for (int e = 0; e < E; e++) o[f][e] = v[e];
-        }
-    }
-    (void)dst_row;
-    if (!valid) return;
-    if constexpr (OP == ZOP_HESS_2LPT) {
-        T *dst = reinterpret_cast<T *>(a.out[0]) + row * a.rp_out;
-#pragma unroll
-        for (int e = 0; e < E; e++) {
-            const int n = n_out(pl, E, t, e);
-            *reinterpret_cast<cplx<T> *>(dst + 2 * n) = acc[e];
-        }
-        if (t == 0 && a.rp_out > N) { dst[N] = 0; dst[N + 1] = 0; }
-        return;
-    }
-    if constexpr (OP == ZOP_HESS_MA) {
-        T *dst = reinterpret_cast<T *>(a.out[0]) + row * a.rp_out;
-        double sres = 0, srho = 0;
-        const T *rho = (OP == ZOP_HESS_MA) ? reinterpret_cast<const T *>(a.in2) + row * a.rp_in : nullptr;
-#pragma unroll
-        for (int e = 0; e < E; e++) {
-            const int n = n_out(pl, E, t, e);
-            T res2[2];
-#pragma unroll
-            for (int c = 0; c < 2; c++) {
-                const T xx = (c ? o[0][e].y : o[0][e].x) * scale;
-                const T xy = (c ? o[1][e].y : o[1][e].x) * scale;
-                const T xz = (c ? o[2][e].y : o[2][e].x) * scale;
-                const T yy = (c ? o[3][e].y : o[3][e].x) * scale;
-                const T yz = (c ? o[4][e].y : o[4][e].x) * scale;
-                const T zz = (c ? o[5][e].y : o[5][e].x) * scale;
-                // second invariant of the Hessian (src/2lpt.c:111-112)
-                const T s2 = zz * yy + zz * xx + yy * xx - xy * xy - yz * yz - xz * xz;
-                if constexpr (OP == ZOP_HESS_2LPT) {
-                    res2[c] = s2;
-                } else {
-                    // (1 + rho) - det(I + H) = (rho - tr H) - s2 - det H  (src/monge_ampere.c:119-145)
-                    const T d3 = xx * (yy * zz - yz * yz) - xy * (xy * zz - yz * xz) + xz * (xy * yz - yy * xz);
-                    const T r = rho[2 * n + c];
-                    const T res = ((r - xx) - yy - zz) - s2 - d3;
-                    res2[c] = res;
-                    sres += (double)res * (double)res;
-                    srho += (double)r * (double)r;
-                }
-            }
-            *reinterpret_cast<cplx<T> *>(dst + 2 * n) = mk<T>(res2[0], res2[1]);
-        }
-        if (t == 0 && a.rp_out > N) { dst[N] = 0; dst[N + 1] = 0; }
-        if constexpr (OP == ZOP_HESS_MA) {
-            for (int off = 16; off > 0; off >>= 1) {
-                sres += __shfl_down_sync(0xffffffffu, sres, off);
-                srho += __shfl_down_sync(0xffffffffu, srho, off);
-            }
-            if ((threadIdx.x & 31) == 0) {
-                atomicAdd(a.red + 0, sres);
-                atomicAdd(a.red + 1, srho);
-            }
-        }
-    }
-}
-
-// ------------------------------------------------------------------------------------------
-// Z r2c: N reals -> N/2+1 complex via an N/2-point forward FFT and the split step.
-// ------------------------------------------------------------------------------------------
-template <typename T, int E>
-__global__ void __launch_bounds__(256) k_z_r2c(GridGeom g, PassArgs a) {
-    extern __shared__ __align__(16) unsigned char smraw[];
-    cplx<T> *sm = reinterpret_cast<cplx<T> *>(smraw);
-    const FFTPlan &pl = g.plH;
-    const int h = pl.n, N = g.N, H = g.H;
-    const int tpp = h / E;
-    const int tid = threadIdx.x, t = tid % tpp, p = tid / tpp;
-    long row = (long)blockIdx.x * g.P_z + p;
-    const bool valid = row < (long)N * N;
-    if (!valid) row = 0;
-    const cplx<T> *tw = reinterpret_cast<const cplx<T> *>(g.twN);
-    cplx<T> *psm = sm + (long)p * spad_len(h);
-    const T ra = (T)a.rho_a, rb = (T)a.rho_b;
-    const T *src = reinterpret_cast<const T *>(a.in[0]) + row * a.rp_in;
-    cplx<T> v[E];
-#pragma unroll
-    for (int e = 0; e < E; e++) {
-        const int n = n_in(pl, E, t, e);
-        cplx<T> z = *reinterpret_cast<const cplx<T> *>(src + 2 * n);
-        if (a.rho_a != 1.0 || a.rho_b != 0.0) z = mk<T>(z.x * ra + rb, z.y * ra + rb);
-        v[e] = z;
-    }
-    fft_regs<T, E, -1>(pl, v, psm, 1, t, tw);
-#pragma unroll
-    for (int e = 0; e < E; e++) psm[spad(n_out(pl, E, t, e))] = v[e];
-    __syncthreads();
-    if (!valid) return;
-    cplx<T> *dst = reinterpret_cast<cplx<T> *>(a.out[0]) + row * H;
-    for (int k = t; k <= h; k += tpp) {
-        const cplx<T> Z = psm[spad(k == h ? 0 : k)];
-        const cplx<T> Zc = psm[spad(k == 0 ? 0 : h - k)];
-        // even = (Z + conj Zc)/2, odd = (Z - conj Zc)/(2i), X = even + e^{-2 pi i k/N} odd
-        const cplx<T> ev = mk<T>((T)0.5 * (Z.x + Zc.x), (T)0.5 * (Z.y - Zc.y));
-        const cplx<T> od = mk<T>((T)0.5 * (Z.y + Zc.y), (T)-0.5 * (Z.x - Zc.x));
-        const cplx<T> w = __ldg(tw + k);
-        dst[k] = cadd<T>(ev, cmul<T>(od, w));
-    }
-}
-
-// ------------------------------------------------------------------------------------------
-// launchers
-// ------------------------------------------------------------------------------------------
-template <typename T, int E, int SIGN, int AXIS, int OP>
-static int launch_strided_e(const GridGeom &g, const PassArgs &a, const T *win) {
-    const int P = g.P_xy;
-    const int threads = P * (g.N / E);
-    size_t smem = (size_t)P * spad_len(g.N) * sizeof(cplx<T>);
-    if (OP == XOP_PK && AXIS == 0) smem += (size_t)a.nbins * (threads / 32) * sizeof(T);
-    long blocks = (AXIS == 0) ? (g.plane + P - 1) / P : (long)g.N * ((g.H + P - 1) / P);
-    auto kern = k_strided<T, E, SIGN, AXIS, OP>;
-    if (smem > 48 * 1024) MITOS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    launch_begin(AXIS == 0 ? (OP == XOP_HESS ? "x_hess" : OP == XOP_DISP ? "x_disp" : OP == XOP_COMBINE_2LPT ? "x_combine" : OP == XOP_ADD_POISSON ? "x_add_poisson" : OP == XOP_PK ? "x_pk" : "x_plain")
-                        : (OP == YOP_HESS ? "y_hess" : OP == YOP_DISP ? "y_disp" : "y_plain"));
-    kern<<<(unsigned)blocks, threads, smem, stream()>>>(g, a, win);
-    count_launch();
-    MITOS_LAUNCH_CHECK("strided FFT pass");
-    return 0;
-}
-
-template <typename T, int SIGN, int AXIS, int OP>
-static int launch_strided(const GridGeom &g, const PassArgs &a, const T *win) {
-    if (g.E == 8) return launch_strided_e<T, 8, SIGN, AXIS, OP>(g, a, win);
-    return launch_strided_e<T, 12, SIGN, AXIS, OP>(g, a, win);
-}
+// pencils per block of the specialised X / Y kernels (512 threads of 8 elements)
+static inline bool ct_ok(const GridGeom &g, int N) { return g.N == N && g.E == 8 && g.P_xy == 512 / (N / 8); }
 
 template <typename T> int launch_x(const GridGeom &g, XOp op, int sign, const PassArgs &a) {
-    const int prec = sizeof(T) == 4 ? MITOS_FP32 : MITOS_FP64;
-    const T *win = a.window_order ? (const T *)window_table(g.N, a.window_order, prec) : nullptr;
-    if (a.window_order && !win) return 5;
-    switch (op) {
-    case XOP_PLAIN:
-        return sign < 0 ? launch_strided<T, -1, 0, XOP_PLAIN>(g, a, win) : launch_strided<T, 1, 0, XOP_PLAIN>(g, a, win);
-    case XOP_HESS: return launch_strided<T, 1, 0, XOP_HESS>(g, a, win);
-    case XOP_DISP: return launch_strided<T, 1, 0, XOP_DISP>(g, a, win);
-    case XOP_COMBINE_2LPT: return launch_strided<T, -1, 0, XOP_COMBINE_2LPT>(g, a, win);
-    case XOP_ADD_POISSON: return launch_strided<T, -1, 0, XOP_ADD_POISSON>(g, a, win);
-    case XOP_PK: return launch_strided<T, -1, 0, XOP_PK>(g, a, win);
-    case XOP_COMBINE_DISP: {
-        const int P = g.P_xy;
-        const int threads = P * (g.N / g.E);
-        const size_t smem = (size_t)P * spad_len(g.N) * sizeof(cplx<T>);
-        const long blocks = (g.plane + P - 1) / P;
-        launch_begin("x_combine_disp");
-        if (g.E == 8) {
-            auto kern = k_x_combine_disp<T, 8>;
-            if (smem > 48 * 1024) MITOS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            kern<<<(unsigned)blocks, threads, smem, stream()>>>(g, a, win);
-        } else {
-            auto kern = k_x_combine_disp<T, 12>;
-            if (smem > 48 * 1024) MITOS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            kern<<<(unsigned)blocks, threads, smem, stream()>>>(g, a, win);
-        }
-        count_launch();
-        MITOS_LAUNCH_CHECK("x combine + displacement pass");
-        return 0;
+    if constexpr (sizeof(T) == 4) {
+        if (ct_ok(g, 512)) return launch_x_ct512(g, op, sign, a);
+        if (ct_ok(g, 256)) return launch_x_ct256(g, op, sign, a);
+        if (ct_ok(g, 1024)) return launch_x_ct1024(g, op, sign, a);
     }
-    }
-    return 3;
+    return launch_x_t<T, 0, 0>(g, op, sign, a);
 }
-
 template <typename T> int launch_y(const GridGeom &g, YOp op, int sign, const PassArgs &a) {
-    switch (op) {
-    case YOP_PLAIN:
-        return sign < 0 ? launch_strided<T, -1, 1, YOP_PLAIN>(g, a, nullptr) : launch_strided<T, 1, 1, YOP_PLAIN>(g, a, nullptr);
-    case YOP_HESS: return launch_strided<T, 1, 1, YOP_HESS>(g, a, nullptr);
-    case YOP_DISP: return launch_strided<T, 1, 1, YOP_DISP>(g, a, nullptr);
+    if constexpr (sizeof(T) == 4) {
+        if (ct_ok(g, 512)) return launch_y_ct512(g, op, sign, a);
+        if (ct_ok(g, 256)) return launch_y_ct256(g, op, sign, a);
+        if (ct_ok(g, 1024)) return launch_y_ct1024(g, op, sign, a);
     }
-    return 3;
+    return launch_y_t<T, 0, 0>(g, op, sign, a);
 }
-
-template <typename T, int E, int OP>
-static int launch_zc_e(const GridGeom &g, const PassArgs &a) {
-    const int h = g.N / 2;
-    const int tpp = h / E;
-    int P = g.P_z;
-    const int threads = P * tpp;
-    const size_t smem = (size_t)P * spad_len(h) * sizeof(cplx<T>);
-    const long rows = (long)g.N * g.N;
-    auto kern = k_z_c2r<T, E, OP>;
-    if (smem > 48 * 1024) MITOS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    launch_begin(OP == ZOP_C2R ? "z_c2r" : OP == ZOP_HESS_2LPT ? "z_hess_2lpt" : OP == ZOP_HESS_MA ? "z_hess_ma" : "z_disp");
-    kern<<<(unsigned)((rows + P - 1) / P), threads, smem, stream()>>>(g, a);
-    count_launch();
-    MITOS_LAUNCH_CHECK("z c2r pass");
-    return 0;
-}
-
 template <typename T> int launch_z_c2r(const GridGeom &g, ZOp op, const PassArgs &a) {
-    if (g.E == 8) {
-        switch (op) {
-        case ZOP_C2R: return launch_zc_e<T, 8, ZOP_C2R>(g, a);
-        case ZOP_HESS_2LPT: return launch_zc_e<T, 8, ZOP_HESS_2LPT>(g, a);
-        case ZOP_HESS_MA: return launch_zc_e<T, 8, ZOP_HESS_MA>(g, a);
-        case ZOP_DISP: return launch_zc_e<T, 8, ZOP_DISP>(g, a);
-        }
-    } else {
-        switch (op) {
-        case ZOP_C2R: return launch_zc_e<T, 12, ZOP_C2R>(g, a);
-        case ZOP_HESS_2LPT: return launch_zc_e<T, 12, ZOP_HESS_2LPT>(g, a);
-        case ZOP_HESS_MA: return launch_zc_e<T, 12, ZOP_HESS_MA>(g, a);
-        case ZOP_DISP: return launch_zc_e<T, 12, ZOP_DISP>(g, a);
-        }
+    if constexpr (sizeof(T) == 4) {
+        if (ct_ok(g, 512)) return launch_zc_ct512(g, op, a);
+        if (ct_ok(g, 256)) return launch_zc_ct256(g, op, a);
+        if (ct_ok(g, 1024)) return launch_zc_ct1024(g, op, a);
     }
-    return 3;
+    return launch_zc_t<T, 0>(g, op, a);
 }
-
-template <typename T, int E>
-static int launch_zr_e(const GridGeom &g, const PassArgs &a) {
-    const int h = g.N / 2;
-    const int tpp = h / E;
-    const int P = g.P_z;
-    const size_t smem = (size_t)P * spad_len(h) * sizeof(cplx<T>);
-    const long rows = (long)g.N * g.N;
-    auto kern = k_z_r2c<T, E>;
-    if (smem > 48 * 1024) MITOS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    launch_begin("z_r2c");
-    kern<<<(unsigned)((rows + P - 1) / P), P * tpp, smem, stream()>>>(g, a);
-    count_launch();
-    MITOS_LAUNCH_CHECK("z r2c pass");
-    return 0;
-}
-
 template <typename T> int launch_z_r2c(const GridGeom &g, const PassArgs &a) {
-    return g.E == 8 ? launch_zr_e<T, 8>(g, a) : launch_zr_e<T, 12>(g, a);
+    if constexpr (sizeof(T) == 4) {
+        if (ct_ok(g, 512)) return launch_zr_ct512(g, a);
+        if (ct_ok(g, 256)) return launch_zr_ct256(g, a);
+        if (ct_ok(g, 1024)) return launch_zr_ct1024(g, a);
+    }
+    return launch_zr_t<T, 0>(g, a);
 }
 
 template int launch_x<float>(const GridGeom &, XOp, int, const PassArgs &);

@@ -7,6 +7,9 @@
 // The deposit is accumulated in units of the mean density: each particle adds (N/M)^3 split
 // over its 8 cells, so the overdensity is the deposited value minus one.
 #include <math.h>
+#include <stdint.h>
+
+#include <algorithm>
 
 #include "context.cuh"
 #include "particles.cuh"
@@ -185,26 +188,26 @@ __device__ __forceinline__ void red_add_v4(float *p, float a, float b, float c, 
 }
 
 // gather of the three displacement grids from global memory for a particle that moved too far
-// for the brick's shared tiles (rare); same arithmetic as the tiled path
+// for the brick's shared tiles (rare); same arithmetic as the tiled path.  rpd: row pitch of
+// the displacement grids.
 template <typename T>
-__device__ __noinline__ void displace_global(int N, T Nf, T boxlen, const T *d1, const T *d2, int y, int z,
+__device__ __noinline__ void displace_global(int N, int rpd, T ginv, const T *d1, const T *d2, int y, int z,
                                              float &p0, float &p1, float &p2) {
-    const long rp = N + 2;
-    const long yz = (long)y * rp + z;
-    const T Xg = (T)p0 * Nf / boxlen;
-    const int nx = (int)dfloor<T>(Xg + (T)0.5);
+    const long yz = (long)y * rpd + z;
+    const T Xg = (T)p0 * ginv;
+    const int nx = ifloor<T>(Xg + (T)0.5);
     T wx[3];
     tsc_w<T>(Xg - (T)nx, wx);
     long xo[3];
-    for (int i = 0; i < 3; i++) xo[i] = (long)wrapn(nx - 1 + i, N) * N * rp;
+    for (int i = 0; i < 3; i++) xo[i] = (long)wrapn(nx - 1 + i, N) * N * rpd;
     p1 = (float)((T)p1 - (wx[0] * d1[xo[0] + yz] + wx[1] * d1[xo[1] + yz] + wx[2] * d1[xo[2] + yz]));
-    const T Yg = (T)p1 * Nf / boxlen;
-    const int ny = (int)dfloor<T>(Yg + (T)0.5);
+    const T Yg = (T)p1 * ginv;
+    const int ny = ifloor<T>(Yg + (T)0.5);
     T wy[3];
     tsc_w<T>(Yg - (T)ny, wy);
     T sv = 0;
     for (int j = 0; j < 3; j++) {
-        const long yo = (long)wrapn(ny - 1 + j, N) * rp + z;
+        const long yo = (long)wrapn(ny - 1 + j, N) * rpd + z;
         sv += wy[j] * (wx[0] * d2[xo[0] + yo] + wx[1] * d2[xo[1] + yo] + wx[2] * d2[xo[2] + yo]);
     }
     p2 = (float)((T)p2 - sv);
@@ -214,159 +217,215 @@ __device__ __noinline__ void displace_global(int N, T Nf, T boxlen, const T *d1,
 #define TH 2
 #define T1X (LB_X + 2 * TH)
 #define T2Y (LB_Y + 2 * TH)
+#define TILE_ELEMS (LB_X * LB_Y * LB_Z + T1X * LB_Y * LB_Z + T1X * T2Y * LB_Z)
 
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// stage the three displacement tiles of brick (x0, y0, z0) into shared memory: rows of LB_Z
+// elements in 16-byte pieces (row pitch rpd * sizeof(T) and z0 are multiples of 16 bytes)
+template <typename T>
+__device__ __forceinline__ void stage_tiles(T *tiles, int N, int rpd, int x0, int y0, int z0, const T *__restrict__ d0,
+                                            const T *__restrict__ d1, const T *__restrict__ d2) {
+    constexpr int CH = 16 / sizeof(T);
+    constexpr int RC = LB_Z / CH;
+    constexpr int C0 = LB_X * LB_Y * RC, C1 = T1X * LB_Y * RC, C2 = T1X * T2Y * RC;
+#pragma unroll
+    for (int c = threadIdx.x; c < C0 + C1 + C2; c += LB_THREADS) {
+        const T *src;
+        if (c < C0) {
+            const int r = c / RC, lx = r / LB_Y, ly = r % LB_Y;
+            src = d0 + ((long)(x0 + lx) * N + y0 + ly) * rpd;
+        } else if (c < C0 + C1) {
+            const int r = (c - C0) / RC, lx = r / LB_Y, ly = r % LB_Y;
+            src = d1 + ((long)wrapn(x0 - TH + lx, N) * N + y0 + ly) * rpd;
+        } else {
+            const int r = (c - C0 - C1) / RC, lx = r / T2Y, ly = r % T2Y;
+            src = d2 + ((long)wrapn(x0 - TH + lx, N) * N + wrapn(y0 - TH + ly, N)) * rpd;
+        }
+        // the three tiles are contiguous in shared memory, each a sequence of LB_Z-element rows
+        cp_async16(tiles + (long)c * CH, src + z0 + (c % RC) * CH);
+    }
+}
+
+// Persistent: each block walks bricks b = blockIdx.x, blockIdx.x + gridDim.x, ..., staging the
+// next brick's tiles (cp.async, second buffer) while it displaces and deposits the current one.
 template <typename T>
 __global__ void __launch_bounds__(LB_THREADS, 2)
-k_lattice_cic(int N, int rpo, float spacing, T boxlen, T gfac, T ginv, const T *__restrict__ d0,
-              const T *__restrict__ d1, const T *__restrict__ d2, T *__restrict__ rho, float *__restrict__ pos_out) {
+k_lattice_cic(int N, int rpd, int rpo, float spacing, float Lf, T ginv, const T *__restrict__ d0, const T *__restrict__ d1,
+              const T *__restrict__ d2, T *__restrict__ rho, float *__restrict__ pos_out) {
     using A = typename RegAcc<T>::type;
     extern __shared__ __align__(16) unsigned char smraw[];
-    A *reg = reinterpret_cast<A *>(smraw);                                  // LR_X * LR_Y * LR_Z
-    T *t0 = reinterpret_cast<T *>(smraw + sizeof(A) * LR_X * LR_Y * LR_Z); // LB_X * LB_Y * LB_Z
-    T *t1 = t0 + LB_X * LB_Y * LB_Z;                                        // T1X * LB_Y * LB_Z
-    T *t2 = t1 + T1X * LB_Y * LB_Z;                                         // T1X * T2Y * LB_Z
+    A *reg = reinterpret_cast<A *>(smraw);                                      // LR_X * LR_Y * LR_Z
+    T *tbuf = reinterpret_cast<T *>(smraw + sizeof(A) * LR_X * LR_Y * LR_Z);    // 2 x TILE_ELEMS
     const int bz_n = N / LB_Z, by_n = N / LB_Y;
-    const int bz = blockIdx.x % bz_n, by = (blockIdx.x / bz_n) % by_n, bx = blockIdx.x / (bz_n * by_n);
-    const int x0 = bx * LB_X, y0 = by * LB_Y, z0 = bz * LB_Z;
-    const long rp = N + 2;  // displacement grids: padded reference layout
-    for (int i = threadIdx.x; i < LR_X * LR_Y * LR_Z; i += blockDim.x) reg[i] = 0;
-    // cooperative, independent loads of the three tiles (rows of LB_Z contiguous values)
-    for (int i = threadIdx.x; i < LB_X * LB_Y * LB_Z; i += blockDim.x) {
-        const int lz = i % LB_Z, ly = (i / LB_Z) % LB_Y, lx = i / (LB_Z * LB_Y);
-        t0[i] = __ldg(d0 + ((long)(x0 + lx) * N + y0 + ly) * rp + z0 + lz);
+    const int nbricks = (N / LB_X) * by_n * bz_n;
+    for (int i = threadIdx.x; i < LR_X * LR_Y * LR_Z; i += LB_THREADS) reg[i] = 0;
+    int b = blockIdx.x;
+    if (b < nbricks) {
+        const int bz = b % bz_n, by = (b / bz_n) % by_n, bx = b / (bz_n * by_n);
+        stage_tiles<T>(tbuf, N, rpd, bx * LB_X, by * LB_Y, bz * LB_Z, d0, d1, d2);
     }
-    for (int i = threadIdx.x; i < T1X * LB_Y * LB_Z; i += blockDim.x) {
-        const int lz = i % LB_Z, ly = (i / LB_Z) % LB_Y, lx = i / (LB_Z * LB_Y);
-        t1[i] = __ldg(d1 + ((long)wrapn(x0 - TH + lx, N) * N + y0 + ly) * rp + z0 + lz);
-    }
-    for (int i = threadIdx.x; i < T1X * T2Y * LB_Z; i += blockDim.x) {
-        const int lz = i % LB_Z, ly = (i / LB_Z) % T2Y, lx = i / (LB_Z * T2Y);
-        t2[i] = __ldg(d2 + ((long)wrapn(x0 - TH + lx, N) * N + wrapn(y0 - TH + ly, N)) * rp + z0 + lz);
-    }
-    __syncthreads();
-    const T Nf = (T)N;
-    const float Lf = (float)boxlen;
+    cp_async_commit();
     const int lz = threadIdx.x % LB_Z, ly = (threadIdx.x / LB_Z) % LB_Y, lxb = threadIdx.x / (LB_Z * LB_Y);
 #pragma unroll 1
-    for (int rep = 0; rep < (LB_X * LB_Y * LB_Z) / LB_THREADS; rep++) {
-        const int lx = lxb + rep * (LB_THREADS / (LB_Z * LB_Y));
-        const int x = x0 + lx, y = y0 + ly, z = z0 + lz;
-        float p0 = x * spacing, p1 = y * spacing, p2 = z * spacing;  // src/particle.c:114-116
-        // direction 0: on nodes (stencil folded into d0)
-        p0 = (float)((T)p0 - t0[(lx * LB_Y + ly) * LB_Z + lz]);
-        // direction 1: x off node (src/grids_interp.c:269-306), y and z on nodes (folded into d1)
-        const T Xg = (T)p0 * ginv;
-        const int nx = ifloor<T>(Xg + (T)0.5);
-        const int ix = nx - 1 - (x0 - TH);  // tile x index of the first stencil node
-        bool tiled = ix >= 0 && ix + 2 < T1X;
-        T wx[3], wy[3];
-        if (tiled) {
-            tsc_w<T>(Xg - (T)nx, wx);
-            const T *r1 = t1 + (ix * LB_Y + ly) * LB_Z + lz;
-            p1 = (float)((T)p1 - (wx[0] * r1[0] + wx[1] * r1[LB_Y * LB_Z] + wx[2] * r1[2 * LB_Y * LB_Z]));
-            // direction 2: x and y off nodes, z on nodes (folded into d2)
-            const T Yg = (T)p1 * ginv;
-            const int ny = ifloor<T>(Yg + (T)0.5);
-            const int iy = ny - 1 - (y0 - TH);
-            tiled = iy >= 0 && iy + 2 < T2Y;
+    for (int buf = 0; b < nbricks; b += gridDim.x, buf ^= 1) {
+        const int bz = b % bz_n, by = (b / bz_n) % by_n, bx = b / (bz_n * by_n);
+        const int x0 = bx * LB_X, y0 = by * LB_Y, z0 = bz * LB_Z;
+        const int bn = b + gridDim.x;
+        if (bn < nbricks) {
+            const int nz = bn % bz_n, ny = (bn / bz_n) % by_n, nx = bn / (bz_n * by_n);
+            stage_tiles<T>(tbuf + (buf ^ 1) * TILE_ELEMS, N, rpd, nx * LB_X, ny * LB_Y, nz * LB_Z, d0, d1, d2);
+        }
+        cp_async_commit();
+        cp_async_wait_prev();
+        __syncthreads();  // this brick's tiles have landed; the accumulators are zero
+        const T *t0 = tbuf + buf * TILE_ELEMS;
+        const T *t1 = t0 + LB_X * LB_Y * LB_Z;
+        const T *t2 = t1 + T1X * LB_Y * LB_Z;
+#pragma unroll 1
+        for (int rep = 0; rep < (LB_X * LB_Y * LB_Z) / LB_THREADS; rep++) {
+            const int lx = lxb + rep * (LB_THREADS / (LB_Z * LB_Y));
+            const int x = x0 + lx, y = y0 + ly, z = z0 + lz;
+            float p0 = x * spacing, p1 = y * spacing, p2 = z * spacing;  // src/particle.c:114-116
+            // direction 0: on nodes (stencil folded into d0)
+            p0 = (float)((T)p0 - t0[(lx * LB_Y + ly) * LB_Z + lz]);
+            // direction 1: x off node (src/grids_interp.c:269-306), y and z on nodes (folded into d1)
+            const T Xg = (T)p0 * ginv;
+            const int nx = ifloor<T>(Xg + (T)0.5);
+            const int ix = nx - 1 - (x0 - TH);  // tile x index of the first stencil node
+            bool tiled = ix >= 0 && ix + 2 < T1X;
+            T wx[3], wy[3];
             if (tiled) {
-                tsc_w<T>(Yg - (T)ny, wy);
-                T sv = 0;
+                tsc_w<T>(Xg - (T)nx, wx);
+                const T *r1 = t1 + (ix * LB_Y + ly) * LB_Z + lz;
+                p1 = (float)((T)p1 - (wx[0] * r1[0] + wx[1] * r1[LB_Y * LB_Z] + wx[2] * r1[2 * LB_Y * LB_Z]));
+                // direction 2: x and y off nodes, z on nodes (folded into d2)
+                const T Yg = (T)p1 * ginv;
+                const int ny = ifloor<T>(Yg + (T)0.5);
+                const int iy = ny - 1 - (y0 - TH);
+                tiled = iy >= 0 && iy + 2 < T2Y;
+                if (tiled) {
+                    tsc_w<T>(Yg - (T)ny, wy);
+                    T sv = 0;
 #pragma unroll
-                for (int i = 0; i < 3; i++) {
-                    const T *r2 = t2 + ((ix + i) * T2Y + iy) * LB_Z + lz;
-                    sv += wx[i] * (wy[0] * r2[0] + wy[1] * r2[LB_Z] + wy[2] * r2[2 * LB_Z]);
+                    for (int i = 0; i < 3; i++) {
+                        const T *r2 = t2 + ((ix + i) * T2Y + iy) * LB_Z + lz;
+                        sv += wx[i] * (wy[0] * r2[0] + wy[1] * r2[LB_Z] + wy[2] * r2[2 * LB_Z]);
+                    }
+                    p2 = (float)((T)p2 - sv);
                 }
-                p2 = (float)((T)p2 - sv);
+            }
+            if (!tiled) {
+                // restart the off-node gathers from global memory
+                p1 = y * spacing;
+                p2 = z * spacing;
+                displace_global<T>(N, rpd, ginv, d1, d2, y, z, p0, p1, p2);
+            }
+            p0 = fwrapf(p0, Lf);
+            p1 = fwrapf(p1, Lf);
+            p2 = fwrapf(p2, Lf);
+            if (pos_out) {
+                const long id = ((long)x * N + y) * N + z;
+                pos_out[3 * id] = p0;
+                pos_out[3 * id + 1] = p1;
+                pos_out[3 * id + 2] = p2;
+            }
+            // CIC (analyse/src/mitos_read.c:288-333), one unit of mean density per particle (M = N)
+            const T X = (T)p0 * ginv, Y = (T)p1 * ginv, Z = (T)p2 * ginv;
+            const int iX = ifloor<T>(X), iY = ifloor<T>(Y), iZ = ifloor<T>(Z);
+            const T dx = X - iX, dy = Y - iY, dz = Z - iZ;
+            const int rx = wrapn(iX - x0 + 1, N), ry = wrapn(iY - y0 + 1, N), rz = wrapn(iZ - z0 + LR_Z0, N);
+            if (rx < LR_X - 1 && ry < LR_Y - 1 && rz < LR_Z - 1) {
+                A *c = reg + (rx * LR_Y + ry) * LR_Z + rz;
+                const T tx = 1 - dx, ty = 1 - dy, tz = 1 - dz;
+                RegAcc<T>::add(c, tx * ty * tz);
+                RegAcc<T>::add(c + 1, tx * ty * dz);
+                RegAcc<T>::add(c + LR_Z, tx * dy * tz);
+                RegAcc<T>::add(c + LR_Z + 1, tx * dy * dz);
+                RegAcc<T>::add(c + LR_Y * LR_Z, dx * ty * tz);
+                RegAcc<T>::add(c + LR_Y * LR_Z + 1, dx * ty * dz);
+                RegAcc<T>::add(c + LR_Y * LR_Z + LR_Z, dx * dy * tz);
+                RegAcc<T>::add(c + LR_Y * LR_Z + LR_Z + 1, dx * dy * dz);
+            } else {
+                cic_global<T>(rho, N, rpo, iX, iY, iZ, dx, dy, dz);
             }
         }
-        if (!tiled) {
-            // restart the off-node gathers from global memory
-            p1 = y * spacing;
-            p2 = z * spacing;
-            displace_global<T>(N, Nf, boxlen, d1, d2, y, z, p0, p1, p2);
-        }
-        p0 = fwrapf(p0, Lf);
-        p1 = fwrapf(p1, Lf);
-        p2 = fwrapf(p2, Lf);
-        if (pos_out) {
-            const long id = ((long)x * N + y) * N + z;
-            pos_out[3 * id] = p0;
-            pos_out[3 * id + 1] = p1;
-            pos_out[3 * id + 2] = p2;
-        }
-        // CIC (analyse/src/mitos_read.c:288-333), one unit of mean density per particle (M = N)
-        const T X = (T)p0 * ginv, Y = (T)p1 * ginv, Z = (T)p2 * ginv;
-        const int iX = ifloor<T>(X), iY = ifloor<T>(Y), iZ = ifloor<T>(Z);
-        const T dx = X - iX, dy = Y - iY, dz = Z - iZ;
-        const int rx = wrapn(iX - x0 + 1, N), ry = wrapn(iY - y0 + 1, N), rz = wrapn(iZ - z0 + LR_Z0, N);
-        if (rx < LR_X - 1 && ry < LR_Y - 1 && rz < LR_Z - 1) {
-            A *c = reg + (rx * LR_Y + ry) * LR_Z + rz;
-            const T tx = 1 - dx, ty = 1 - dy, tz = 1 - dz;
-            RegAcc<T>::add(c, tx * ty * tz);
-            RegAcc<T>::add(c + 1, tx * ty * dz);
-            RegAcc<T>::add(c + LR_Z, tx * dy * tz);
-            RegAcc<T>::add(c + LR_Z + 1, tx * dy * dz);
-            RegAcc<T>::add(c + LR_Y * LR_Z, dx * ty * tz);
-            RegAcc<T>::add(c + LR_Y * LR_Z + 1, dx * ty * dz);
-            RegAcc<T>::add(c + LR_Y * LR_Z + LR_Z, dx * dy * tz);
-            RegAcc<T>::add(c + LR_Y * LR_Z + LR_Z + 1, dx * dy * dz);
-        } else {
-            cic_global<T>(rho, N, rpo, iX, iY, iZ, dx, dy, dz);
-        }
-    }
-    __syncthreads();
-    // flush: rows of LR_Z cells starting at z0 - 4 (a multiple of 4, so 16-byte aligned with the
-    // 16-byte aligned row pitch rpo)
-    constexpr int Q = LR_Z / 4;
-    for (int i = threadIdx.x; i < LR_X * LR_Y * Q; i += blockDim.x) {
-        const int qz = i % Q, qy = (i / Q) % LR_Y, qx = i / (Q * LR_Y);
-        const A *c = reg + (qx * LR_Y + qy) * LR_Z + 4 * qz;
-        if (c[0] == (A)0 && c[1] == (A)0 && c[2] == (A)0 && c[3] == (A)0) continue;
-        T v[4];
-#pragma unroll
-        for (int k = 0; k < 4; k++) v[k] = RegAcc<T>::value(c[k]);
-        const long row = ((long)wrapn(x0 - 1 + qx, N) * N + wrapn(y0 - 1 + qy, N)) * rpo;
-        const int gz = z0 - LR_Z0 + 4 * qz;
-        if constexpr (sizeof(T) == 4) {
-            if (gz >= 0 && gz + 3 < N) {
-                red_add_v4((float *)rho + row + gz, (float)v[0], (float)v[1], (float)v[2], (float)v[3]);
-                continue;
+        __syncthreads();
+        // flush and re-zero: rows of LR_Z cells starting at z0 - 4 (a multiple of 4, so 16-byte
+        // aligned with the 16-byte aligned row pitch rpo)
+        constexpr int Q = LR_Z / 4;
+        for (int i = threadIdx.x; i < LR_X * LR_Y * Q; i += LB_THREADS) {
+            const int qz = i % Q, qy = (i / Q) % LR_Y, qx = i / (Q * LR_Y);
+            A *c = reg + (qx * LR_Y + qy) * LR_Z + 4 * qz;
+            const A c0 = c[0], c1 = c[1], c2 = c[2], c3 = c[3];
+            if (c0 == (A)0 && c1 == (A)0 && c2 == (A)0 && c3 == (A)0) continue;
+            c[0] = 0; c[1] = 0; c[2] = 0; c[3] = 0;
+            const T v[4] = {RegAcc<T>::value(c0), RegAcc<T>::value(c1), RegAcc<T>::value(c2), RegAcc<T>::value(c3)};
+            const long row = ((long)wrapn(x0 - 1 + qx, N) * N + wrapn(y0 - 1 + qy, N)) * rpo;
+            const int gz = z0 - LR_Z0 + 4 * qz;
+            if constexpr (sizeof(T) == 4) {
+                if (gz >= 0 && gz + 3 < N) {
+                    red_add_v4((float *)rho + row + gz, (float)v[0], (float)v[1], (float)v[2], (float)v[3]);
+                    continue;
+                }
             }
-        }
 #pragma unroll
-        for (int k = 0; k < 4; k++)
-            if (v[k] != (T)0) atomicAdd(rho + row + wrapn(gz + k, N), v[k]);
+            for (int k = 0; k < 4; k++)
+                if (v[k] != (T)0) atomicAdd(rho + row + wrapn(gz + k, N), v[k]);
+        }
+        // the zeroed accumulators and the free tile buffer are published by the barrier at the
+        // top of the next brick
     }
+    cp_async_wait_all();
 }
 
 static size_t lattice_smem(size_t elem) {
     // the region accumulators have the size of one element in either precision
-    return elem * ((size_t)LR_X * LR_Y * LR_Z + LB_X * LB_Y * LB_Z + (size_t)T1X * LB_Y * LB_Z +
-                   (size_t)T1X * T2Y * LB_Z);
+    return elem * ((size_t)LR_X * LR_Y * LR_Z + 2 * (size_t)TILE_ELEMS);
+}
+
+template <typename T>
+static int lattice_launch(int N, int rpd, int rpo, float spacing, float Lf, double ginv, const void *d0, const void *d1,
+                          const void *d2, void *rho, float *pos_out) {
+    static int blocks_per_sm[2] = {0, 0};  // per precision, for the current device
+    static int sms = 0;
+    const size_t smem = lattice_smem(sizeof(T));
+    auto kern = k_lattice_cic<T>;
+    int &bps = blocks_per_sm[sizeof(T) == 4];
+    if (!bps) {
+        MITOS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int dev = 0;
+        MITOS_CUDA(cudaGetDevice(&dev));
+        MITOS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        MITOS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, LB_THREADS, smem));
+        if (bps < 1) bps = 1;
+    }
+    const long nbricks = (long)(N / LB_X) * (N / LB_Y) * (N / LB_Z);
+    const unsigned blocks = (unsigned)std::min<long>(nbricks, (long)sms * bps);
+    kern<<<blocks, LB_THREADS, smem, stream()>>>(N, rpd, rpo, spacing, Lf, (T)ginv, (const T *)d0, (const T *)d1,
+                                                 (const T *)d2, (T *)rho, pos_out);
+    return 0;
 }
 
 int lattice_deposit(int N, double boxlen, int precision, const void *d0, const void *d1, const void *d2,
-                    void *rho, int rho_pitch, float *pos_out) {
-    if (N % LB_Z || N % LB_Y || N % LB_X || (rho_pitch * (precision == MITOS_FP32 ? 4 : 8)) % 16) return 3;
+                    int disp_pitch, void *rho, int rho_pitch, float *pos_out) {
+    const size_t es = precision == MITOS_FP32 ? 4 : 8;
+    if (N % LB_Z || N % LB_Y || N % LB_X || (rho_pitch * es) % 16 || (disp_pitch * es) % 16 ||
+        ((uintptr_t)d0 | (uintptr_t)d1 | (uintptr_t)d2 | (uintptr_t)rho) % 16)
+        return 3;
     const float Lf = (float)boxlen;
     const float spacing = Lf / N;  // src/particle.c:102-103 with M = N
-    const double gfac = boxlen / N;
-    const unsigned blocks = (unsigned)((N / LB_X) * (N / LB_Y) * (N / LB_Z));
     launch_begin("lattice_cic");
-    if (precision == MITOS_FP32) {
-        const size_t smem = lattice_smem(sizeof(float));
-        MITOS_CUDA(cudaFuncSetAttribute(k_lattice_cic<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_lattice_cic<float><<<blocks, LB_THREADS, smem, stream()>>>(N, rho_pitch, spacing, (float)boxlen, (float)gfac,
-                                                                     (float)(N / boxlen), (const float *)d0, (const float *)d1,
-                                                                     (const float *)d2, (float *)rho, pos_out);
-    } else {
-        const size_t smem = lattice_smem(sizeof(double));
-        MITOS_CUDA(cudaFuncSetAttribute(k_lattice_cic<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_lattice_cic<double><<<blocks, LB_THREADS, smem, stream()>>>(N, rho_pitch, spacing, boxlen, gfac,
-                                                                      (double)N / boxlen, (const double *)d0, (const double *)d1,
-                                                                      (const double *)d2, (double *)rho, pos_out);
-    }
+    const int e = precision == MITOS_FP32
+                      ? lattice_launch<float>(N, disp_pitch, rho_pitch, spacing, Lf, N / boxlen, d0, d1, d2, rho, pos_out)
+                      : lattice_launch<double>(N, disp_pitch, rho_pitch, spacing, Lf, N / boxlen, d0, d1, d2, rho, pos_out);
+    if (e) return e;
     count_launch();
     MITOS_LAUNCH_CHECK("lattice CIC");
     return 0;

@@ -9,8 +9,9 @@ int displace_and_deposit(int N, int M, double boxlen, int precision, const void 
                          const void *d2, void *rho, float *pos_out);
 // lattice-aligned fast path (M = N, exact nodes); the displacement grids must carry the folded
 // on-node TSC stencils (PassArgs::stencil in the displacement passes)
+// disp_pitch / rho_pitch: row pitches (elements) of the displacement grids and of rho, 16-byte multiples
 int lattice_deposit(int N, double boxlen, int precision, const void *d0, const void *d1, const void *d2,
-                    void *rho, int rho_pitch, float *pos_out);
+                    int disp_pitch, void *rho, int rho_pitch, float *pos_out);
 bool lattice_aligned(int N, int M, double boxlen);
 // CIC of n given positions with per-particle value val
 int cic_positions(long n, int N, double boxlen, int precision, const float *pos, double val, void *rho);

@@ -94,7 +94,12 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     void *phi = workspace(gb, 0), *S = workspace(gb, 10), *Sk = workspace(gb, 11), *rho = workspace(gb, 12);
     void *A0 = workspace(gb, 1), *A1 = workspace(gb, 2);
     void *B0 = workspace(gb, 4), *B1 = workspace(gb, 5), *B2 = workspace(gb, 6);
-    void *D0 = workspace(gb, 7), *D1 = workspace(gb, 8), *D2 = workspace(gb, 9);
+    // displacement grids: row pitch N + 4 on the lattice-aligned path (16-byte aligned rows for
+    // the staged tile copies of the deposit), the reference's N + 2 otherwise
+    const bool aligned = lattice_aligned(N, M, L);
+    const int disp_pitch = aligned ? N + 4 : N + 2;
+    const size_t db = (size_t)N * N * disp_pitch * sizeof(T);
+    void *D0 = workspace(db, 7), *D1 = workspace(db, 8), *D2 = workspace(db, 9);
     if (!phi || !S || !Sk || !rho || !A0 || !A1 || !B0 || !B1 || !B2 || !D0 || !D1 || !D2) return 5;
     const long n2max = 3L * (N / 2) * (N / 2);
     T *filt = (T *)workspace(sizeof(T) * (n2max + 1), 106);
@@ -220,7 +225,6 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     }
 
     // S4: displacement grids d_i = c2r(i k_i phi W^-3) (src/mitos.c:395-416)
-    const bool aligned = lattice_aligned(N, M, L);
     memset(&a, 0, sizeof a);
     a.dk = dk;
     a.scale = 1.0;
@@ -246,7 +250,7 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     a.out[0] = D0;
     a.out[1] = D1;
     a.out[2] = D2;
-    a.rp_out = N + 2;
+    a.rp_out = disp_pitch;
     a.scale = 1.0 / V;
     e = launch_z_c2r<T>(g, ZOP_DISP, a);
     if (e) return e;
@@ -264,7 +268,7 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     void *rhoD = aligned ? workspace(rho_bytes, 15) : rho;
     if (!rhoD) return 5;
     MITOS_CUDA(cudaMemsetAsync(rhoD, 0, rho_bytes, stream()));
-    e = aligned ? lattice_deposit(N, L, prec, D0, D1, D2, rhoD, rho_pitch, dpos)
+    e = aligned ? lattice_deposit(N, L, prec, D0, D1, D2, disp_pitch, rhoD, rho_pitch, dpos)
                 : displace_and_deposit(N, M, L, prec, D0, D1, D2, rhoD, dpos);
     if (e) return e;
     tim.mark();
