@@ -245,6 +245,16 @@ template <int D> __device__ __forceinline__ int spad_plus(int i, int si) {
     else return spad(i + D);
 }
 
+// Exchange slot of element i of a pencil.  With pencils interleaved across the lanes (SN > 1)
+// or a runtime length: the padded index i + i/8.  With one pencil per (half-)warp (SN == 1, the
+// Z passes): an XOR swizzle of bits 0-3 by bits 3-6, under which the stage writes (stride Nsp)
+// and the contiguous stage reads of 8-byte elements fill each half-warp's 128-byte wavefront
+// without bank conflicts.
+template <int NL, int SN> __device__ __forceinline__ int xpos(int i) {
+    if constexpr (NL > 0 && SN == 1) return i ^ ((i >> 3) & 3) ^ (((i >> 5) & 3) << 2);
+    else return spad(i);
+}
+
 template <typename T, int E, int SIGN, int NL, int SN, int S>
 struct CTStage {
     using Sch = CTSched<NL, E>;
@@ -259,7 +269,10 @@ struct CTStage {
             for (int b = 0; b < E / Rp; b++) {
                 const int j = t + b * (NL / E);
                 const int idxD = (j / Nsp) * Nsp * Rp + (j % Nsp);
-                if constexpr (Nsp == 1 && Rp <= 8) {
+                if constexpr (SN == 1) {
+#pragma unroll
+                    for (int r = 0; r < Rp; r++) sm[xpos<NL, SN>(idxD + r * Nsp)] = v[b * Rp + r];
+                } else if constexpr (Nsp == 1 && Rp <= 8) {
                     // idxD = j Rp and the Rp outputs stay in one padding group when Rp divides 8
                     const int base = spad(idxD);
 #pragma unroll
@@ -284,7 +297,8 @@ struct CTStage {
 #pragma unroll
                 for (int r = 0; r < R; r++) {
                     constexpr int D = NL / R;
-                    const int o = ((D % 8) == 0) ? base + r * D + (r * D) / 8 : spad(j + r * D);
+                    const int o = (SN == 1) ? xpos<NL, SN>(j + r * D)
+                                  : ((D % 8) == 0) ? base + r * D + (r * D) / 8 : spad(j + r * D);
                     cplx<T> x = sm[o * SN];
                     if (r > 0) {
                         cplx<T> w = __ldg(tw + r * step);

@@ -15,8 +15,17 @@ template <> __device__ __forceinline__ double dev_sqrt<double>(double x) { retur
 // X and Y passes: complex FFTs along a strided axis.  Block = P pencils; thread (t, p) with
 // p fastest so that a warp reads P consecutive columns of each row.
 // ------------------------------------------------------------------------------------------
+// The multi-output Y passes (Hessian, displacement) keep their per-pass twiddles and exchange
+// offsets in registers across the repeated transforms when the length is a compile-time
+// constant: they run 256-thread blocks with up to 128 registers.  Everything else runs
+// 512-thread blocks with up to 64 (the X passes need the wider pencil groups for coalescing:
+// their pencils are adjacent columns of an x-plane).
+template <int AXIS, int OP, int NL> constexpr bool strided_heavy() {
+    return NL > 0 && AXIS == 1 && (OP == YOP_HESS || OP == YOP_DISP);
+}
+
 template <typename T, int E, int SIGN, int AXIS, int OP, int NL, int PC>
-__global__ void __launch_bounds__(512, 2) k_strided(GridGeom g, PassArgs a, const T *__restrict__ win) {
+__global__ void __launch_bounds__(strided_heavy<AXIS, OP, NL>() ? 256 : 512, 2) k_strided(GridGeom g, PassArgs a, const T *__restrict__ win) {
     extern __shared__ __align__(16) unsigned char smraw[];
     cplx<T> *sm = reinterpret_cast<cplx<T> *>(smraw);
     const FFTPlan &pl = g.plN;
@@ -404,13 +413,13 @@ __global__ void __launch_bounds__(256) k_z_r2c(GridGeom g, PassArgs a) {
     }
     fft_any<T, E, -1, NL, 1>(pl, v, psm, 1, t, tw);
 #pragma unroll
-    for (int e = 0; e < E; e++) psm[spad(nout_any<NL, E>(pl, t, e))] = v[e];
+    for (int e = 0; e < E; e++) psm[xpos<NL, 1>(nout_any<NL, E>(pl, t, e))] = v[e];
     __syncthreads();
     if (!valid) return;
     cplx<T> *dst = reinterpret_cast<cplx<T> *>(a.out[0]) + row * H;
     for (int k = t; k <= h; k += tpp) {
-        const cplx<T> Z = psm[spad(k == h ? 0 : k)];
-        const cplx<T> Zc = psm[spad(k == 0 ? 0 : h - k)];
+        const cplx<T> Z = psm[xpos<NL, 1>(k == h ? 0 : k)];
+        const cplx<T> Zc = psm[xpos<NL, 1>(k == 0 ? 0 : h - k)];
         // even = (Z + conj Zc)/2, odd = (Z - conj Zc)/(2i), X = even + e^{-2 pi i k/N} odd
         const cplx<T> ev = mk<T>((T)0.5 * (Z.x + Zc.x), (T)0.5 * (Z.y - Zc.y));
         const cplx<T> od = mk<T>((T)0.5 * (Z.y + Zc.y), (T)-0.5 * (Z.x - Zc.x));
@@ -447,6 +456,9 @@ static int launch_strided(const GridGeom &g, const PassArgs &a, const T *win) {
         return launch_strided_e<T, 12, SIGN, AXIS, OP, 0, 0>(g, a, win);
     }
 }
+
+// pencils per block of the multi-output Y passes of the compile-time lengths (256 threads)
+template <int NL, int PC> constexpr int pc_heavy() { return NL > 0 ? PC / 2 : PC; }
 
 template <typename T, int NL, int PC>
 int launch_x_t(const GridGeom &g, XOp op, int sign, const PassArgs &a) {
@@ -486,12 +498,12 @@ int launch_x_t(const GridGeom &g, XOp op, int sign, const PassArgs &a) {
 
 template <typename T, int NL, int PC>
 int launch_y_t(const GridGeom &g, YOp op, int sign, const PassArgs &a) {
+    constexpr int PCH = pc_heavy<NL, PC>();
     switch (op) {
     case YOP_PLAIN:
         return sign < 0 ? launch_strided<T, -1, 1, YOP_PLAIN, NL, PC>(g, a, nullptr) : launch_strided<T, 1, 1, YOP_PLAIN, NL, PC>(g, a, nullptr);
-    // the six-output Y pass stays on the runtime plan: fully unrolled stages spill at 64 registers
-    case YOP_HESS: return launch_strided<T, 1, 1, YOP_HESS, 0, 0>(g, a, nullptr);
-    case YOP_DISP: return launch_strided<T, 1, 1, YOP_DISP, NL, PC>(g, a, nullptr);
+    case YOP_HESS: return launch_strided<T, 1, 1, YOP_HESS, NL, PCH>(g, a, nullptr);
+    case YOP_DISP: return launch_strided<T, 1, 1, YOP_DISP, NL, PCH>(g, a, nullptr);
     }
     return 3;
 }
