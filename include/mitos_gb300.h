@@ -271,6 +271,11 @@ struct ic_result {
 int ic_pipeline_run(const struct ic_config *cfg, const struct perturb_spline *spline,
                     struct ic_result *res);
 /* The same on caller-provided host table arrays (convenience for bindings without structs). */
+int ic_pipeline_run_table(const struct ic_config *cfg, int k_size, int tau_size,
+                          int n_functions, const double *k, const double *log_tau,
+                          const double *redshift, const double *D_growth, const double *delta,
+                          struct ic_result *res);
+
 /* P(k) binning that allocates no device memory.  No counterpart in the reference: for callers
  * that must not allocate device memory in their loop, because another allocator already holds
  * the device's memory or because cudaMalloc / cudaFree would synchronise a streaming pipeline.
@@ -283,10 +288,68 @@ int ic_pipeline_run(const struct ic_config *cfg, const struct perturb_spline *sp
 int calc_cross_powerspec_noalloc(int N, double boxlen, const void *dev_box1, const void *dev_box2,
                                  int precision, int bins, int linear, double *k_in_bins,
                                  double *power_in_bins, long *obs_in_bins);
-int ic_pipeline_run_table(const struct ic_config *cfg, int k_size, int tau_size,
-                          int n_functions, const double *k, const double *log_tau,
-                          const double *redshift, const double *D_growth, const double *delta,
-                          struct ic_result *res);
+
+/* ---- Learned Monge-Ampere warm start (no reference counterpart) ----------------------------
+ * A 3D convolutional network: 4 periodic 3x3x3 layers, channels 3 -> 16 -> 16 -> 16 -> 1, ReLU
+ * after the first three; BF16 weights and activations on the tensor cores with FP32 accumulation.
+ * Inputs: delta(x), the 1LPT potential phi_1(x) = c2r(-delta/k^2) and the 2LPT potential
+ * phi_2(x) = c2r(-S(k)/k^2) (S the 2LPT source, src/2lpt.c:111-112).  Output: a source-space
+ * correction sigma(x); the warm start adds G(k) r2c(sigma) to phi(k) after the first cycle.
+ * Grids are FP32 device arrays of row pitch `pitch` (N for packed, N + 2 for the padded real
+ * grids of struct distributed_grid); N must be a multiple of 32. */
+#define MANET_PARAMS 27712 /* 4 x (27 * 16 * 16 weights + 16 biases), channel padded */
+struct manet {
+    float scale_in[3]; /* delta, phi_1, phi_2 are divided by these before the first layer */
+    float scale_out;   /* the network output is multiplied by this */
+    int steps;         /* Adam steps taken */
+    void *priv;        /* device parameters, gradients and Adam moments */
+};
+/* He-normal initial weights from a splitmix64 stream of `seed`; scales 1 */
+int manet_init(struct manet *net, unsigned long long seed);
+int manet_free(struct manet *net);
+/* FP32 parameters, layer by layer: w[t][ci][co] (27 x 16 x 16, taps t = (dx+1)*9 + (dy+1)*3 +
+ * (dz+1)) then b[16]; entries of padded channels are zero */
+int manet_get_params(const struct manet *net, float *host);
+int manet_set_params(struct manet *net, const float *host);
+/* gradients of the last manet_loss_grad / manet_train_step, same layout */
+int manet_get_grads(const struct manet *net, float *host);
+/* loss = mean over voxels of (net(inputs) - target / scale_out)^2 and its gradients */
+int manet_loss_grad(struct manet *net, int N, int pitch, const float *delta, const float *phi1,
+                    const float *phi2, const float *target, double *loss);
+/* manet_loss_grad followed by one Adam step (beta 0.9 / 0.999) of learning rate lr */
+int manet_train_step(struct manet *net, int N, int pitch, const float *delta, const float *phi1,
+                     const float *phi2, const float *target, float lr, double *loss);
+/* out = scale_out * net(inputs) */
+int manet_infer(struct manet *net, int N, int pitch, const float *delta, const float *phi1,
+                const float *phi2, float *out);
+
+/* Monge-Ampere to a tolerance (no reference counterpart; the cycle of src/monge_ampere.c:50-183
+ * with phi kept in k space: phi(k) += G(k) r2c(res)(k)).  Stops when the relative rms residual
+ * rel = sqrt(sum res^2 / sum rho^2) is <= tol; the reference's eps (src/monge_ampere.c:177) is
+ * rel / N^(3/2).  dens: density in momentum space with rho(x) in its box (as solveMongeAmpere);
+ * pot->fbox receives phi(k).  warm: NULL for the reference's Zel'dovich start
+ * (src/monge_ampere.c:87), or a trained network whose correction is added after the first
+ * update (FP32 grids).  Returns 0, or 7 when max_cycles updates leave rel above tol. */
+struct ma_stats {
+    int cycles;         /* phi updates applied (the network correction not counted) */
+    int evaluations;    /* residual evaluations (six-Hessian passes) */
+    double rel;         /* last relative rms residual */
+    double eps;         /* the reference's eps of the last evaluation: rel / N^(3/2) */
+    double rel_first;   /* residual of the Zel'dovich start */
+    double rel_second;  /* residual after the first update (and the network correction, if warm) */
+    double ms;          /* device time of the call (CUDA events) */
+    double ms_warm;     /* of which the warm start: 2LPT potential, network inference, correction */
+};
+int solveMongeAmpereTol(struct distributed_grid *potential, struct distributed_grid *density,
+                        struct distributed_grid *workspace, double tol, int max_cycles,
+                        struct manet *warm, struct ma_stats *stats);
+/* One training pair for the network from a density (FP32 grids): the cold iteration runs
+ * `cycles` updates; outputs are device FP32 real grids of N*N*(N+2) floats (pitch N+2):
+ * delta(x), phi_1(x), phi_2(x) (the inputs) and sigma(x) = lap(phi_final - phi_after_first_update),
+ * the source-space correction the network learns. */
+int manet_training_pair(struct distributed_grid *potential, struct distributed_grid *density,
+                        struct distributed_grid *workspace, int cycles, float *delta, float *phi1,
+                        float *phi2, float *sigma, struct ma_stats *stats);
 
 #ifdef __cplusplus
 }

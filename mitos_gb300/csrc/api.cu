@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "context.cuh"
+#include "grids.cuh"
 #include "kspace.cuh"
 #include "particles.cuh"
 
@@ -13,7 +14,6 @@ using namespace mitos;
 
 static int g_default_precision = MITOS_FP64;
 
-static inline size_t csize(int prec) { return prec == MITOS_FP32 ? 8 : 16; }
 static inline size_t grid_bytes(const struct distributed_grid *dg) {
     return (size_t)dg->local_size * csize(dg->precision);
 }
@@ -74,7 +74,7 @@ int grid_r2c(const GridGeom &g, int prec, double boxlen, const void *box, int rp
 // six Hessian components of phi (k space) through the fused X / Y / Z passes into out (real);
 // ZOP_HESS_2LPT writes the second-order source, ZOP_HESS_MA the Monge-Ampere residual
 int grid_hessian(const GridGeom &g, int prec, double boxlen, const void *phi, int zop,
-                 const void *rho, void *out, double *red, int window_order) {
+                 const void *rho, void *out, double *red, int window_order, void *out2) {
     const size_t gb = (size_t)g.cells * csize(prec);
     void *A[3], *B[6];
     for (int i = 0; i < 3; i++) if (!(A[i] = workspace(gb, 1 + i))) return 5;
@@ -95,6 +95,7 @@ int grid_hessian(const GridGeom &g, int prec, double boxlen, const void *phi, in
     if (e) return e;
     for (int i = 0; i < 6; i++) a.in[i] = B[i];
     a.out[0] = out;
+    a.out[1] = out2;
     a.in2 = rho;
     a.red = red;
     a.rp_in = g.N + 2;

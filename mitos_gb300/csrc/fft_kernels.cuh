@@ -346,7 +346,7 @@ __global__ void __launch_bounds__(256, OP == ZOP_HESS_MA ? 1 : 2) k_z_c2r(GridGe
 #pragma unroll
         for (int e = 0; e < E; e++) {
             const int n = nout_any<NL, E>(pl, t, e);
-            T res2[2];
+            T res2[2], s2v[2];
 #pragma unroll
             for (int c = 0; c < 2; c++) {
                 const T xx = (c ? o[0][e].y : o[0][e].x) * scale;
@@ -357,6 +357,7 @@ __global__ void __launch_bounds__(256, OP == ZOP_HESS_MA ? 1 : 2) k_z_c2r(GridGe
                 const T zz = (c ? o[5][e].y : o[5][e].x) * scale;
                 // second invariant of the Hessian (src/2lpt.c:111-112)
                 const T s2 = zz * yy + zz * xx + yy * xx - xy * xy - yz * yz - xz * xz;
+                s2v[c] = s2;
                 if constexpr (OP == ZOP_HESS_2LPT) {
                     res2[c] = s2;
                 } else {
@@ -370,6 +371,8 @@ __global__ void __launch_bounds__(256, OP == ZOP_HESS_MA ? 1 : 2) k_z_c2r(GridGe
                 }
             }
             *reinterpret_cast<cplx<T> *>(dst + 2 * n) = mk<T>(res2[0], res2[1]);
+            // optional second output: the second-order source S of the same Hessian
+            if (a.out[1]) *reinterpret_cast<cplx<T> *>(reinterpret_cast<T *>(a.out[1]) + row * a.rp_out + 2 * n) = mk<T>(s2v[0], s2v[1]);
         }
         if (t == 0 && a.rp_out > N) { dst[N] = 0; dst[N + 1] = 0; }
         if constexpr (OP == ZOP_HESS_MA) {

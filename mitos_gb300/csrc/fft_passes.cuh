@@ -47,7 +47,8 @@ enum YOp {
 enum ZOp {
     ZOP_C2R = 0,      // real out = c2r(in) * scale
     ZOP_HESS_2LPT,    // 6 in (kz factors 1, 1, i kz, 1, i kz, -kz^2) -> S = sum_{i<j} (p_ii p_jj - p_ij^2)
-    ZOP_HESS_MA,      // same 6 in -> residual (1 + rho) - det(I + H), sums of res^2 and rho^2
+    ZOP_HESS_MA,      // same 6 in -> residual (1 + rho) - det(I + H), sums of res^2 and rho^2;
+                      // out[1] (optional): the second-order source S of the same Hessian
     ZOP_DISP          // 3 in (kz factors 1, 1, i kz) -> 3 real out
 };
 

@@ -1,0 +1,22 @@
+// grids.cuh -- whole-grid transforms shared by the entry points (api.cu), the fused pipeline
+// (pipeline.cu) and the Monge-Ampere solver (ma.cu).
+#pragma once
+
+#include "context.cuh"
+
+namespace mitos {
+
+// fbox (destroyed) -> box (pitch N + 2), FFTW c2r order and the 1/V normalisation (src/fft.c:110-125)
+int grid_c2r(const GridGeom &g, int prec, double boxlen, void *fbox, void *box);
+// box (pitch rp, transformed on load as x * rho_a + rho_b) -> fbox, x V/N^3 (src/fft.c:91-106)
+int grid_r2c(const GridGeom &g, int prec, double boxlen, const void *box, int rp, double rho_a, double rho_b,
+             void *fbox);
+// six Hessian components of phi (k space) through the fused X / Y / Z passes into out (real);
+// ZOP_HESS_2LPT writes the second-order source, ZOP_HESS_MA the Monge-Ampere residual (and, when
+// out2 is given, the second-order source too)
+int grid_hessian(const GridGeom &g, int prec, double boxlen, const void *phi, int zop, const void *rho, void *out,
+                 double *red, int window_order, void *out2 = nullptr);
+int axpby(int prec, long n, double a, const void *x, double b, const void *y, void *out);
+inline size_t csize(int prec) { return prec == MITOS_FP32 ? 8 : 16; }
+
+}  // namespace mitos

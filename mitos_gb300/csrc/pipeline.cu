@@ -16,14 +16,9 @@
 #include <vector>
 
 #include "context.cuh"
+#include "grids.cuh"
 #include "kspace.cuh"
 #include "particles.cuh"
-
-namespace mitos {
-int grid_c2r(const GridGeom &g, int prec, double boxlen, void *fbox, void *box);
-int grid_hessian(const GridGeom &g, int prec, double boxlen, const void *phi, int zop, const void *rho,
-                 void *out, double *red, int window_order);
-}  // namespace mitos
 
 using namespace mitos;
 

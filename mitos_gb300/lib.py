@@ -367,3 +367,103 @@ def kernel_times(max_n: int = 4096):
     ms = np.zeros(max_n)
     n = load().mitos_kernel_times(names, ms.ctypes.data_as(_dp), max_n)
     return [(names[i].decode(), float(ms[i])) for i in range(n)]
+
+
+# ---- learned Monge-Ampere warm start -------------------------------------------------------
+MANET_PARAMS = 27712
+
+
+class Manet(ctypes.Structure):
+    """struct manet: input / output scales, Adam step count, device state."""
+    _fields_ = [("scale_in", ctypes.c_float * 3), ("scale_out", ctypes.c_float), ("steps", ctypes.c_int),
+                ("priv", ctypes.c_void_p)]
+
+
+def _vp(p):
+    """a device pointer from an int, a c_void_p, or a DistributedGrid (its real box)"""
+    if isinstance(p, DistributedGrid):
+        return ctypes.c_void_p(p.box)
+    if isinstance(p, ctypes.c_void_p):
+        return p
+    return ctypes.c_void_p(int(p))
+
+
+def manet_init(seed: int = 1) -> Manet:
+    net = Manet()
+    _check(load().manet_init(ctypes.byref(net), ctypes.c_ulonglong(seed)))
+    return net
+
+
+def manet_free(net: Manet) -> None:
+    load().manet_free(ctypes.byref(net))
+
+
+def manet_params(net: Manet) -> np.ndarray:
+    out = np.zeros(MANET_PARAMS, np.float32)
+    _check(load().manet_get_params(ctypes.byref(net), out.ctypes.data_as(_fp)))
+    return out
+
+
+def manet_set_params(net: Manet, p: np.ndarray) -> None:
+    p = np.ascontiguousarray(p, np.float32)
+    assert p.size == MANET_PARAMS
+    _check(load().manet_set_params(ctypes.byref(net), p.ctypes.data_as(_fp)))
+
+
+def manet_grads(net: Manet) -> np.ndarray:
+    out = np.zeros(MANET_PARAMS, np.float32)
+    _check(load().manet_get_grads(ctypes.byref(net), out.ctypes.data_as(_fp)))
+    return out
+
+
+def manet_loss_grad(net: Manet, N: int, pitch: int, delta, phi1, phi2, target) -> float:
+    loss = ctypes.c_double(0)
+    _check(load().manet_loss_grad(ctypes.byref(net), N, pitch, _vp(delta), _vp(phi1), _vp(phi2), _vp(target),
+                                  ctypes.byref(loss)))
+    return loss.value
+
+
+def manet_train_step(net: Manet, N: int, pitch: int, delta, phi1, phi2, target, lr: float) -> float:
+    loss = ctypes.c_double(0)
+    _check(load().manet_train_step(ctypes.byref(net), N, pitch, _vp(delta), _vp(phi1), _vp(phi2), _vp(target),
+                                   ctypes.c_float(lr), ctypes.byref(loss)))
+    return loss.value
+
+
+def manet_infer(net: Manet, N: int, pitch: int, delta, phi1, phi2, out) -> None:
+    _check(load().manet_infer(ctypes.byref(net), N, pitch, _vp(delta), _vp(phi1), _vp(phi2), _vp(out)))
+
+
+def manet_layers(p: np.ndarray):
+    """split a parameter vector into per-layer (w[27][16][16], b[16]) arrays"""
+    ppl = MANET_PARAMS // 4
+    return [(p[l * ppl:l * ppl + 27 * 256].reshape(27, 16, 16), p[l * ppl + 27 * 256:(l + 1) * ppl])
+            for l in range(4)]
+
+
+class MAStats(ctypes.Structure):
+    _fields_ = [("cycles", ctypes.c_int), ("evaluations", ctypes.c_int), ("rel", ctypes.c_double),
+                ("eps", ctypes.c_double), ("rel_first", ctypes.c_double), ("rel_second", ctypes.c_double),
+                ("ms", ctypes.c_double), ("ms_warm", ctypes.c_double)]
+
+    def as_dict(self) -> dict:
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+def solveMongeAmpereTol(pot, dens, work, tol: float, max_cycles: int, net: Manet | None = None) -> dict:
+    """Monge-Ampere to a relative rms residual tol; returns the statistics (converged: status 0)."""
+    st = MAStats()
+    s = load().solveMongeAmpereTol(ctypes.byref(pot), ctypes.byref(dens), ctypes.byref(work), ctypes.c_double(tol),
+                                   max_cycles, ctypes.byref(net) if net is not None else None, ctypes.byref(st))
+    if s not in (0, 7):
+        _check(s)
+    d = st.as_dict()
+    d["converged"] = s == 0
+    return d
+
+
+def manet_training_pair(pot, dens, work, cycles: int, delta, phi1, phi2, sigma) -> dict:
+    st = MAStats()
+    _check(load().manet_training_pair(ctypes.byref(pot), ctypes.byref(dens), ctypes.byref(work), cycles,
+                                      _vp(delta), _vp(phi1), _vp(phi2), _vp(sigma), ctypes.byref(st)))
+    return st.as_dict()

@@ -285,3 +285,36 @@ def ref_norms(seed: int, n: int) -> np.ndarray:
     out = np.empty(n, np.float64)
     ref_lib().ref_norms(ctypes.c_uint64(seed), ctypes.c_int64(n), P(out))
     return out
+
+
+# ---- Monge-Ampere warm-start network (manet_oracle.c) ----------------------------------------
+MANET_CIN = (3, 16, 16, 16)
+MANET_COUT = (16, 16, 16, 1)
+
+
+def bf16(x: np.ndarray) -> np.ndarray:
+    """round to bfloat16 (through float32, ties to even), as float64"""
+    f = lib().orc_bf16
+    f.restype = ctypes.c_double
+    f.argtypes = [ctypes.c_double]
+    return np.vectorize(f)(np.asarray(x, np.float64))
+
+
+def manet_loss_grad(x: np.ndarray, target: np.ndarray, layers, round_bf16: bool = True):
+    """FP64 forward, MSE loss and gradients of the 4-layer network.
+    x: [N, N, N, 3]; target: [N, N, N]; layers: [(w [27, cin, cout], b [cout])] with the real
+    channel counts.  Returns (loss, pred [N, N, N], [(dw, db)])."""
+    N = x.shape[0]
+    xs = np.ascontiguousarray(x, np.float64)
+    ts = np.ascontiguousarray(target, np.float64)
+    ws = [np.ascontiguousarray(w, np.float64) for w, _ in layers]
+    bs = [np.ascontiguousarray(b, np.float64) for _, b in layers]
+    dws = [np.zeros_like(w) for w in ws]
+    dbs = [np.zeros_like(b) for b in bs]
+    pred = np.zeros((N, N, N))
+    arr = lambda lst: (_dp * 4)(*[a.ctypes.data_as(_dp) for a in lst])
+    f = lib().orc_manet_loss_grad
+    f.restype = ctypes.c_double
+    loss = f(N, xs.ctypes.data_as(_dp), ts.ctypes.data_as(_dp), arr(ws), arr(bs), int(round_bf16),
+             pred.ctypes.data_as(_dp), arr(dws), arr(dbs))
+    return loss, pred, list(zip(dws, dbs))

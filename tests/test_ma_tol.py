@@ -1,0 +1,84 @@
+"""Monge-Ampere to a tolerance (k-space update) and the learned warm start: pinned to the oracle's
+reference iteration in FP64, convergence in FP32, training pairs, and the warm start's gain."""
+import numpy as np
+import pytest
+
+import mitos_gb300.lib as ml
+from mitos_gb300 import manet
+from mitos_gb300.perturb import load_table
+from conftest import rel_err
+from test_gpu_core import _solver_grids, oracle_2lpt
+
+pytestmark = pytest.mark.gpu
+
+
+def test_tolerance_iteration_matches_reference_cycles_fp64(table):
+    """three k-space updates give the potential of three reference cycles (src/monge_ampere.c)"""
+    N, L = 32, 128.0
+    f, dens = _solver_grids(N, L, ml.FP64, table)
+    # 3000x the helper's amplitude (delta rms 3.4e-3): the residuals of the first cycles
+    # (1.7e-3, 8e-6, 4.5e-8) stay far above both FP64 floors (the reference's real-space round trip
+    # of phi floors near 1e-10, the k-space update near 1e-12)
+    f = f * 3000.0
+    ml.set_fbox(dens, f)
+    ml.fft_c2r_dg(dens)
+    ml.fft_r2c_dg(dens)
+    pot, work = ml.alloc_local_grid(N, L, ml.FP64), ml.alloc_local_grid(N, L, ml.FP64)
+    st = ml.solveMongeAmpereTol(pot, dens, work, 0.0, 3)
+    assert not st["converged"] and st["cycles"] == 3 and st["evaluations"] == 4
+    ref, eps, rel = oracle_2lpt(N, L, f, ma_cycles=3)
+    assert rel[1] > 1e-6
+    assert rel_err(ml.get_fbox(pot), ref) < 1e-10
+    assert st["rel_first"] == pytest.approx(rel[0], rel=1e-8)
+    assert st["rel_second"] == pytest.approx(rel[1], rel=1e-5)
+    for g in (pot, work, dens):
+        ml.free_local_grid(g)
+
+
+# The reference iteration's residual levels off at a floor that FP32 and FP64 share (measured:
+# 5.8e-5 at 64^3 / L = 125, 2.1e-7 at 256^3 / L = 500), so the 64^3 tests use a tolerance of 1e-4.
+TOL64 = 1e-4
+
+
+def test_tolerance_fp32_tracks_fp64(table, spline):
+    N, L = 64, 125.0
+    res = {}
+    for prec in (ml.FP32, ml.FP64):
+        dens = manet.density(N, L, 3001, table, spline, prec)
+        pot, work = ml.alloc_local_grid(N, L, prec), ml.alloc_local_grid(N, L, prec)
+        res[prec] = ml.solveMongeAmpereTol(pot, dens, work, TOL64, 30)
+        for g in (pot, work, dens):
+            ml.free_local_grid(g)
+    s32, s64 = res[ml.FP32], res[ml.FP64]
+    assert s32["converged"] and s64["converged"], (s32, s64)
+    assert s32["cycles"] == s64["cycles"]
+    assert s32["rel"] <= TOL64 and s32["eps"] == pytest.approx(s32["rel"] / N ** 1.5)
+    assert s32["rel_first"] == pytest.approx(s64["rel_first"], rel=1e-4)
+    assert s32["rel"] == pytest.approx(s64["rel"], rel=1e-2)
+
+
+def test_training_pair_and_warm_start(table, spline):
+    """pairs from the cold iteration; a trained network must lower the residual after the first
+    update on held-out realisations, and the warm-started solve still meets the tolerance"""
+    N, L = 64, 125.0
+    train = manet.PairSet(N, L, range(2000, 2024), table, spline, cycles=10)
+    held = manet.PairSet(N, L, range(3000, 3004), table, spline, cycles=10)
+    net = ml.manet_init(7)
+    try:
+        rms = train.rms()
+        assert np.all(np.isfinite(rms)) and np.all(rms > 0)
+        manet.set_scales(net, rms)
+        before = manet.evaluate(net, held)
+        losses = manet.train(net, train, 400, lr=2e-3)
+        after = manet.evaluate(net, held)
+        assert np.all(np.isfinite(losses))
+        assert after < 0.5 * before and after < 0.8, (before, after)
+        cmp = manet.compare(net, N, L, [3000, 3001], table, spline, tol=TOL64)
+        for c, w in zip(cmp["cold"], cmp["warm"]):
+            assert c["converged"] and w["converged"], (c, w)
+            assert w["rel_second"] < c["rel_second"]
+            assert w["ms_warm"] > 0
+    finally:
+        ml.manet_free(net)
+        train.free()
+        held.free()
