@@ -351,6 +351,26 @@ int manet_training_pair(struct distributed_grid *potential, struct distributed_g
                         struct distributed_grid *workspace, int cycles, float *delta, float *phi1,
                         float *phi2, float *sigma, struct ma_stats *stats);
 
+/* ---- Ensembles of realisations in one CUDA graph (no reference counterpart: the reference runs
+ * one realisation per process) -------------------------------------------------------------------
+ * ic_ensemble_create runs every configuration once (workspaces, tables), then captures all of
+ * them into one graph over `streams` concurrent streams (largest grids first).  A replay
+ * (ic_ensemble_run) recomputes the same realisations; *ms receives its device time.
+ * ic_ensemble_result fills P(k) of configuration i (pos is not produced). */
+struct ic_ensemble;
+int ic_ensemble_create(struct ic_ensemble **ens, const struct ic_config *cfgs, int n,
+                       const struct perturb_spline *spline, int streams);
+int ic_ensemble_run(struct ic_ensemble *ens, double *ms);
+int ic_ensemble_result(struct ic_ensemble *ens, int i, struct ic_result *res);
+int ic_ensemble_launches(const struct ic_ensemble *ens); /* kernel launches in one replay */
+int ic_ensemble_destroy(struct ic_ensemble *ens);
+/* FFT tile autotuner: times the IC of cfg for every fitting pair of X/Y pencils per block and Z
+ * rows per block, keeps the fastest for (N, precision) in this process and returns it. */
+int mitos_autotune(const struct ic_config *cfg, const struct perturb_spline *spline, int *p_xy,
+                   int *p_z, double *ms);
+int mitos_set_tiles(int N, int precision, int p_xy, int p_z);
+int mitos_get_tiles(int N, int precision, int *p_xy, int *p_z);
+
 #ifdef __cplusplus
 }
 #endif

@@ -59,6 +59,8 @@ int check_cuda(cudaError_t e, const char *what);
 
 // the library's stream (created on first use) and kernel-launch counter
 cudaStream_t stream();
+void set_stream(cudaStream_t s);      // this thread's launches go to s (nullptr: the library stream)
+void set_workspace_set(int s);        // this thread's workspace() buffers come from set s
 void count_launch(int n = 1);
 void launch_begin(const char *name);  // pairs with count_launch for per-launch timing
 

@@ -36,10 +36,18 @@ int check_cuda(cudaError_t e, const char *what) {
     return 4;
 }
 
+// the stream every launch goes to: the library stream, or the stream a caller on this thread
+// selected (set_stream; the ensemble runs each realisation on its own stream)
+static thread_local cudaStream_t t_stream = nullptr;
+static thread_local int t_ws_set = 0;
+
 cudaStream_t stream() {
+    if (t_stream) return t_stream;
     if (!g_stream) cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking);
     return g_stream;
 }
+void set_stream(cudaStream_t s) { t_stream = s; }
+void set_workspace_set(int s) { t_ws_set = s; }
 
 // optional per-launch timing: events recorded on the library stream around every launch
 static bool g_ktime = false;
@@ -159,6 +167,33 @@ const GridGeom *geom(int N, int precision) {
     g.twN = ge->tw;
     g_geoms[key] = ge;
     return &ge->g;
+}
+
+int set_tiles(int N, int precision, int p_xy, int p_z) {
+    const GridGeom *gc = geom(N, precision);
+    if (!gc) return 3;
+    const int tpp = N / gc->E, tz = (N / 2) / gc->E;
+    const size_t csz = precision == MITOS_FP32 ? 8 : 16;
+    // X / Y kernels: at most 512 threads and 96 KB of exchange buffer; Z kernels: 256 threads; all
+    // blocks whole warps (the per-warp P(k) histograms and the warp-shuffle reductions need them)
+    if (p_xy < 1 || p_xy * tpp > 512 || (p_xy * tpp) % 32 || (size_t)p_xy * spad_len(N) * csz > 96 * 1024 ||
+        p_z < 1 || p_z * tz > 256 || (p_z * tz) % 32 || (size_t)p_z * spad_len(N / 2) * csz > 96 * 1024) {
+        set_error(1, "tile %d x %d does not fit N = %d", p_xy, p_z, N);
+        return 1;
+    }
+    std::lock_guard<std::mutex> lk(g_mu);
+    GridGeom *g = const_cast<GridGeom *>(gc);
+    g->P_xy = p_xy;
+    g->P_z = p_z;
+    return 0;
+}
+
+int get_tiles(int N, int precision, int *p_xy, int *p_z) {
+    const GridGeom *g = geom(N, precision);
+    if (!g) return 3;
+    *p_xy = g->P_xy;
+    *p_z = g->P_z;
+    return 0;
 }
 
 // 1 / sinc(pi m / N)^order, m = -N/2 .. N/2, stored at m + N/2
@@ -302,7 +337,7 @@ int bin_geometry(int N, int bins, int linear, double boxlen, const double **ksum
 static std::map<std::pair<size_t, int>, std::vector<void *>> g_ws;
 void *workspace(size_t bytes, int slot) {
     std::lock_guard<std::mutex> lk(g_mu);
-    auto &v = g_ws[std::make_pair(bytes, 0)];
+    auto &v = g_ws[std::make_pair(bytes, t_ws_set)];
     while ((int)v.size() <= slot) v.push_back(nullptr);
     if (!v[slot]) {
         if (cudaMalloc(&v[slot], bytes) != cudaSuccess) {

@@ -12,6 +12,10 @@ const int *bin_table(int N, int bins, int linear, double boxlen);
 int bin_geometry(int N, int bins, int linear, double boxlen, const double **ksum, const long long **count);
 // grid-sized scratch buffer number `slot` of `bytes` bytes (kept until mitos_release_all)
 void *workspace(size_t bytes, int slot);
+// FFT tiles of one grid size: pencils per block of the X / Y passes and rows per block of the Z
+// passes (the autotuner's knobs); returns 1 when the tile does not fit the kernels' limits
+int set_tiles(int N, int precision, int p_xy, int p_z);
+int get_tiles(int N, int precision, int *p_xy, int *p_z);
 void release_all();
 
 // white noise (noise.cu)

@@ -19,4 +19,17 @@ int grid_hessian(const GridGeom &g, int prec, double boxlen, const void *phi, in
 int axpby(int prec, long n, double a, const void *x, double b, const void *y, void *out);
 inline size_t csize(int prec) { return prec == MITOS_FP32 ? 8 : 16; }
 
+// options of one pipeline run (pipeline.cu): acc, when set, receives the P(k) accumulators
+// (3 * pk_bins + 2 doubles: k sums, power sums, counts); graph = a run inside a stream capture (no
+// host copies or synchronisation; the transfer rows an earlier run of the workspace set uploaded)
+struct PipeOpts {
+    double *acc;
+    bool graph;
+};
+int pipeline_table(const struct ic_config *cfg, int k_size, int tau_size, int n_functions, const double *k,
+                   const double *log_tau, const double *redshift, const double *D_growth, const double *delta,
+                   struct ic_result *res, const PipeOpts *opt);
+int pipeline_spline(const struct ic_config *cfg, const struct perturb_spline *spline, struct ic_result *res,
+                    const PipeOpts *opt);
+
 }  // namespace mitos

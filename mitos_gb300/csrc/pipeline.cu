@@ -73,7 +73,7 @@ struct StageTimer {
 
 template <typename T>
 static int run_pipeline(const struct ic_config *cfg, const double *ktab, const double *tlo, const double *thi,
-                        int k_size, double u_tau, struct ic_result *res) {
+                        int k_size, double u_tau, struct ic_result *res, const PipeOpts *opt) {
     const int prec = cfg->precision;
     const int N = cfg->N, M = cfg->M;
     const double L = cfg->boxlen;
@@ -99,14 +99,18 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     const long n2max = 3L * (N / 2) * (N / 2);
     T *filt = (T *)workspace(sizeof(T) * (n2max + 1), 106);
     double *dtab = (double *)workspace(sizeof(double) * 3 * k_size, 107);
-    double *acc = (double *)workspace(sizeof(double) * 3 * (size_t)cfg->pk_bins + 2 * sizeof(double), 104);
+    double *acc = (opt && opt->acc) ? opt->acc
+                                    : (double *)workspace(sizeof(double) * 3 * (size_t)cfg->pk_bins + 2 * sizeof(double), 104);
     if (!filt || !dtab || !acc) return 5;
     double *red = acc + 3 * cfg->pk_bins;
 
-    // inputs: the transfer table rows of the source time (host -> device)
-    MITOS_CUDA(cudaMemcpyAsync(dtab, ktab, sizeof(double) * k_size, cudaMemcpyHostToDevice, stream()));
-    MITOS_CUDA(cudaMemcpyAsync(dtab + k_size, tlo, sizeof(double) * k_size, cudaMemcpyHostToDevice, stream()));
-    MITOS_CUDA(cudaMemcpyAsync(dtab + 2 * k_size, thi, sizeof(double) * k_size, cudaMemcpyHostToDevice, stream()));
+    // inputs: the transfer table rows of the source time (host -> device); a graph-mode run reuses
+    // the rows an earlier run of the same workspace set uploaded (no pageable copies in a capture)
+    if (!(opt && opt->graph)) {
+        MITOS_CUDA(cudaMemcpyAsync(dtab, ktab, sizeof(double) * k_size, cudaMemcpyHostToDevice, stream()));
+        MITOS_CUDA(cudaMemcpyAsync(dtab + k_size, tlo, sizeof(double) * k_size, cudaMemcpyHostToDevice, stream()));
+        MITOS_CUDA(cudaMemcpyAsync(dtab + 2 * k_size, thi, sizeof(double) * k_size, cudaMemcpyHostToDevice, stream()));
+    }
     const bool ma = cfg->method == MITOS_METHOD_MONGE_AMPERE;
     {
         int blocks = (int)((n2max + 256) / 256);
@@ -296,6 +300,7 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     if (!e) e = launch_x<T>(g, XOP_PK, -1, a);
     if (e) return e;
     tim.mark();
+    if (opt && opt->graph) return 0;  // results stay in opt->acc
 
     if (res) {
         const double *ksum;
@@ -324,9 +329,9 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     return 0;
 }
 
-extern "C" int ic_pipeline_run_table(const struct ic_config *cfg, int k_size, int tau_size, int n_functions,
-                                     const double *k, const double *log_tau, const double *redshift,
-                                     const double *D_growth, const double *delta, struct ic_result *res) {
+int mitos::pipeline_table(const struct ic_config *cfg, int k_size, int tau_size, int n_functions, const double *k,
+                          const double *log_tau, const double *redshift, const double *D_growth, const double *delta,
+                          struct ic_result *res, const PipeOpts *opt) {
     if (!cfg || cfg->N < 16 || cfg->M < 1 || cfg->boxlen <= 0 || cfg->pk_bins < 1) {
         set_error(1, "invalid ic_config");
         return 1;
@@ -352,19 +357,30 @@ extern "C" int ic_pipeline_run_table(const struct ic_config *cfg, int k_size, in
     find_tau_h(&pd, lt, &tau_index, &u_tau);
     const double *arr = delta + (long)cfg->index_src * k_size * tau_size;
     const double *tlo = arr + (long)k_size * tau_index, *thi = arr + (long)k_size * (tau_index + 1);
-    if (cfg->precision == MITOS_FP32) return run_pipeline<float>(cfg, k, tlo, thi, k_size, u_tau, res);
-    if (cfg->precision == MITOS_FP64) return run_pipeline<double>(cfg, k, tlo, thi, k_size, u_tau, res);
+    if (cfg->precision == MITOS_FP32) return run_pipeline<float>(cfg, k, tlo, thi, k_size, u_tau, res, opt);
+    if (cfg->precision == MITOS_FP64) return run_pipeline<double>(cfg, k, tlo, thi, k_size, u_tau, res, opt);
     set_error(3, "unknown precision %d", cfg->precision);
     return 3;
 }
 
-extern "C" int ic_pipeline_run(const struct ic_config *cfg, const struct perturb_spline *spline,
-                               struct ic_result *res) {
+extern "C" int ic_pipeline_run_table(const struct ic_config *cfg, int k_size, int tau_size, int n_functions,
+                                     const double *k, const double *log_tau, const double *redshift,
+                                     const double *D_growth, const double *delta, struct ic_result *res) {
+    return pipeline_table(cfg, k_size, tau_size, n_functions, k, log_tau, redshift, D_growth, delta, res, nullptr);
+}
+
+int mitos::pipeline_spline(const struct ic_config *cfg, const struct perturb_spline *spline, struct ic_result *res,
+                           const PipeOpts *opt) {
     if (!spline || !spline->ptdat) {
         set_error(1, "missing perturbation spline");
         return 1;
     }
     const struct perturb_data *pd = spline->ptdat;
-    return ic_pipeline_run_table(cfg, pd->k_size, pd->tau_size, pd->n_functions, pd->k, pd->log_tau, pd->redshift,
-                                 pd->D_growth, pd->delta, res);
+    return pipeline_table(cfg, pd->k_size, pd->tau_size, pd->n_functions, pd->k, pd->log_tau, pd->redshift,
+                          pd->D_growth, pd->delta, res, opt);
+}
+
+extern "C" int ic_pipeline_run(const struct ic_config *cfg, const struct perturb_spline *spline,
+                               struct ic_result *res) {
+    return pipeline_spline(cfg, spline, res, nullptr);
 }

@@ -467,3 +467,52 @@ def manet_training_pair(pot, dens, work, cycles: int, delta, phi1, phi2, sigma) 
     _check(load().manet_training_pair(ctypes.byref(pot), ctypes.byref(dens), ctypes.byref(work), cycles,
                                       _vp(delta), _vp(phi1), _vp(phi2), _vp(sigma), ctypes.byref(st)))
     return st.as_dict()
+
+
+# ---- ensembles in one CUDA graph, FFT tile autotuner -----------------------------------------
+class Ensemble:
+    """ic_ensemble_create / run / result / destroy over a list of ICConfig"""
+
+    def __init__(self, cfgs, spline: Spline, streams: int = 8):
+        self.n = len(cfgs)
+        self.cfgs = (ICConfig * self.n)(*cfgs)
+        self.spline = spline
+        self.h = ctypes.c_void_p()
+        _check(load().ic_ensemble_create(ctypes.byref(self.h), self.cfgs, self.n, ctypes.byref(spline.sp), streams))
+
+    def run(self) -> float:
+        ms = ctypes.c_double(0)
+        _check(load().ic_ensemble_run(self.h, ctypes.byref(ms)))
+        return ms.value
+
+    def launches(self) -> int:
+        return load().ic_ensemble_launches(self.h)
+
+    def result(self, i: int) -> dict:
+        bins = self.cfgs[i].pk_bins
+        k, p, o = np.zeros(bins), np.zeros(bins), np.zeros(bins, np.int64)
+        r = ICResult(k.ctypes.data_as(_dp), p.ctypes.data_as(_dp), o.ctypes.data_as(_lp), None, 0, 0.0)
+        _check(load().ic_ensemble_result(self.h, i, ctypes.byref(r)))
+        return {"pk_k": k, "pk_p": p, "pk_obs": o}
+
+    def close(self) -> None:
+        if self.h:
+            load().ic_ensemble_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+
+def autotune(cfg: ICConfig, spline: Spline) -> tuple:
+    pxy, pz, ms = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_double(0)
+    _check(load().mitos_autotune(ctypes.byref(cfg), ctypes.byref(spline.sp), ctypes.byref(pxy), ctypes.byref(pz),
+                                 ctypes.byref(ms)))
+    return pxy.value, pz.value, ms.value
+
+
+def set_tiles(N: int, precision: int, pxy: int, pz: int) -> None:
+    _check(load().mitos_set_tiles(N, precision, pxy, pz))
+
+
+def get_tiles(N: int, precision: int) -> tuple:
+    pxy, pz = ctypes.c_int(0), ctypes.c_int(0)
+    _check(load().mitos_get_tiles(N, precision, ctypes.byref(pxy), ctypes.byref(pz)))
+    return pxy.value, pz.value
