@@ -166,6 +166,16 @@ void kernel_undo_Hermite_window(struct kernel *the_kernel);
 /* Advances *state past every draw, as the sequential reference does. */
 int generate_complex_grf(struct distributed_grid *dg, rng_state *state);
 int enforce_hermiticity(struct distributed_grid *dg);
+/* src/grf_ngeniclike.c:28-203 (include/grf_ngeniclike.h:29-30): the N-GenIC-style field (RANLUX
+ * ranlxd1 seed table, per-column reseeding, amplitude sqrt(-ln U), kz = 0 conjugate fill).  fbox:
+ * device buffer of NX*N*(N/2+1) complex doubles (the rows X0 .. X0+NX-1); block_size unused, as in
+ * the reference.  Returns 0, 1 (invalid grid) or 4 (seed table allocation). */
+int generate_ngeniclike_grf(mitos_c128 *fbox, int N, int NX, int X0, long block_size, double boxlen,
+                            long seed);
+/* the same into a grid of either precision (its N, NX, X0, boxlen), left in momentum space */
+int generate_ngeniclike_grf_dg(struct distributed_grid *grf, long seed);
+/* the first n uniforms of ranlxd1 seeded with seed (host; the generator of the two above) */
+int mitos_ranlxd1_uniforms(unsigned long seed, long n, double *out);
 
 /* ---- perturbation grid, Poisson, 2LPT, Monge-Ampere ----------------------------------- */
 /* src/generate_grids.c:28-67 (include/generate_grids.h:29-34).  fname is not written: field

@@ -516,3 +516,14 @@ def get_tiles(N: int, precision: int) -> tuple:
     pxy, pz = ctypes.c_int(0), ctypes.c_int(0)
     _check(load().mitos_get_tiles(N, precision, ctypes.byref(pxy), ctypes.byref(pz)))
     return pxy.value, pz.value
+
+
+# ---- N-GenIC-like field --------------------------------------------------------------------
+def generate_ngeniclike_grf_dg(grf: DistributedGrid, seed: int) -> None:
+    _check(load().generate_ngeniclike_grf_dg(ctypes.byref(grf), ctypes.c_long(seed)))
+
+
+def ranlxd1_uniforms(seed: int, n: int) -> np.ndarray:
+    out = np.zeros(n)
+    _check(load().mitos_ranlxd1_uniforms(ctypes.c_ulong(seed), ctypes.c_long(n), out.ctypes.data_as(_dp)))
+    return out

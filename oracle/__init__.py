@@ -318,3 +318,32 @@ def manet_loss_grad(x: np.ndarray, target: np.ndarray, layers, round_bf16: bool 
     loss = f(N, xs.ctypes.data_as(_dp), ts.ctypes.data_as(_dp), arr(ws), arr(bs), int(round_bf16),
              pred.ctypes.data_as(_dp), arr(dws), arr(dbs))
     return loss, pred, list(zip(dws, dbs))
+
+
+# ---- N-GenIC-like field (ngenic_oracle.c; parity with libgsl unpinned) -----------------------
+class OrcRanlxd(ctypes.Structure):
+    _fields_ = [("x", ctypes.c_uint64 * 12), ("carry", ctypes.c_int), ("i", ctypes.c_int), ("left", ctypes.c_int)]
+
+
+def ranlxd1_uniforms(seed: int, n: int) -> np.ndarray:
+    r = OrcRanlxd()
+    L = lib()
+    L.orc_ranlxd1_set(ctypes.byref(r), ctypes.c_ulong(seed))
+    f = L.orc_ranlxd1_uniform
+    f.restype = ctypes.c_double
+    return np.array([f(ctypes.byref(r)) for _ in range(n)])
+
+
+def ngenic_seedtable(N: int, seed: int) -> np.ndarray:
+    t = np.zeros(N * N, np.uint32)
+    lib().orc_ngenic_seedtable(N, ctypes.c_ulong(seed), t.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)))
+    return t.reshape(N, N)
+
+
+def ngeniclike_grf(N: int, boxlen: float, seed: int) -> np.ndarray:
+    """complex [N, N, N/2+1] field of src/grf_ngeniclike.c on one rank"""
+    buf = np.zeros(N * N * (N // 2 + 1) * 2)
+    s = lib().orc_ngeniclike_grf(N, ctypes.c_double(boxlen), ctypes.c_ulong(seed), buf.ctypes.data_as(_dp))
+    assert s == 0
+    b = buf.reshape(N, N, N // 2 + 1, 2)
+    return b[..., 0] + 1j * b[..., 1]
