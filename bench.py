@@ -166,7 +166,97 @@ def config(args):
                         f"CIC, P(k) {args.bins} linear shells",
             "N": args.N, "M": args.N, "boxlen": args.boxlen, "precision": args.precision,
             "pk_bins": args.bins, "parallelism": "replicas (independent seeds per GPU)",
-            "l2": "inputs larger than L2 (each grid 0.54 GB)", "cuda_graph": False}
+            "l2": f"inputs larger than L2 (each grid {args.N ** 3 * 4 / 1e9:.2f} GB)" if args.N ** 3 * 4 > 129e6
+                  else "grids smaller than L2 (no flush)", "cuda_graph": False}
+
+
+def extras(ml, table, spline, args) -> dict:
+    """the other parts of the benchmark configuration, measured after the main line's timing"""
+    out = {}
+    N, L = args.N, args.boxlen
+
+    def cfg(prec, seed, n=N, box=L, bins=args.bins):
+        return ml.ic_config(n, n, box, seed, table, method=ml.METHOD_2LPT, pk_bins=bins, pk_linear=True,
+                            precision=prec)
+
+    # FP64 512^3 IC (the FP64 GPU path) and the FP32 P(k) against it on the same seed
+    r32 = ml.ic_pipeline_run(cfg(ml.FP32, args.seed), spline)
+    r64 = ml.ic_pipeline_run(cfg(ml.FP64, args.seed), spline)
+    ml.timer_start()
+    for i in range(3):
+        ml.ic_pipeline_run(cfg(ml.FP64, args.seed + 1 + i), spline)
+    ms64 = ml.timer_stop() / 3
+    ok = np.isfinite(r64["pk_p"]) & (r64["pk_p"] != 0)
+    rel = np.abs(r32["pk_p"][ok] / r64["pk_p"][ok] - 1)
+    out["fp64"] = {"ms_per_ic": ms64, "ic_per_s": 1e3 / ms64,
+                   "pk_fp32_vs_fp64": {"max_rel": float(rel.max()), "bins": int(ok.sum()), "target": 1e-4}}
+
+    # 48 realisations (16 x 64^3 / 256, 16 x 96^3 / 384, 16 x 128^3 / 512 Mpc/h; 4 Mpc/h cells),
+    # seeds 1000-1047, one captured CUDA graph over 8 streams, tiles from the autotuner
+    sizes = [(64, 256.0), (96, 384.0), (128, 512.0)]
+    tiles = {}
+    for n, box in sizes:
+        pxy, pz, _ = ml.autotune(cfg(ml.FP32, 1000, n, box, 32), spline)
+        tiles[n] = [pxy, pz]
+    cfgs = [cfg(ml.FP32, 1000 + 16 * k + i, n, box, 32) for k, (n, box) in enumerate(sizes) for i in range(16)]
+    ens = ml.Ensemble(cfgs, spline, streams=8)
+    ens.run()
+    t = min(ens.run() for _ in range(5))
+    launches = ens.launches()
+    ens.close()
+    lat = {}
+    for n, box in sizes:
+        e1 = ml.Ensemble([cfg(ml.FP32, 1000, n, box, 32)], spline, streams=1)
+        e1.run()
+        lat[str(n)] = min(e1.run() for _ in range(10))
+        e1.close()
+    G = lambda n: n * n * (n // 2 + 1) * 8
+    model = 16 * 15 * G(64) + 16 * 37 * G(96) + 16 * 37 * G(128)  # byte model (N <= 64: one-pass FFT)
+    peak, _ = peak_hbm()
+    out["ensemble"] = {"realizations": 48, "ms_per_replay": t, "realizations_per_s": 48e3 / t,
+                       "latency_ms": lat, "gpu_launches_per_replay": launches, "tiles": tiles,
+                       "roofline": {"model_bytes": model, "GBps": model / (t / 1e3) / 1e9,
+                                    "frac": model / (t / 1e3) / 1e9 / peak}}
+
+    # Monge-Ampere to a relative rms residual of 1e-6 at 256^3 / 500 Mpc/h, cold against the
+    # learned warm start (trained here: 256 seeds at 128^3 / 250 Mpc/h, 3000 Adam steps)
+    from mitos_gb300 import manet
+    t0 = time.perf_counter()
+    pairs = manet.PairSet(128, 250.0, range(2000, 2256), table, spline, cycles=10)
+    held = manet.PairSet(128, 250.0, range(3000, 3016), table, spline, cycles=10)
+    t_pairs = time.perf_counter() - t0
+    net = ml.manet_init(1)
+    manet.set_scales(net, pairs.rms())
+    t0 = time.perf_counter()
+    losses = manet.train(net, pairs, 3000, lr=2e-3)
+    ml.load().mitos_sync()
+    t_train = time.perf_counter() - t0
+    held_loss = manet.evaluate(net, held)
+    pairs.free()
+    held.free()
+    cmp = manet.compare(net, 256, 500.0, range(3000, 3016), table, spline, tol=1e-6, max_cycles=30)
+    ml.manet_free(net)
+    mean = lambda k, f: float(np.mean([x[f] for x in cmp[k]]))
+    out["monge_ampere"] = {
+        "config": "256^3, L = 500 Mpc/h, z = 31, FP32 grids, FP64 residual sums, tol = 1e-6 on "
+                  "sqrt(sum res^2 / sum rho^2) (reference eps = that / N^1.5), 16 held-out seeds 3000-3015",
+        "cold": {"cycles": mean("cold", "cycles"), "ms": mean("cold", "ms"),
+                 "converged": sum(x["converged"] for x in cmp["cold"])},
+        "warm": {"cycles": mean("warm", "cycles"), "ms": mean("warm", "ms"), "ms_warm_start": mean("warm", "ms_warm"),
+                 "converged": sum(x["converged"] for x in cmp["warm"])},
+        "rel_after_first_update": {"cold": mean("cold", "rel_second"), "warm": mean("warm", "rel_second")},
+        "net": {"train_pairs_s": t_pairs, "train_s": t_train, "steps": 3000,
+                "loss_first": float(losses[:10].mean()), "loss_last": float(losses[-100:].mean()),
+                "held_out_loss": held_loss}}
+
+    # N-GenIC-like field (src/grf_ngeniclike.c) at 512^3
+    g = ml.alloc_local_grid(N, L, ml.FP32)
+    ml.generate_ngeniclike_grf_dg(g, 1)
+    ml.timer_start()
+    ml.generate_ngeniclike_grf_dg(g, 2)
+    out["ngeniclike_ms"] = ml.timer_stop()
+    ml.free_local_grid(g)
+    return out
 
 
 def main():
@@ -181,6 +271,8 @@ def main():
     ap.add_argument("--seed", type=int, default=42)
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the FP64, ensemble, Monge-Ampere and N-GenIC measurements")
     ap.add_argument("--quick", action="store_true",
                     help="timed steps only (no e2e, per-kernel timing or CPU baseline): the profiling run")
     args = ap.parse_args()
@@ -301,6 +393,8 @@ def main():
             "ic_hbm": {"model_bytes": alg_ic, "GBps": alg_ic / (ms_per_step / 1e3) / 1e9,
                        "frac": alg_ic / (ms_per_step / 1e3) / 1e9 / peak},
             "kernels": kernels, "clocks": clk}
+    if not args.no_extras and N == 512 and prec == ml.FP32:
+        line["extras"] = extras(ml, table, spline, args)
     if not args.no_cpu_baseline:
         base, _ = cpu_baseline(args, table, steps=1)
         line["cpu_baseline"] = base
