@@ -121,7 +121,8 @@ __global__ void __launch_bounds__(strided_heavy<AXIS, OP, NL>() ? 256 : 512, 2) 
                 v[e] = x;
             }
             fft_any<T, E, SIGN, NL, PC>(pl, v, psm, P, t, tw);
-            if (!valid) continue;
+            // the P(k) epilogue keeps the whole warp together (warp-level bin sums)
+            if (!valid && OP != XOP_PK) continue;
             cplx<T> *dst = reinterpret_cast<cplx<T> *>(a.out[outs[m]]);
 #pragma unroll
             for (int e = 0; e < E; e++) {
@@ -134,12 +135,25 @@ __global__ void __launch_bounds__(strided_heavy<AXIS, OP, NL>() ? 256 : 512, 2) 
                     const long n2 = (long)jx * jx + (long)iy * iy + (long)iz * iz;
                     if constexpr (OP == XOP_PK) {
                         if (win) r = cscale<T>(r, win[jx + N / 2] * win[iy + N / 2] * win[iz + N / 2]);
-                        int bin = a.bin_of_n2[n2];
-                        if (bin >= 0) {
-                            const T mult = (iz == 0 || iz == N / 2) ? (T)1 : (T)2;
-                            atomicAdd(hp + bin, mult * (r.x * r.x + r.y * r.y));
+                        const int bin = valid ? a.bin_of_n2[n2] : -1;
+                        const T mult = (iz == 0 || iz == N / 2) ? (T)1 : (T)2;
+                        const T pw = mult * (r.x * r.x + r.y * r.y);
+                        // per distinct bin of the warp: a butterfly sum, added by one lane into
+                        // the warp's own histogram (no atomics: no other warp writes it)
+                        const int lane = threadIdx.x & 31;
+                        unsigned todo = __ballot_sync(0xffffffffu, bin >= 0);
+                        while (todo) {
+                            const int leader = __ffs(todo) - 1;
+                            const int b0 = __shfl_sync(0xffffffffu, bin, leader);
+                            const bool in = bin == b0 && ((todo >> lane) & 1u);
+                            T sum = in ? pw : (T)0;
+#pragma unroll
+                            for (int off = 16; off > 0; off >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, off);
+                            if (lane == leader) hp[b0] += sum;
+                            todo &= ~__ballot_sync(0xffffffffu, in);
                         }
-                        if (a.out[0]) dst[idx] = r;
+                        __syncwarp();  // a later leader of the same bin may be another lane
+                        if (valid && a.out[0]) dst[idx] = r;
                     } else {
                         const T kk2 = (T)n2 * dk * dk;
                         const T G = (n2 > 0) ? (T)-1 / kk2 : (T)1;

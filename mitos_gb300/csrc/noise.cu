@@ -233,21 +233,28 @@ __device__ __forceinline__ double gauss64(uint64_t A, uint64_t B) {
     return sqrt(-2 * log(u)) * cos(2 * 3.14159265358979323846 * v);
 }
 
-// the same Box-Muller transform in FP32; ln u of u >= 1/2 goes through log1p of the exact
-// complement so that no precision is lost near u = 1
+// the same Box-Muller transform in FP32, without divergence: t = u or 1 - u (the exact complement
+// ~A), t in (0, 1/2]; ln u = ln t for u < 1/2 (|ln t| >= ln 2, so the hardware log2 keeps full
+// relative precision) and ln u = ln(1 - t) = -2 atanh(s), s = t / (2 - t) <= 1/3, for u >= 1/2
+// (the atanh series through s^15; the next term is below 4e-9 relative)
 __device__ __forceinline__ float gauss32(uint64_t A, uint64_t B) {
     const float inv64 = 5.42101086242752217e-20f;  // 2^-64
-    float lnu;
-    if (A >> 63) {
-        const float t = (__ull2float_rn(~A) + 0.5f) * inv64;
-        lnu = log1pf(-t);
-    } else {
-        // u < 1/2: |ln u| >= ln 2, so the hardware log2 keeps full relative precision
-        lnu = __logf((__ull2float_rn(A) + 0.5f) * inv64);
-    }
+    const bool hi = (A >> 63) != 0;
+    const float t = (__ull2float_rn(hi ? ~A : A) + 0.5f) * inv64;
+    const float s = __fdividef(t, 2.f - t), s2 = s * s;
+    float p = 1.f / 15.f;
+    p = fmaf(p, s2, 1.f / 13.f);
+    p = fmaf(p, s2, 1.f / 11.f);
+    p = fmaf(p, s2, 1.f / 9.f);
+    p = fmaf(p, s2, 1.f / 7.f);
+    p = fmaf(p, s2, 1.f / 5.f);
+    p = fmaf(p, s2, 1.f / 3.f);
+    p = fmaf(p, s2, 1.f);
+    const float lnu = hi ? -2.f * s * p : __logf(t);
+    const float x = -2.f * lnu;  // > 0
     // cos(2 pi v) = -cos(2 pi (v - 1/2)), argument in (-pi, pi) for the hardware cosine
     const float w = ((float)(long long)(B - 0x8000000000000000ULL) + 0.5f) * inv64;
-    return -sqrtf(-2.f * lnu) * __cosf(6.28318530717958647692f * w);
+    return -(x * rsqrtf(x)) * __cosf(6.28318530717958647692f * w);
 }
 
 template <typename T> __device__ __forceinline__ T gauss(uint64_t A, uint64_t B);
@@ -297,7 +304,7 @@ k_noise(int N, const uint64_t *__restrict__ polys, RngState s0, T factor, const 
             for (int j = 0; j < cz; j++) {
                 const int z = z0 + j;
                 cplx<T> val = mk<T>(0, 0);
-                const long n2 = (long)kx * kx + (long)ky * ky + (long)z * z;
+                const int n2 = kx * kx + ky * ky + z * z;
                 if (n2 > 0) {
                     const uint64_t A = dnext(r0, r1, r2, r3), B = dnext(r0, r1, r2, r3);
                     const uint64_t C2 = dnext(r0, r1, r2, r3), D = dnext(r0, r1, r2, r3);
@@ -315,10 +322,21 @@ k_noise(int N, const uint64_t *__restrict__ polys, RngState s0, T factor, const 
         }
         __syncthreads();
         // coalesced write-out: the block's rows are contiguous in memory
-        for (int idx = threadIdx.x; idx < NOISE_THREADS * cz; idx += NOISE_THREADS) {
-            const int rr = idx / cz, j = idx % cz;
-            if ((long)blockIdx.x * NOISE_THREADS + rr < ncol)
-                out[rowbase0 + (long)rr * H + z0 + j] = stage[rr][j];
+        if (cz == NOISE_CHUNK) {
+            static_assert((NOISE_CHUNK & (NOISE_CHUNK - 1)) == 0, "chunk is a power of two");
+            constexpr int SH = __builtin_ctz(NOISE_CHUNK);
+#pragma unroll 4
+            for (int idx = threadIdx.x; idx < NOISE_THREADS * NOISE_CHUNK; idx += NOISE_THREADS) {
+                const int rr = idx >> SH, j = idx & (NOISE_CHUNK - 1);
+                if ((long)blockIdx.x * NOISE_THREADS + rr < ncol)
+                    out[rowbase0 + (long)rr * H + z0 + j] = stage[rr][j];
+            }
+        } else {
+            for (int idx = threadIdx.x; idx < NOISE_THREADS * cz; idx += NOISE_THREADS) {
+                const int rr = idx / cz, j = idx % cz;
+                if ((long)blockIdx.x * NOISE_THREADS + rr < ncol)
+                    out[rowbase0 + (long)rr * H + z0 + j] = stage[rr][j];
+            }
         }
         __syncthreads();
     }
