@@ -280,6 +280,16 @@ struct ic_result {
 };
 int ic_pipeline_run(const struct ic_config *cfg, const struct perturb_spline *spline,
                     struct ic_result *res);
+/* Asynchronous form of ic_pipeline_run (no reference counterpart), for callers producing many ICs:
+ * it enqueues the IC and returns.  The particle positions travel to res->pos on a copy stream while
+ * later submissions compute; with res->pos in pinned (page-locked) host memory that transfer
+ * overlaps the next IC's compute, otherwise the call waits for it.  At most two ICs are in flight:
+ * a third submission first completes the oldest.  res and the arrays it points to must stay valid
+ * until ic_pipeline_wait (or the submission after next) returns; ic_pipeline_wait completes every
+ * submitted IC and fills its P(k) and Monge-Ampere fields. */
+int ic_pipeline_submit(const struct ic_config *cfg, const struct perturb_spline *spline,
+                       struct ic_result *res);
+int ic_pipeline_wait(void);
 /* The same on caller-provided host table arrays (convenience for bindings without structs). */
 int ic_pipeline_run_table(const struct ic_config *cfg, int k_size, int tau_size,
                           int n_functions, const double *k, const double *log_tau,

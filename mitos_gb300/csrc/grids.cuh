@@ -25,6 +25,10 @@ inline size_t csize(int prec) { return prec == MITOS_FP32 ? 8 : 16; }
 struct PipeOpts {
     double *acc;
     bool graph;
+    int async_slot = -1;         // >= 0: an ic_pipeline_submit run in staging slot 0 or 1
+    double *acc_host = nullptr;  // async: pinned host buffer for the power sums
+    int *iters = nullptr;        // async: Monge-Ampere cycles and residual, filled on the host
+    double *last_rel = nullptr;
 };
 int pipeline_table(const struct ic_config *cfg, int k_size, int tau_size, int n_functions, const double *k,
                    const double *log_tau, const double *redshift, const double *D_growth, const double *delta,

@@ -263,23 +263,25 @@ k_lattice_cic(int N, int rpd, int rpo, float spacing, float Lf, T ginv, const T 
     extern __shared__ __align__(16) unsigned char smraw[];
     A *reg = reinterpret_cast<A *>(smraw);                                      // LR_X * LR_Y * LR_Z
     T *tbuf = reinterpret_cast<T *>(smraw + sizeof(A) * LR_X * LR_Y * LR_Z);    // 2 x TILE_ELEMS
-    const int bz_n = N / LB_Z, by_n = N / LB_Y;
-    const int nbricks = (N / LB_X) * by_n * bz_n;
+    // brick order: x fastest, then y, then z, so the x and y neighbours whose planes the tile halos
+    // read are in flight at the same time (their halo rows come from L2, not DRAM)
+    const int bx_n = N / LB_X, by_n = N / LB_Y;
+    const int nbricks = bx_n * by_n * (N / LB_Z);
     for (int i = threadIdx.x; i < LR_X * LR_Y * LR_Z; i += LB_THREADS) reg[i] = 0;
     int b = blockIdx.x;
     if (b < nbricks) {
-        const int bz = b % bz_n, by = (b / bz_n) % by_n, bx = b / (bz_n * by_n);
+        const int bx = b % bx_n, by = (b / bx_n) % by_n, bz = b / (bx_n * by_n);
         stage_tiles<T>(tbuf, N, rpd, bx * LB_X, by * LB_Y, bz * LB_Z, d0, d1, d2);
     }
     cp_async_commit();
     const int lz = threadIdx.x % LB_Z, ly = (threadIdx.x / LB_Z) % LB_Y, lxb = threadIdx.x / (LB_Z * LB_Y);
 #pragma unroll 1
     for (int buf = 0; b < nbricks; b += gridDim.x, buf ^= 1) {
-        const int bz = b % bz_n, by = (b / bz_n) % by_n, bx = b / (bz_n * by_n);
+        const int bx = b % bx_n, by = (b / bx_n) % by_n, bz = b / (bx_n * by_n);
         const int x0 = bx * LB_X, y0 = by * LB_Y, z0 = bz * LB_Z;
         const int bn = b + gridDim.x;
         if (bn < nbricks) {
-            const int nz = bn % bz_n, ny = (bn / bz_n) % by_n, nx = bn / (bz_n * by_n);
+            const int nx = bn % bx_n, ny = (bn / bx_n) % by_n, nz = bn / (bx_n * by_n);
             stage_tiles<T>(tbuf + (buf ^ 1) * TILE_ELEMS, N, rpd, nx * LB_X, ny * LB_Y, nz * LB_Z, d0, d1, d2);
         }
         cp_async_commit();

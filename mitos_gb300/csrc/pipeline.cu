@@ -71,6 +71,47 @@ struct StageTimer {
     }
 };
 
+// pinned host staging of the transfer rows, one buffer per slot (0, 1: ic_pipeline_submit, 2: the
+// synchronous entry point); a slot's buffer is rewritten only after its previous IC completed
+static double *table_pinned(int slot, size_t n) {
+    static double *buf[3] = {nullptr, nullptr, nullptr};
+    static size_t cap[3] = {0, 0, 0};
+    if (cap[slot] < n) {
+        if (buf[slot]) cudaFreeHost(buf[slot]);
+        buf[slot] = nullptr;
+        cap[slot] = 0;
+        if (cudaMallocHost((void **)&buf[slot], sizeof(double) * n) != cudaSuccess) {
+            cudaGetLastError();
+            set_error(5, "out of pinned host memory for the transfer table");
+            return nullptr;
+        }
+        cap[slot] = n;
+    }
+    return buf[slot];
+}
+
+__global__ void k_copy_table(const double *__restrict__ src, double *__restrict__ dst, int n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = src[i];
+}
+
+// the copy stream of the position transfers and the events of the two staging slots:
+// pos_event(s, 0) = positions ready on the device, pos_event(s, 1) = their copy done (buffer free)
+static cudaStream_t copy_stream() {
+    static cudaStream_t s = nullptr;
+    if (!s) cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    return s;
+}
+static cudaEvent_t pos_event(int slot, int which) {
+    static cudaEvent_t ev[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    if (!ev[slot][which]) cudaEventCreateWithFlags(&ev[slot][which], cudaEventDisableTiming);
+    return ev[slot][which];
+}
+static cudaEvent_t acc_event(int slot) {
+    static cudaEvent_t ev[2] = {nullptr, nullptr};
+    if (!ev[slot]) cudaEventCreateWithFlags(&ev[slot], cudaEventDisableTiming);
+    return ev[slot];
+}
+
 template <typename T>
 static int run_pipeline(const struct ic_config *cfg, const double *ktab, const double *tlo, const double *thi,
                         int k_size, double u_tau, struct ic_result *res, const PipeOpts *opt) {
@@ -104,12 +145,30 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     if (!filt || !dtab || !acc) return 5;
     double *red = acc + 3 * cfg->pk_bins;
 
-    // inputs: the transfer table rows of the source time (host -> device); a graph-mode run reuses
-    // the rows an earlier run of the same workspace set uploaded (no pageable copies in a capture)
-    if (!(opt && opt->graph)) {
-        MITOS_CUDA(cudaMemcpyAsync(dtab, ktab, sizeof(double) * k_size, cudaMemcpyHostToDevice, stream()));
-        MITOS_CUDA(cudaMemcpyAsync(dtab + k_size, tlo, sizeof(double) * k_size, cudaMemcpyHostToDevice, stream()));
-        MITOS_CUDA(cudaMemcpyAsync(dtab + 2 * k_size, thi, sizeof(double) * k_size, cudaMemcpyHostToDevice, stream()));
+    // inputs: the transfer table rows of the source time (host -> device).  Ensemble runs upload
+    // them with a copy once per workspace set (a graph-mode run reuses them: no pageable copies in a
+    // capture).  Other runs place them in a pinned buffer of their slot and a small kernel reads
+    // them over the link, so no copy engine is involved: the positions of a previous submission may
+    // still occupy one for milliseconds.
+    if (opt && (opt->graph || opt->acc)) {
+        if (!opt->graph) {
+            MITOS_CUDA(cudaMemcpyAsync(dtab, ktab, sizeof(double) * k_size, cudaMemcpyHostToDevice, stream()));
+            MITOS_CUDA(cudaMemcpyAsync(dtab + k_size, tlo, sizeof(double) * k_size, cudaMemcpyHostToDevice, stream()));
+            MITOS_CUDA(cudaMemcpyAsync(dtab + 2 * k_size, thi, sizeof(double) * k_size, cudaMemcpyHostToDevice, stream()));
+        }
+    } else {
+        const int tslot = (opt && opt->async_slot >= 0) ? opt->async_slot : 2;
+        double *ht = table_pinned(tslot, 3 * (size_t)k_size);
+        if (!ht) return 5;
+        memcpy(ht, ktab, sizeof(double) * k_size);
+        memcpy(ht + k_size, tlo, sizeof(double) * k_size);
+        memcpy(ht + 2 * k_size, thi, sizeof(double) * k_size);
+        double *hd = nullptr;
+        MITOS_CUDA(cudaHostGetDevicePointer((void **)&hd, ht, 0));
+        launch_begin("table_in");
+        k_copy_table<<<8, 256, 0, stream()>>>(hd, dtab, 3 * k_size);
+        count_launch();
+        MITOS_LAUNCH_CHECK("transfer table upload");
     }
     const bool ma = cfg->method == MITOS_METHOD_MONGE_AMPERE;
     {
@@ -255,11 +314,16 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     if (e) return e;
     tim.mark();
 
-    // S5: particles + CIC
+    // S5: particles + CIC.  The positions are staged in a device buffer of the run's slot and copied
+    // to the caller on the copy stream as soon as the deposit ends, under the P(k) passes (and, for
+    // ic_pipeline_submit, under the next IC); the buffer is reused once its last copy is done.
     float *dpos = nullptr;
+    const int pslot = (opt && opt->async_slot >= 0) ? opt->async_slot : 0;
+    const size_t pos_bytes = sizeof(float) * 3 * (size_t)M * M * M;
     if (res && res->pos) {
-        dpos = (float *)workspace(sizeof(float) * 3 * (size_t)M * M * M, 108);
+        dpos = (float *)workspace(pos_bytes, 108 + pslot);
         if (!dpos) return 5;
+        MITOS_CUDA(cudaStreamWaitEvent(stream(), pos_event(pslot, 1), 0));
     }
     // the aligned deposit uses a row pitch of N + 4 reals (16-byte aligned rows for vector reductions)
     const int rho_pitch = aligned ? N + 4 : N + 2;
@@ -270,6 +334,12 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     e = aligned ? lattice_deposit(N, L, prec, D0, D1, D2, disp_pitch, rhoD, rho_pitch, dpos)
                 : displace_and_deposit(N, M, L, prec, D0, D1, D2, rhoD, dpos);
     if (e) return e;
+    if (dpos) {
+        MITOS_CUDA(cudaEventRecord(pos_event(pslot, 0), stream()));
+        MITOS_CUDA(cudaStreamWaitEvent(copy_stream(), pos_event(pslot, 0), 0));
+        MITOS_CUDA(cudaMemcpyAsync(res->pos, dpos, pos_bytes, cudaMemcpyDeviceToHost, copy_stream()));
+        MITOS_CUDA(cudaEventRecord(pos_event(pslot, 1), copy_stream()));
+    }
     tim.mark();
 
     // S6: overdensity r2c, CIC window undo, P(k) (analyse/src/mitos_read.c:364-419)
@@ -301,6 +371,20 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     if (e) return e;
     tim.mark();
     if (opt && opt->graph) return 0;  // results stay in opt->acc
+    if (opt && opt->async_slot >= 0) {
+        // the power sums go to the slot's pinned buffer through a kernel's stores, not a copy
+        // engine (which the positions may occupy); the host finishes the bins at wait time
+        double *hd = nullptr;
+        MITOS_CUDA(cudaHostGetDevicePointer((void **)&hd, opt->acc_host, 0));
+        launch_begin("pk_out");
+        k_copy_table<<<1, 256, 0, stream()>>>(acc + cfg->pk_bins, hd, cfg->pk_bins);
+        count_launch();
+        MITOS_LAUNCH_CHECK("P(k) sums to the host");
+        MITOS_CUDA(cudaEventRecord(acc_event(opt->async_slot), stream()));
+        if (opt->iters) *opt->iters = iters;
+        if (opt->last_rel) *opt->last_rel = last_rel;
+        return 0;
+    }
 
     if (res) {
         const double *ksum;
@@ -310,10 +394,8 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
         std::vector<double> h(cfg->pk_bins);
         MITOS_CUDA(cudaMemcpyAsync(h.data(), acc + cfg->pk_bins, sizeof(double) * cfg->pk_bins,
                                    cudaMemcpyDeviceToHost, stream()));
-        if (dpos)
-            MITOS_CUDA(cudaMemcpyAsync(res->pos, dpos, sizeof(float) * 3 * (size_t)M * M * M, cudaMemcpyDeviceToHost,
-                                       stream()));
         MITOS_CUDA(cudaStreamSynchronize(stream()));
+        if (dpos) MITOS_CUDA(cudaEventSynchronize(pos_event(pslot, 1)));
         for (int i = 0; i < cfg->pk_bins; i++) {
             const double n = (double)count[i];
             if (res->pk_obs) res->pk_obs[i] = (long)count[i];
@@ -383,4 +465,90 @@ int mitos::pipeline_spline(const struct ic_config *cfg, const struct perturb_spl
 extern "C" int ic_pipeline_run(const struct ic_config *cfg, const struct perturb_spline *spline,
                                struct ic_result *res) {
     return pipeline_spline(cfg, spline, res, nullptr);
+}
+
+// ---- asynchronous submission: two ICs in flight, the positions of one travelling under the
+// compute of the next --------------------------------------------------------------------------
+namespace {
+struct AsyncSlot {
+    bool busy = false;
+    struct ic_config cfg;
+    struct ic_result *res = nullptr;
+    double *acc_host = nullptr;
+    int acc_cap = 0;
+    int iters = 0;
+    double last_rel = 0;
+    long order = 0;
+};
+AsyncSlot g_slot[2];
+int g_next = 0;
+long g_order = 0;
+
+int finish_slot(int k) {
+    AsyncSlot &s = g_slot[k];
+    if (!s.busy) return 0;
+    s.busy = false;
+    MITOS_CUDA(cudaEventSynchronize(acc_event(k)));
+    if (s.res && s.res->pos) MITOS_CUDA(cudaEventSynchronize(pos_event(k, 1)));
+    if (!s.res) return 0;
+    const double *ksum;
+    const long long *count;
+    int e = bin_geometry(s.cfg.N, s.cfg.pk_bins, s.cfg.pk_linear, s.cfg.boxlen, &ksum, &count);
+    if (e) return e;
+    const double V = s.cfg.boxlen * s.cfg.boxlen * s.cfg.boxlen;
+    for (int i = 0; i < s.cfg.pk_bins; i++) {
+        const double n = (double)count[i];
+        if (s.res->pk_obs) s.res->pk_obs[i] = (long)count[i];
+        if (s.res->pk_k) s.res->pk_k[i] = ksum[i] / n;
+        if (s.res->pk_p) s.res->pk_p[i] = s.acc_host[i] / n / V;
+    }
+    s.res->ma_iterations = s.iters;
+    s.res->ma_residual = s.last_rel;
+    return 0;
+}
+}  // namespace
+
+extern "C" int ic_pipeline_submit(const struct ic_config *cfg, const struct perturb_spline *spline,
+                                  struct ic_result *res) {
+    if (!cfg || cfg->pk_bins < 1) {
+        set_error(1, "invalid ic_config");
+        return 1;
+    }
+    const int k = g_next;
+    int e = finish_slot(k);  // the slot's previous IC (submitted two calls ago)
+    if (e) return e;
+    AsyncSlot &s = g_slot[k];
+    if (s.acc_cap < cfg->pk_bins) {
+        if (s.acc_host) cudaFreeHost(s.acc_host);
+        s.acc_host = nullptr;
+        s.acc_cap = 0;
+        if (cudaMallocHost(&s.acc_host, sizeof(double) * cfg->pk_bins) != cudaSuccess) {
+            cudaGetLastError();
+            set_error(5, "out of pinned host memory for the P(k) sums");
+            return 5;
+        }
+        s.acc_cap = cfg->pk_bins;
+    }
+    PipeOpts o;
+    o.acc = nullptr;
+    o.graph = false;
+    o.async_slot = k;
+    o.acc_host = s.acc_host;
+    o.iters = &s.iters;
+    o.last_rel = &s.last_rel;
+    e = pipeline_spline(cfg, spline, res, &o);
+    if (e) return e;
+    s.busy = true;
+    s.cfg = *cfg;
+    s.res = res;
+    s.order = g_order++;
+    g_next = k ^ 1;
+    return 0;
+}
+
+extern "C" int ic_pipeline_wait(void) {
+    const int first = (g_slot[0].busy && g_slot[1].busy && g_slot[1].order < g_slot[0].order) ? 1 : 0;
+    int e = finish_slot(first);
+    const int e2 = finish_slot(first ^ 1);
+    return e ? e : e2;
 }

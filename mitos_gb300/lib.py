@@ -527,3 +527,13 @@ def ranlxd1_uniforms(seed: int, n: int) -> np.ndarray:
     out = np.zeros(n)
     _check(load().mitos_ranlxd1_uniforms(ctypes.c_ulong(seed), ctypes.c_long(n), out.ctypes.data_as(_dp)))
     return out
+
+
+# ---- asynchronous IC submission --------------------------------------------------------------
+def ic_pipeline_submit(cfg: ICConfig, spline: Spline, res: ICResult) -> None:
+    """enqueue one IC; res (and its arrays) must stay alive until ic_pipeline_wait returns"""
+    _check(load().ic_pipeline_submit(ctypes.byref(cfg), ctypes.byref(spline.sp), ctypes.byref(res)))
+
+
+def ic_pipeline_wait() -> None:
+    _check(load().ic_pipeline_wait())

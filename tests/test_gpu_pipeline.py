@@ -1,5 +1,7 @@
 """GPU parity of the fused initial-condition pipeline against the oracle (the reference restated)
 and the FP32 precision study against the FP64 GPU path."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -64,3 +66,35 @@ def test_precision_study_fp32_vs_fp64(N, L, seed, bins, table, spline):
     d32 = _wrapdiff(q, o32["pos"], L)
     rms = np.sqrt(np.mean((d32 - d64) ** 2)) / np.sqrt(np.mean(d64 ** 2))
     assert rms < 1e-5, rms
+
+
+def test_async_submissions_match_synchronous_runs(table, spline):
+    """ic_pipeline_submit: three ICs in flight in a row (positions into pinned and pageable host
+    buffers) give the positions of ic_pipeline_run bit for bit and its P(k) to the tolerance of the
+    floating-point atomics in the CIC flush and the P(k) sums"""
+    torch = pytest.importorskip("torch")
+    N, L, bins = 64, 256.0, 32
+    seeds = [11, 12, 13]
+    refs = [ml.ic_pipeline_run(ml.ic_config(N, N, L, s, table, pk_bins=bins), spline, want_pos=True) for s in seeds]
+    keep = []
+    for i, s in enumerate(seeds):
+        k, p, o = np.zeros(bins), np.zeros(bins), np.zeros(bins, np.int64)
+        if i == 1:
+            pos_t = torch.zeros((N ** 3, 3), dtype=torch.float32, pin_memory=True)
+            pos, ptr = pos_t, ctypes.cast(pos_t.data_ptr(), ctypes.POINTER(ctypes.c_float))
+        else:
+            pos = np.zeros((N ** 3, 3), np.float32)
+            ptr = pos.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+        res = ml.ICResult(k.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                          p.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                          o.ctypes.data_as(ctypes.POINTER(ctypes.c_long)), ptr, 0, 0.0)
+        cfg = ml.ic_config(N, N, L, s, table, pk_bins=bins)
+        ml.ic_pipeline_submit(cfg, spline, res)
+        keep.append((k, p, o, pos, res, cfg))
+    ml.ic_pipeline_wait()
+    for (k, p, o, pos, res, cfg), ref in zip(keep, refs):
+        got = pos.numpy() if hasattr(pos, "numpy") else pos
+        assert np.array_equal(got, ref["pos"])
+        assert np.array_equal(o, ref["pk_obs"])
+        assert np.allclose(k, ref["pk_k"], rtol=1e-12, equal_nan=True)
+        assert np.allclose(p, ref["pk_p"], rtol=1e-5, equal_nan=True)
