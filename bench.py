@@ -249,6 +249,22 @@ def extras(ml, table, spline, args) -> dict:
                 "loss_first": float(losses[:10].mean()), "loss_last": float(losses[-100:].mean()),
                 "held_out_loss": held_loss}}
 
+    # 1024^3 FP32 IC, L = 2000 Mpc/h (the large configuration; about 80 GB of workspace)
+    c1k = lambda seed: ml.ic_config(1024, 1024, 2000.0, seed, table, method=ml.METHOD_2LPT, pk_bins=256,
+                                    pk_linear=True, precision=ml.FP32)
+    r1k = ml.ic_pipeline_run(c1k(args.seed), spline)
+    ml.timer_start()
+    for i in range(3):
+        ml.ic_pipeline_run(c1k(args.seed + 1 + i), spline)
+    ms1k = ml.timer_stop() / 3
+    G1k = 1024 * 1024 * 513 * 8
+    peak, _ = peak_hbm()
+    out["ic1024"] = {"ms_per_ic": ms1k, "ic_per_s": 1e3 / ms1k, "pk_bins": 256,
+                     "pk_finite_bins": int(np.isfinite(r1k["pk_p"]).sum()),
+                     "roofline": {"model_bytes": 37 * G1k, "GBps": 37 * G1k / (ms1k / 1e3) / 1e9,
+                                  "frac": 37 * G1k / (ms1k / 1e3) / 1e9 / peak}}
+    ml.load().mitos_release_all()
+
     # N-GenIC-like field (src/grf_ngeniclike.c) at 512^3
     g = ml.alloc_local_grid(N, L, ml.FP32)
     ml.generate_ngeniclike_grf_dg(g, 1)
