@@ -374,15 +374,22 @@ int manet_training_pair(struct distributed_grid *potential, struct distributed_g
 /* ---- Ensembles of realisations in one CUDA graph (no reference counterpart: the reference runs
  * one realisation per process) -------------------------------------------------------------------
  * ic_ensemble_create runs every configuration once (workspaces, tables), then captures all of
- * them into one graph over `streams` concurrent streams (largest grids first).  A replay
- * (ic_ensemble_run) recomputes the same realisations; *ms receives its device time.
- * ic_ensemble_result fills P(k) of configuration i (pos is not produced). */
+ * them into one graph over `streams` concurrent streams (largest work first).  Configurations
+ * that differ only in the seed (Zel'dovich or 2LPT, lattice-aligned) form batched units: one
+ * launch per pass covers the whole unit.  A replay (ic_ensemble_run) recomputes the same
+ * realisations; *ms receives its device time.  ic_ensemble_result fills P(k) of configuration i
+ * (pos is not produced). */
 struct ic_ensemble;
 int ic_ensemble_create(struct ic_ensemble **ens, const struct ic_config *cfgs, int n,
                        const struct perturb_spline *spline, int streams);
+/* The same with at most max_batch realisations per unit (1: no batching; 0: as many as fit in
+ * 2^25 grid cells, the ic_ensemble_create default). */
+int ic_ensemble_create_batched(struct ic_ensemble **ens, const struct ic_config *cfgs, int n,
+                               const struct perturb_spline *spline, int streams, int max_batch);
 int ic_ensemble_run(struct ic_ensemble *ens, double *ms);
 int ic_ensemble_result(struct ic_ensemble *ens, int i, struct ic_result *res);
 int ic_ensemble_launches(const struct ic_ensemble *ens); /* kernel launches in one replay */
+int ic_ensemble_units(const struct ic_ensemble *ens);    /* batched pipeline runs in one replay */
 int ic_ensemble_destroy(struct ic_ensemble *ens);
 /* FFT tile autotuner: times the IC of cfg for every fitting pair of X/Y pencils per block and Z
  * rows per block, keeps the fastest for (N, precision) in this process and returns it. */

@@ -74,13 +74,17 @@ int grid_r2c(const GridGeom &g, int prec, double boxlen, const void *box, int rp
 // six Hessian components of phi (k space) through the fused X / Y / Z passes into out (real);
 // ZOP_HESS_2LPT writes the second-order source, ZOP_HESS_MA the Monge-Ampere residual
 int grid_hessian(const GridGeom &g, int prec, double boxlen, const void *phi, int zop,
-                 const void *rho, void *out, double *red, int window_order, void *out2) {
-    const size_t gb = (size_t)g.cells * csize(prec);
+                 const void *rho, void *out, double *red, int window_order, void *out2, int batch,
+                 size_t bstride) {
+    // batched (batch > 1): every grid holds batch realisations bstride bytes apart
+    const size_t gb = batch > 1 ? (size_t)batch * bstride : (size_t)g.cells * csize(prec);
     void *A[3], *B[6];
     for (int i = 0; i < 3; i++) if (!(A[i] = workspace(gb, 1 + i))) return 5;
     for (int i = 0; i < 6; i++) if (!(B[i] = workspace(gb, 4 + i))) return 5;
     PassArgs a;
     memset(&a, 0, sizeof a);
+    a.batch = batch;
+    a.bstride = batch > 1 ? (long long)bstride : 0;
     a.dk = 2 * M_PI / boxlen;
     a.scale = 1.0;
     a.window_order = window_order;

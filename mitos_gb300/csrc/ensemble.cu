@@ -1,10 +1,13 @@
 // ensemble.cu -- many independent realisations (any mix of grid sizes) as one CUDA graph, and the
 // FFT tile autotuner.  No reference counterpart: the reference runs one realisation per process.
 //
-// Creation runs every realisation once on its stream (allocating the workspaces of that stream's
-// set and uploading the tables), then captures the same launches into one graph: a fork from the
-// capture stream to S streams, each stream running its realisations back to back (largest grids
-// first, so the streams finish together), and a join.  A replay is one cudaGraphLaunch.
+// Members whose configurations differ only in the seed form batched units: one pipeline run
+// covers up to max_batch of them, every pass one launch over all their grids (a 128^3 pass alone
+// fills a fraction of the GPU and is bound by its launch and tail latencies).  Creation runs every
+// unit once on its stream (allocating the workspaces of that stream's set and uploading the
+// tables), then captures the same launches into one graph: a fork from the capture stream to S
+// streams, each stream running its units back to back (largest first, so the streams finish
+// together), and a join.  A replay is one cudaGraphLaunch.
 #include <math.h>
 #include <string.h>
 
@@ -13,17 +16,27 @@
 
 #include "context.cuh"
 #include "grids.cuh"
+#include "particles.cuh"
 
 namespace mitos {
 
+struct Unit {
+    struct ic_config cfg;             // the members' configuration (the seed of the first)
+    int batch = 1;
+    double *acc = nullptr;            // device P(k) accumulators, batch x (3 pk_bins + 2)
+    uint64_t *states = nullptr;       // device start states, batch x 4
+    double *dtab = nullptr;           // device transfer rows of cfg
+    int stream = 0;
+};
+
 struct Member {
     struct ic_config cfg;
-    double *acc = nullptr;  // device P(k) accumulators
-    int stream = 0;
+    int unit = 0, index = 0;          // realisation index within the unit
 };
 
 struct Ensemble {
     std::vector<Member> m;
+    std::vector<Unit> u;
     std::vector<cudaStream_t> streams;
     cudaStream_t cap = nullptr;
     cudaGraph_t graph = nullptr;
@@ -37,8 +50,11 @@ static void destroy(Ensemble *e) {
     if (!e) return;
     if (e->exec) cudaGraphExecDestroy(e->exec);
     if (e->graph) cudaGraphDestroy(e->graph);
-    for (auto &m : e->m)
-        if (m.acc) cudaFree(m.acc);
+    for (auto &u : e->u) {
+        if (u.acc) cudaFree(u.acc);
+        if (u.states) cudaFree(u.states);
+        if (u.dtab) cudaFree(u.dtab);
+    }
     for (auto s : e->streams) cudaStreamDestroy(s);
     if (e->cap) cudaStreamDestroy(e->cap);
     if (e->t0) cudaEventDestroy(e->t0);
@@ -46,14 +62,29 @@ static void destroy(Ensemble *e) {
     delete e;
 }
 
-// run (or capture) every member on its stream and workspace set
+// configurations that one batched run can cover: all fields but the seed equal
+static bool same_but_seed(const struct ic_config &a, const struct ic_config &b) {
+    return a.N == b.N && a.M == b.M && a.boxlen == b.boxlen && a.A_s == b.A_s && a.n_s == b.n_s &&
+           a.k_pivot == b.k_pivot && a.z_ini == b.z_ini && a.index_src == b.index_src && a.method == b.method &&
+           a.ma_cycles == b.ma_cycles && a.ma_tol == b.ma_tol && a.pk_bins == b.pk_bins &&
+           a.pk_linear == b.pk_linear && a.precision == b.precision;
+}
+
+static bool batchable(const struct ic_config &c) {
+    return c.method != MITOS_METHOD_MONGE_AMPERE && lattice_aligned(c.N, c.M, c.boxlen);
+}
+
+// run (or capture) every unit on its stream and workspace set, in the order of e->u
 static int enqueue_all(Ensemble *e, bool graph) {
     int err = 0;
-    for (auto &m : e->m) {
-        set_stream(e->streams[m.stream]);
-        set_workspace_set(1000 + m.stream);
-        PipeOpts o = {m.acc, graph};
-        err = pipeline_spline(&m.cfg, e->spline, nullptr, &o);
+    for (auto &u : e->u) {
+        set_stream(e->streams[u.stream]);
+        set_workspace_set(1000 + u.stream);
+        PipeOpts o = {u.acc, graph};
+        o.batch = u.batch;
+        o.states = u.states;
+        o.dtab = u.dtab;
+        err = pipeline_spline(&u.cfg, e->spline, nullptr, &o);
         if (err) break;
     }
     set_stream(nullptr);
@@ -61,13 +92,16 @@ static int enqueue_all(Ensemble *e, bool graph) {
     return err;
 }
 
+// members of one unit at most this many grid cells together (a 16 x 128^3 batch)
+static const double UNIT_CELLS = 33554432.0;
+
 }  // namespace mitos
 
 using namespace mitos;
 
-extern "C" int ic_ensemble_create(struct ic_ensemble **out, const struct ic_config *cfgs, int n,
-                                  const struct perturb_spline *spline, int nstreams) {
-    if (!out || !cfgs || n < 1 || !spline || nstreams < 1) {
+extern "C" int ic_ensemble_create_batched(struct ic_ensemble **out, const struct ic_config *cfgs, int n,
+                                          const struct perturb_spline *spline, int nstreams, int max_batch) {
+    if (!out || !cfgs || n < 1 || !spline || !spline->ptdat || nstreams < 1 || max_batch < 0) {
         set_error(1, "invalid ensemble arguments");
         return 1;
     }
@@ -75,23 +109,44 @@ extern "C" int ic_ensemble_create(struct ic_ensemble **out, const struct ic_conf
     e->spline = spline;
     e->m.resize(n);
     for (int i = 0; i < n; i++) e->m[i].cfg = cfgs[i];
-    // longest-processing-time assignment: members by decreasing N^3 to the least loaded stream
-    std::vector<int> order(n);
-    for (int i = 0; i < n; i++) order[i] = i;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cfgs[a].N > cfgs[b].N; });
-    const int S = std::min(nstreams, n);
+    // units: members in input order join the first open unit of an equal configuration
+    for (int i = 0; i < n; i++) {
+        const struct ic_config &c = cfgs[i];
+        const double cells = pow((double)c.N, 3);
+        int cap = max_batch > 0 ? max_batch : std::max(1, (int)(UNIT_CELLS / cells));
+        if (!batchable(c)) cap = 1;
+        int k = -1;
+        for (int j = 0; j < (int)e->u.size() && k < 0; j++)
+            if (e->u[j].batch < cap && same_but_seed(e->u[j].cfg, c)) k = j;
+        if (k < 0) {
+            e->u.emplace_back();
+            e->u.back().cfg = c;
+            e->u.back().batch = 0;
+            k = (int)e->u.size() - 1;
+        }
+        e->m[i].unit = k;
+        e->m[i].index = e->u[k].batch++;
+    }
+    // longest-processing-time assignment: units by decreasing work to the least loaded stream;
+    // units keep that order within each stream
+    const int nu = (int)e->u.size();
+    std::vector<int> order(nu);
+    for (int i = 0; i < nu; i++) order[i] = i;
+    auto work = [&](int i) { return pow((double)e->u[i].cfg.N, 3) * e->u[i].batch; };
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return work(a) > work(b); });
+    const int S = std::min(nstreams, nu);
     std::vector<double> load(S, 0.0);
+    std::vector<int> where(nu);
+    std::vector<Unit> sorted;
     for (int i : order) {
         const int s = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-        e->m[i].stream = s;
-        load[s] += pow((double)cfgs[i].N, 3);
+        e->u[i].stream = s;
+        load[s] += work(i);
+        where[i] = (int)sorted.size();
+        sorted.push_back(e->u[i]);
     }
-    // members run in the order above within each stream
-    std::vector<Member> sorted;
-    for (int i : order) sorted.push_back(e->m[i]);
-    std::vector<int> where(n);
-    for (int k = 0; k < n; k++) where[order[k]] = k;
-    e->m = sorted;
+    e->u = sorted;
+    for (auto &m : e->m) m.unit = where[m.unit];
     int err = 0;
     e->streams.resize(S);
     for (int s = 0; s < S && !err; s++)
@@ -99,9 +154,23 @@ extern "C" int ic_ensemble_create(struct ic_ensemble **out, const struct ic_conf
     if (!err && (cudaStreamCreateWithFlags(&e->cap, cudaStreamNonBlocking) != cudaSuccess ||
                  cudaEventCreate(&e->t0) != cudaSuccess || cudaEventCreate(&e->t1) != cudaSuccess))
         err = 4;
-    for (auto &m : e->m) {
+    const int k_size = spline->ptdat->k_size;
+    for (auto &u : e->u) {
         if (err) break;
-        if (cudaMalloc(&m.acc, sizeof(double) * (3 * (size_t)m.cfg.pk_bins + 2)) != cudaSuccess) err = 5;
+        if (cudaMalloc(&u.acc, sizeof(double) * (3 * (size_t)u.cfg.pk_bins + 2) * u.batch) != cudaSuccess ||
+            cudaMalloc(&u.states, sizeof(uint64_t) * 4 * u.batch) != cudaSuccess ||
+            cudaMalloc(&u.dtab, sizeof(double) * 3 * (size_t)k_size) != cudaSuccess)
+            err = 5;
+    }
+    if (!err) {
+        // start states of every realisation, in unit order
+        std::vector<std::vector<uint64_t>> st(e->u.size());
+        for (size_t k = 0; k < e->u.size(); k++) st[k].resize(4 * (size_t)e->u[k].batch);
+        for (auto &m : e->m) seed_state(m.cfg.seed, &st[m.unit][4 * (size_t)m.index]);
+        for (size_t k = 0; k < e->u.size() && !err; k++)
+            if (cudaMemcpy(e->u[k].states, st[k].data(), sizeof(uint64_t) * st[k].size(), cudaMemcpyHostToDevice) !=
+                cudaSuccess)
+                err = 4;
     }
     if (err) {
         cudaGetLastError();
@@ -112,7 +181,7 @@ extern "C" int ic_ensemble_create(struct ic_ensemble **out, const struct ic_conf
     // 1) one uncaptured pass: workspaces, tables, kernel attributes
     err = enqueue_all(e, false);
     if (!err && cudaDeviceSynchronize() != cudaSuccess) err = check_cuda(cudaGetLastError(), "ensemble warm-up");
-    // 2) capture: fork to the member streams, run, join
+    // 2) capture: fork to the unit streams, run, join
     if (!err) {
         std::vector<cudaEvent_t> ev(S + 1);
         for (auto &x : ev) cudaEventCreateWithFlags(&x, cudaEventDisableTiming);
@@ -138,12 +207,18 @@ extern "C" int ic_ensemble_create(struct ic_ensemble **out, const struct ic_conf
         destroy(e);
         return err;
     }
-    // the caller's index i refers to cfgs[i]: keep the permutation in the member order
-    std::vector<Member> back(n);
-    for (int i = 0; i < n; i++) back[i] = e->m[where[i]];
-    e->m = back;
     *out = reinterpret_cast<struct ic_ensemble *>(e);
     return 0;
+}
+
+extern "C" int ic_ensemble_create(struct ic_ensemble **out, const struct ic_config *cfgs, int n,
+                                  const struct perturb_spline *spline, int nstreams) {
+    return ic_ensemble_create_batched(out, cfgs, n, spline, nstreams, 0);
+}
+
+extern "C" int ic_ensemble_units(const struct ic_ensemble *ens) {
+    const Ensemble *e = reinterpret_cast<const Ensemble *>(ens);
+    return e ? (int)e->u.size() : 0;
 }
 
 extern "C" int ic_ensemble_run(struct ic_ensemble *ens, double *ms) {
@@ -165,12 +240,13 @@ extern "C" int ic_ensemble_result(struct ic_ensemble *ens, int i, struct ic_resu
     if (!e || i < 0 || i >= (int)e->m.size() || !res) return 1;
     const Member &m = e->m[i];
     const int bins = m.cfg.pk_bins;
+    const double *acc = e->u[m.unit].acc + (size_t)m.index * (3 * (size_t)bins + 2);
     const double *ksum;
     const long long *count;
     int err = bin_geometry(m.cfg.N, bins, m.cfg.pk_linear, m.cfg.boxlen, &ksum, &count);
     if (err) return err;
     std::vector<double> h(bins);
-    MITOS_CUDA(cudaMemcpy(h.data(), m.acc + bins, sizeof(double) * bins, cudaMemcpyDeviceToHost));
+    MITOS_CUDA(cudaMemcpy(h.data(), acc + bins, sizeof(double) * bins, cudaMemcpyDeviceToHost));
     const double V = m.cfg.boxlen * m.cfg.boxlen * m.cfg.boxlen;
     for (int b = 0; b < bins; b++) {
         const double nb = (double)count[b];

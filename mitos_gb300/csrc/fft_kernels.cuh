@@ -58,6 +58,7 @@ __global__ void __launch_bounds__(strided_heavy<AXIS, OP, NL>() ? 256 : 512, 2) 
     const T dk = (T)a.dk;
     const T scale = (T)a.scale;
     cplx<T> *psm = sm + p;
+    const size_t bo = (size_t)blockIdx.y * (size_t)a.bstride;  // realisation of a batched launch
 
     // P(k): one power histogram per warp behind the FFT exchange buffer (the counts and the
     // wavenumber sums of the bins depend only on the geometry and are tabulated on the host)
@@ -76,7 +77,7 @@ __global__ void __launch_bounds__(strided_heavy<AXIS, OP, NL>() ? 256 : 512, 2) 
     cplx<T> v[E];
 #pragma unroll 1
     for (int i = 0; i < NIN; i++) {
-        const cplx<T> *src = reinterpret_cast<const cplx<T> *>(a.in[i]);
+        const cplx<T> *src = bat<const cplx<T>>(a.in[i], bo);
 #pragma unroll
         for (int e = 0; e < E; e++) {
             int n = nin_any<NL, E>(pl, t, e);
@@ -123,7 +124,7 @@ __global__ void __launch_bounds__(strided_heavy<AXIS, OP, NL>() ? 256 : 512, 2) 
             fft_any<T, E, SIGN, NL, PC>(pl, v, psm, P, t, tw);
             // the P(k) epilogue keeps the whole warp together (warp-level bin sums)
             if (!valid && OP != XOP_PK) continue;
-            cplx<T> *dst = reinterpret_cast<cplx<T> *>(a.out[outs[m]]);
+            cplx<T> *dst = bat<cplx<T>>(a.out[outs[m]], bo);
 #pragma unroll
             for (int e = 0; e < E; e++) {
                 int n = nout_any<NL, E>(pl, t, e);
@@ -157,7 +158,7 @@ __global__ void __launch_bounds__(strided_heavy<AXIS, OP, NL>() ? 256 : 512, 2) 
                     } else {
                         const T kk2 = (T)n2 * dk * dk;
                         const T G = (n2 > 0) ? (T)-1 / kk2 : (T)1;
-                        const cplx<T> q = reinterpret_cast<const cplx<T> *>(a.in2)[idx];
+                        const cplx<T> q = bat<const cplx<T>>(a.in2, bo)[idx];
                         cplx<T> o;
                         if constexpr (OP == XOP_COMBINE_2LPT) {
                             const T f1 = (T)a.f1, f2 = (T)a.f2;
@@ -182,7 +183,7 @@ __global__ void __launch_bounds__(strided_heavy<AXIS, OP, NL>() ? 256 : 512, 2) 
         for (int i = tid; i < a.nbins; i += blockDim.x) {
             double sum = 0;
             for (int w = 0; w < nw; w++) sum += (double)hist[w * a.nbins + i];
-            if (sum != 0) atomicAdd(a.bin_p + i, sum);
+            if (sum != 0) atomicAdd(a.bin_p + (size_t)blockIdx.y * a.acc_stride + i, sum);
         }
     }
 }
@@ -209,8 +210,9 @@ __global__ void __launch_bounds__(512, 2) k_x_combine_disp(GridGeom g, PassArgs 
     const T dk = (T)a.dk, scale = (T)a.scale, f1 = (T)a.f1, f2 = (T)a.f2;
     const T *stn = reinterpret_cast<const T *>(a.stencil);
     cplx<T> *psm = sm + p;
-    const cplx<T> *src = reinterpret_cast<const cplx<T> *>(a.in[0]);
-    const cplx<T> *phi1 = reinterpret_cast<const cplx<T> *>(a.in2);
+    const size_t bo = (size_t)blockIdx.y * (size_t)a.bstride;
+    const cplx<T> *src = bat<const cplx<T>>(a.in[0], bo);
+    const cplx<T> *phi1 = bat<const cplx<T>>(a.in2, bo);
     cplx<T> v[E];
 #pragma unroll
     for (int e = 0; e < E; e++) v[e] = valid ? src[col + (long)nin_any<NL, E>(pl, t, e) * g.plane] : mk<T>(0, 0);
@@ -247,7 +249,7 @@ __global__ void __launch_bounds__(512, 2) k_x_combine_disp(GridGeom g, PassArgs 
         }
         fft_any<T, E, 1, NL, PC>(pl, v, psm, P, t, tw);
         if (valid) {
-            cplx<T> *dst = reinterpret_cast<cplx<T> *>(a.out[m]);
+            cplx<T> *dst = bat<cplx<T>>(a.out[m], bo);
 #pragma unroll
             for (int e = 0; e < E; e++) dst[col + (long)nout_any<NL, E>(pl, t, e) * g.plane] = v[e];
         }
@@ -273,6 +275,7 @@ __global__ void __launch_bounds__(256, OP == ZOP_HESS_MA ? 1 : 2) k_z_c2r(GridGe
     const T dk = (T)a.dk;
     const T scale = (T)a.scale;
     cplx<T> *psm = sm + (long)p * spad_len(h);
+    const size_t bo = (size_t)blockIdx.y * (size_t)a.bstride;
 
     constexpr int NIN = (OP == ZOP_C2R) ? 1 : (OP == ZOP_DISP) ? 3 : 6;
     // inputs of the Hessian passes are [xx, xy, xz, yy, yz, zz]; the 2LPT source is accumulated
@@ -289,7 +292,7 @@ __global__ void __launch_bounds__(256, OP == ZOP_HESS_MA ? 1 : 2) k_z_c2r(GridGe
         int fac = 0;
         if (OP == ZOP_HESS_2LPT || OP == ZOP_HESS_MA) fac = (f == 2 || f == 4) ? 1 : (f == 5 ? 2 : 0);
         if (OP == ZOP_DISP) fac = (f == 2) ? 1 : 0;
-        const cplx<T> *src = reinterpret_cast<const cplx<T> *>(a.in[f]) + row * H;
+        const cplx<T> *src = bat<const cplx<T>>(a.in[f], bo) + row * H;
         cplx<T> v[E];
 #pragma unroll
         for (int e = 0; e < E; e++) {
@@ -315,7 +318,7 @@ __global__ void __launch_bounds__(256, OP == ZOP_HESS_MA ? 1 : 2) k_z_c2r(GridGe
         fft_any<T, E, 1, NL, 1>(pl, v, psm, 1, t, tw);
         if constexpr (OP == ZOP_C2R || OP == ZOP_DISP) {
             if (valid) {
-                T *dst = reinterpret_cast<T *>(a.out[f]) + row * a.rp_out;
+                T *dst = bat<T>(a.out[f], bo) + row * a.rp_out;
 #pragma unroll
                 for (int e = 0; e < E; e++) {
                     const int n = nout_any<NL, E>(pl, t, e);
@@ -344,7 +347,7 @@ __global__ void __launch_bounds__(256, OP == ZOP_HESS_MA ? 1 : 2) k_z_c2r(GridGe
     (void)dst_row;
     if (!valid) return;
     if constexpr (OP == ZOP_HESS_2LPT) {
-        T *dst = reinterpret_cast<T *>(a.out[0]) + row * a.rp_out;
+        T *dst = bat<T>(a.out[0], bo) + row * a.rp_out;
 #pragma unroll
         for (int e = 0; e < E; e++) {
             const int n = nout_any<NL, E>(pl, t, e);
@@ -354,9 +357,9 @@ __global__ void __launch_bounds__(256, OP == ZOP_HESS_MA ? 1 : 2) k_z_c2r(GridGe
         return;
     }
     if constexpr (OP == ZOP_HESS_MA) {
-        T *dst = reinterpret_cast<T *>(a.out[0]) + row * a.rp_out;
+        T *dst = bat<T>(a.out[0], bo) + row * a.rp_out;
         double sres = 0, srho = 0;
-        const T *rho = (OP == ZOP_HESS_MA) ? reinterpret_cast<const T *>(a.in2) + row * a.rp_in : nullptr;
+        const T *rho = (OP == ZOP_HESS_MA) ? bat<const T>(a.in2, bo) + row * a.rp_in : nullptr;
 #pragma unroll
         for (int e = 0; e < E; e++) {
             const int n = nout_any<NL, E>(pl, t, e);
@@ -386,7 +389,7 @@ __global__ void __launch_bounds__(256, OP == ZOP_HESS_MA ? 1 : 2) k_z_c2r(GridGe
             }
             *reinterpret_cast<cplx<T> *>(dst + 2 * n) = mk<T>(res2[0], res2[1]);
             // optional second output: the second-order source S of the same Hessian
-            if (a.out[1]) *reinterpret_cast<cplx<T> *>(reinterpret_cast<T *>(a.out[1]) + row * a.rp_out + 2 * n) = mk<T>(s2v[0], s2v[1]);
+            if (a.out[1]) *reinterpret_cast<cplx<T> *>(bat<T>(a.out[1], bo) + row * a.rp_out + 2 * n) = mk<T>(s2v[0], s2v[1]);
         }
         if (t == 0 && a.rp_out > N) { dst[N] = 0; dst[N + 1] = 0; }
         if constexpr (OP == ZOP_HESS_MA) {
@@ -395,8 +398,8 @@ __global__ void __launch_bounds__(256, OP == ZOP_HESS_MA ? 1 : 2) k_z_c2r(GridGe
                 srho += __shfl_down_sync(0xffffffffu, srho, off);
             }
             if ((threadIdx.x & 31) == 0) {
-                atomicAdd(a.red + 0, sres);
-                atomicAdd(a.red + 1, srho);
+                atomicAdd(a.red + (size_t)blockIdx.y * a.acc_stride + 0, sres);
+                atomicAdd(a.red + (size_t)blockIdx.y * a.acc_stride + 1, srho);
             }
         }
     }
@@ -419,7 +422,8 @@ __global__ void __launch_bounds__(256) k_z_r2c(GridGeom g, PassArgs a) {
     const cplx<T> *tw = reinterpret_cast<const cplx<T> *>(g.twN);
     cplx<T> *psm = sm + (long)p * spad_len(h);
     const T ra = (T)a.rho_a, rb = (T)a.rho_b;
-    const T *src = reinterpret_cast<const T *>(a.in[0]) + row * a.rp_in;
+    const size_t bo = (size_t)blockIdx.y * (size_t)a.bstride;
+    const T *src = bat<const T>(a.in[0], bo) + row * a.rp_in;
     cplx<T> v[E];
 #pragma unroll
     for (int e = 0; e < E; e++) {
@@ -433,7 +437,7 @@ __global__ void __launch_bounds__(256) k_z_r2c(GridGeom g, PassArgs a) {
     for (int e = 0; e < E; e++) psm[xpos<NL, 1>(nout_any<NL, E>(pl, t, e))] = v[e];
     __syncthreads();
     if (!valid) return;
-    cplx<T> *dst = reinterpret_cast<cplx<T> *>(a.out[0]) + row * H;
+    cplx<T> *dst = bat<cplx<T>>(a.out[0], bo) + row * H;
     for (int k = t; k <= h; k += tpp) {
         const cplx<T> Z = psm[xpos<NL, 1>(k == h ? 0 : k)];
         const cplx<T> Zc = psm[xpos<NL, 1>(k == 0 ? 0 : h - k)];
@@ -459,7 +463,7 @@ static int launch_strided_e(const GridGeom &g, const PassArgs &a, const T *win) 
     if (smem > 48 * 1024) MITOS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     launch_begin(AXIS == 0 ? (OP == XOP_HESS ? "x_hess" : OP == XOP_DISP ? "x_disp" : OP == XOP_COMBINE_2LPT ? "x_combine" : OP == XOP_ADD_POISSON ? "x_add_poisson" : OP == XOP_PK ? "x_pk" : "x_plain")
                         : (OP == YOP_HESS ? "y_hess" : OP == YOP_DISP ? "y_disp" : "y_plain"));
-    kern<<<(unsigned)blocks, threads, smem, stream()>>>(g, a, win);
+    kern<<<dim3((unsigned)blocks, a.batch > 1 ? a.batch : 1), threads, smem, stream()>>>(g, a, win);
     count_launch();
     MITOS_LAUNCH_CHECK("strided FFT pass");
     return 0;
@@ -499,11 +503,11 @@ int launch_x_t(const GridGeom &g, XOp op, int sign, const PassArgs &a) {
         if (NL > 0 || g.E == 8) {
             auto kern = k_x_combine_disp<T, 8, NL, PC>;
             if (smem > 48 * 1024) MITOS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            kern<<<(unsigned)blocks, threads, smem, stream()>>>(g, a, win);
+            kern<<<dim3((unsigned)blocks, a.batch > 1 ? a.batch : 1), threads, smem, stream()>>>(g, a, win);
         } else {
             auto kern = k_x_combine_disp<T, 12, 0, 0>;
             if (smem > 48 * 1024) MITOS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            kern<<<(unsigned)blocks, threads, smem, stream()>>>(g, a, win);
+            kern<<<dim3((unsigned)blocks, a.batch > 1 ? a.batch : 1), threads, smem, stream()>>>(g, a, win);
         }
         count_launch();
         MITOS_LAUNCH_CHECK("x combine + displacement pass");
@@ -536,7 +540,7 @@ static int launch_zc_e(const GridGeom &g, const PassArgs &a) {
     auto kern = k_z_c2r<T, E, OP, NLZ>;
     if (smem > 48 * 1024) MITOS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     launch_begin(OP == ZOP_C2R ? "z_c2r" : OP == ZOP_HESS_2LPT ? "z_hess_2lpt" : OP == ZOP_HESS_MA ? "z_hess_ma" : "z_disp");
-    kern<<<(unsigned)((rows + P - 1) / P), threads, smem, stream()>>>(g, a);
+    kern<<<dim3((unsigned)((rows + P - 1) / P), a.batch > 1 ? a.batch : 1), threads, smem, stream()>>>(g, a);
     count_launch();
     MITOS_LAUNCH_CHECK("z c2r pass");
     return 0;
@@ -572,7 +576,7 @@ static int launch_zr_e(const GridGeom &g, const PassArgs &a) {
     auto kern = k_z_r2c<T, E, NLZ>;
     if (smem > 48 * 1024) MITOS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     launch_begin("z_r2c");
-    kern<<<(unsigned)((rows + P - 1) / P), P * tpp, smem, stream()>>>(g, a);
+    kern<<<dim3((unsigned)((rows + P - 1) / P), a.batch > 1 ? a.batch : 1), P * tpp, smem, stream()>>>(g, a);
     count_launch();
     MITOS_LAUNCH_CHECK("z r2c pass");
     return 0;

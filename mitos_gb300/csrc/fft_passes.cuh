@@ -71,7 +71,17 @@ struct PassArgs {
     // axes along which the later gather sits on grid nodes (x for d_x, y for d_x and d_y, z for
     // all three); table of 3/4 + cos(2 pi m / N)/4 at m + N/2
     const void *stencil;
+    // batched launches (the ensemble): batch realisations, blockIdx.y = realisation, every grid
+    // pointer (in, out, in2) bstride bytes apart, the P(k) / residual sums acc_stride doubles apart
+    int batch;            // 0 or 1: one realisation
+    long long bstride;
+    int acc_stride;
 };
+
+// pointer p shifted by bo bytes (null stays null)
+template <typename P> __host__ __device__ __forceinline__ P *bat(const void *p, size_t bo) {
+    return p ? reinterpret_cast<P *>(const_cast<char *>(reinterpret_cast<const char *>(p)) + bo) : nullptr;
+}
 
 template <typename T> int launch_x(const GridGeom &g, XOp op, int sign, const PassArgs &a);
 template <typename T> int launch_y(const GridGeom &g, YOp op, int sign, const PassArgs &a);

@@ -15,7 +15,7 @@ int grid_r2c(const GridGeom &g, int prec, double boxlen, const void *box, int rp
 // ZOP_HESS_2LPT writes the second-order source, ZOP_HESS_MA the Monge-Ampere residual (and, when
 // out2 is given, the second-order source too)
 int grid_hessian(const GridGeom &g, int prec, double boxlen, const void *phi, int zop, const void *rho, void *out,
-                 double *red, int window_order, void *out2 = nullptr);
+                 double *red, int window_order, void *out2 = nullptr, int batch = 1, size_t bstride = 0);
 int axpby(int prec, long n, double a, const void *x, double b, const void *y, void *out);
 inline size_t csize(int prec) { return prec == MITOS_FP32 ? 8 : 16; }
 
@@ -25,11 +25,18 @@ inline size_t csize(int prec) { return prec == MITOS_FP32 ? 8 : 16; }
 struct PipeOpts {
     double *acc;
     bool graph;
+    // batch > 1: that many realisations of cfg, realisation b started at states[4 b .. 4 b + 3]
+    // (device; seed_state of its seed), its P(k) sums at acc + b (3 pk_bins + 2); one launch per pass
+    int batch = 1;
+    const uint64_t *states = nullptr;
+    double *dtab = nullptr;      // device transfer rows of this run (3 k_size), or the workspace's
     int async_slot = -1;         // >= 0: an ic_pipeline_submit run in staging slot 0 or 1
     double *acc_host = nullptr;  // async: pinned host buffer for the power sums
     int *iters = nullptr;        // async: Monge-Ampere cycles and residual, filled on the host
     double *last_rel = nullptr;
 };
+// the xoshiro256** start state of a seed (splitmix64, as the reference seeds Seed + rank 0)
+void seed_state(uint64_t seed, uint64_t st[4]);
 int pipeline_table(const struct ic_config *cfg, int k_size, int tau_size, int n_functions, const double *k,
                    const double *log_tau, const double *redshift, const double *D_growth, const double *delta,
                    struct ic_result *res, const PipeOpts *opt);

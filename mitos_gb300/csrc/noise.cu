@@ -267,7 +267,12 @@ template <> __device__ __forceinline__ double gauss<double>(uint64_t A, uint64_t
 template <typename T>
 __global__ void __launch_bounds__(NOISE_THREADS)
 k_noise(int N, const uint64_t *__restrict__ polys, RngState s0, T factor, const T *__restrict__ filt,
-        cplx<T> *__restrict__ out) {
+        cplx<T> *__restrict__ out, const RngState *__restrict__ states, size_t ostride) {
+    // batched launches: realisation blockIdx.y has its own start state and output grid
+    if (states) {
+        s0 = states[blockIdx.y];
+        out = bat<cplx<T>>(out, (size_t)blockIdx.y * ostride);
+    }
     __shared__ cplx<T> stage[NOISE_THREADS][NOISE_CHUNK + 1];
     const int H = N / 2 + 1;
     const long ncol = (long)N * N;
@@ -345,10 +350,11 @@ k_noise(int N, const uint64_t *__restrict__ polys, RngState s0, T factor, const 
 // enforce_hermiticity on the kz = 0 and kz = N/2 planes (src/grf.c:103-137): targets are never
 // sources, so the planes are fixed in place
 template <typename T>
-__global__ void k_hermitian(int N, cplx<T> *fbox) {
+__global__ void k_hermitian(int N, cplx<T> *fbox, size_t bstride) {
     const int H = N / 2 + 1;
     const int x = blockIdx.y;  // 0 .. N/2
-    const int zsel = blockIdx.z;
+    const int zsel = blockIdx.z & 1;
+    fbox = bat<cplx<T>>(fbox, (size_t)(blockIdx.z >> 1) * bstride);  // realisation of a batch
     const int z = zsel ? N / 2 : 0;
     for (int y = blockIdx.x * blockDim.x + threadIdx.x; y < N; y += gridDim.x * blockDim.x) {
         if ((x == 0 || x == N / 2) && y > N / 2) continue;
@@ -365,7 +371,7 @@ __global__ void k_hermitian(int N, cplx<T> *fbox) {
 }
 
 int noise_generate(const GridGeom &g, int precision, double boxlen, uint64_t st[4],
-                   const void *filter_by_n2, void *fbox) {
+                   const void *filter_by_n2, void *fbox, const void *states, int batch, size_t bstride) {
     const uint64_t *polys = column_polys(g.N);
     if (!polys) return 5;
     RngState s0;
@@ -374,23 +380,25 @@ int noise_generate(const GridGeom &g, int precision, double boxlen, uint64_t st[
     const double factor = sqrt(boxvol / 2);  // src/grf.c:33
     const long ncol = (long)g.N * g.N;
     const unsigned blocks = (unsigned)((ncol + NOISE_THREADS - 1) / NOISE_THREADS);
+    const dim3 grid(blocks, states && batch > 1 ? batch : 1);
+    const RngState *sts = (const RngState *)states;
     launch_begin("noise");
     if (precision == MITOS_FP32)
-        k_noise<float><<<blocks, NOISE_THREADS, 0, stream()>>>(g.N, polys, s0, (float)factor,
-                                                               (const float *)filter_by_n2, (float2 *)fbox);
+        k_noise<float><<<grid, NOISE_THREADS, 0, stream()>>>(g.N, polys, s0, (float)factor,
+                                                             (const float *)filter_by_n2, (float2 *)fbox, sts, bstride);
     else
-        k_noise<double><<<blocks, NOISE_THREADS, 0, stream()>>>(g.N, polys, s0, factor,
-                                                                (const double *)filter_by_n2, (double2 *)fbox);
+        k_noise<double><<<grid, NOISE_THREADS, 0, stream()>>>(g.N, polys, s0, factor,
+                                                              (const double *)filter_by_n2, (double2 *)fbox, sts, bstride);
     count_launch();
     MITOS_LAUNCH_CHECK("noise");
     return 0;
 }
 
-int hermitian_planes(const GridGeom &g, int precision, void *fbox) {
-    dim3 grid((g.N + 255) / 256, g.N / 2 + 1, 2);
+int hermitian_planes(const GridGeom &g, int precision, void *fbox, int batch, size_t bstride) {
+    dim3 grid((g.N + 255) / 256, g.N / 2 + 1, 2 * (batch > 1 ? batch : 1));
     launch_begin("hermitian");
-    if (precision == MITOS_FP32) k_hermitian<float><<<grid, 256, 0, stream()>>>(g.N, (float2 *)fbox);
-    else k_hermitian<double><<<grid, 256, 0, stream()>>>(g.N, (double2 *)fbox);
+    if (precision == MITOS_FP32) k_hermitian<float><<<grid, 256, 0, stream()>>>(g.N, (float2 *)fbox, bstride);
+    else k_hermitian<double><<<grid, 256, 0, stream()>>>(g.N, (double2 *)fbox, bstride);
     count_launch();
     MITOS_LAUNCH_CHECK("hermitian planes");
     return 0;

@@ -258,7 +258,15 @@ __device__ __forceinline__ void stage_tiles(T *tiles, int N, int rpd, int x0, in
 template <typename T>
 __global__ void __launch_bounds__(LB_THREADS, 2)
 k_lattice_cic(int N, int rpd, int rpo, float spacing, float Lf, T ginv, const T *__restrict__ d0, const T *__restrict__ d1,
-              const T *__restrict__ d2, T *__restrict__ rho, float *__restrict__ pos_out) {
+              const T *__restrict__ d2, T *__restrict__ rho, float *__restrict__ pos_out, size_t bstride) {
+    // batched launches: realisation blockIdx.y (its grids bstride bytes apart)
+    if (gridDim.y > 1) {
+        const size_t bo = (size_t)blockIdx.y * bstride;
+        d0 = bat<const T>(d0, bo);
+        d1 = bat<const T>(d1, bo);
+        d2 = bat<const T>(d2, bo);
+        rho = bat<T>(rho, bo);
+    }
     using A = typename RegAcc<T>::type;
     extern __shared__ __align__(16) unsigned char smraw[];
     A *reg = reinterpret_cast<A *>(smraw);                                      // LR_X * LR_Y * LR_Z
@@ -394,7 +402,7 @@ static size_t lattice_smem(size_t elem) {
 
 template <typename T>
 static int lattice_launch(int N, int rpd, int rpo, float spacing, float Lf, double ginv, const void *d0, const void *d1,
-                          const void *d2, void *rho, float *pos_out) {
+                          const void *d2, void *rho, float *pos_out, int batch, size_t bstride) {
     static int blocks_per_sm[2] = {0, 0};  // per precision, for the current device
     static int sms = 0;
     const size_t smem = lattice_smem(sizeof(T));
@@ -409,14 +417,15 @@ static int lattice_launch(int N, int rpd, int rpo, float spacing, float Lf, doub
         if (bps < 1) bps = 1;
     }
     const long nbricks = (long)(N / LB_X) * (N / LB_Y) * (N / LB_Z);
-    const unsigned blocks = (unsigned)std::min<long>(nbricks, (long)sms * bps);
-    kern<<<blocks, LB_THREADS, smem, stream()>>>(N, rpd, rpo, spacing, Lf, (T)ginv, (const T *)d0, (const T *)d1,
-                                                 (const T *)d2, (T *)rho, pos_out);
+    const int nb = batch > 1 ? batch : 1;
+    const unsigned blocks = (unsigned)std::max<long>(1, std::min<long>(nbricks, (long)sms * bps / nb));
+    kern<<<dim3(blocks, nb), LB_THREADS, smem, stream()>>>(N, rpd, rpo, spacing, Lf, (T)ginv, (const T *)d0,
+                                                           (const T *)d1, (const T *)d2, (T *)rho, pos_out, bstride);
     return 0;
 }
 
 int lattice_deposit(int N, double boxlen, int precision, const void *d0, const void *d1, const void *d2,
-                    int disp_pitch, void *rho, int rho_pitch, float *pos_out) {
+                    int disp_pitch, void *rho, int rho_pitch, float *pos_out, int batch, size_t bstride) {
     const size_t es = precision == MITOS_FP32 ? 4 : 8;
     if (N % LB_Z || N % LB_Y || N % LB_X || (rho_pitch * es) % 16 || (disp_pitch * es) % 16 ||
         ((uintptr_t)d0 | (uintptr_t)d1 | (uintptr_t)d2 | (uintptr_t)rho) % 16)
@@ -425,8 +434,10 @@ int lattice_deposit(int N, double boxlen, int precision, const void *d0, const v
     const float spacing = Lf / N;  // src/particle.c:102-103 with M = N
     launch_begin("lattice_cic");
     const int e = precision == MITOS_FP32
-                      ? lattice_launch<float>(N, disp_pitch, rho_pitch, spacing, Lf, N / boxlen, d0, d1, d2, rho, pos_out)
-                      : lattice_launch<double>(N, disp_pitch, rho_pitch, spacing, Lf, N / boxlen, d0, d1, d2, rho, pos_out);
+                      ? lattice_launch<float>(N, disp_pitch, rho_pitch, spacing, Lf, N / boxlen, d0, d1, d2, rho, pos_out,
+                                              batch, bstride)
+                      : lattice_launch<double>(N, disp_pitch, rho_pitch, spacing, Lf, N / boxlen, d0, d1, d2, rho, pos_out,
+                                               batch, bstride);
     if (e) return e;
     count_launch();
     MITOS_LAUNCH_CHECK("lattice CIC");

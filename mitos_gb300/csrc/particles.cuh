@@ -10,8 +10,9 @@ int displace_and_deposit(int N, int M, double boxlen, int precision, const void 
 // lattice-aligned fast path (M = N, exact nodes); the displacement grids must carry the folded
 // on-node TSC stencils (PassArgs::stencil in the displacement passes)
 // disp_pitch / rho_pitch: row pitches (elements) of the displacement grids and of rho, 16-byte multiples
+// batch > 1: that many realisations, every grid (d0, d1, d2, rho) bstride bytes apart; pos_out null
 int lattice_deposit(int N, double boxlen, int precision, const void *d0, const void *d1, const void *d2,
-                    int disp_pitch, void *rho, int rho_pitch, float *pos_out);
+                    int disp_pitch, void *rho, int rho_pitch, float *pos_out, int batch = 1, size_t bstride = 0);
 bool lattice_aligned(int N, int M, double boxlen);
 // CIC of n given positions with per-particle value val
 int cic_positions(long n, int N, double boxlen, int precision, const float *pos, double val, void *rho);

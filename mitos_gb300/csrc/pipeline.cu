@@ -13,6 +13,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "context.cuh"
@@ -112,6 +113,18 @@ static cudaEvent_t acc_event(int slot) {
     return ev[slot];
 }
 
+// splitmix64 seeding (include/random_xorshift.h:38-59) of Seed + rank 0
+void mitos::seed_state(uint64_t seed, uint64_t st[4]) {
+    uint64_t s = seed;
+    for (int i = 0; i < 4; i++) {
+        uint64_t r = s;
+        s = r + 0x9E3779B97f4A7C15ULL;
+        r = (r ^ (r >> 30)) * 0xBF58476D1CE4E5B9ULL;
+        r = (r ^ (r >> 27)) * 0x94D049BB133111EBULL;
+        st[i] = r ^ (r >> 31);
+    }
+}
+
 template <typename T>
 static int run_pipeline(const struct ic_config *cfg, const double *ktab, const double *tlo, const double *thi,
                         int k_size, double u_tau, struct ic_result *res, const PipeOpts *opt) {
@@ -121,27 +134,44 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     const GridGeom *gp = geom(N, prec);
     if (!gp) return 3;
     const GridGeom &g = *gp;
-    const size_t gb = (size_t)g.cells * sizeof(cplx<T>);
+    const size_t gb1 = (size_t)g.cells * sizeof(cplx<T>);
     const double V = L * L * L;
     const double dk = 2 * M_PI / L;
+    // displacement grids: row pitch N + 4 on the lattice-aligned path (16-byte aligned rows for
+    // the staged tile copies of the deposit), the reference's N + 2 otherwise
+    const bool aligned = lattice_aligned(N, M, L);
+    const int disp_pitch = aligned ? N + 4 : N + 2;
+    const size_t db1 = (size_t)N * N * disp_pitch * sizeof(T);
+    // batched runs (the ensemble): B realisations of cfg with their own start states, every grid
+    // of realisation b at b * bs bytes from the first; one launch per pass covers all of them
+    const int B = (opt && opt->batch > 1) ? opt->batch : 1;
+    const size_t bs = B > 1 ? ((std::max(gb1, db1) + 255) & ~(size_t)255) : 0;
+    if (B > 1 && (!opt->states || !opt->acc || cfg->method == MITOS_METHOD_MONGE_AMPERE || !aligned ||
+                  (res && res->pos))) {
+        set_error(3, "batched runs need device start states and accumulators, a lattice-aligned "
+                     "Zel'dovich or 2LPT configuration and no positions");
+        return 3;
+    }
+    const size_t gb = B > 1 ? B * bs : gb1, db = B > 1 ? B * bs : db1;
+    const int acc_stride = 3 * cfg->pk_bins + 2;
+    auto reset = [&](PassArgs &x) {
+        memset(&x, 0, sizeof x);
+        x.batch = B;
+        x.bstride = (long long)bs;
+        x.acc_stride = acc_stride;
+    };
     StageTimer tim(getenv("MITOS_PROFILE") != nullptr);
     tim.mark();
 
     void *phi = workspace(gb, 0), *S = workspace(gb, 10), *Sk = workspace(gb, 11), *rho = workspace(gb, 12);
     void *A0 = workspace(gb, 1), *A1 = workspace(gb, 2);
     void *B0 = workspace(gb, 4), *B1 = workspace(gb, 5), *B2 = workspace(gb, 6);
-    // displacement grids: row pitch N + 4 on the lattice-aligned path (16-byte aligned rows for
-    // the staged tile copies of the deposit), the reference's N + 2 otherwise
-    const bool aligned = lattice_aligned(N, M, L);
-    const int disp_pitch = aligned ? N + 4 : N + 2;
-    const size_t db = (size_t)N * N * disp_pitch * sizeof(T);
     void *D0 = workspace(db, 7), *D1 = workspace(db, 8), *D2 = workspace(db, 9);
     if (!phi || !S || !Sk || !rho || !A0 || !A1 || !B0 || !B1 || !B2 || !D0 || !D1 || !D2) return 5;
     const long n2max = 3L * (N / 2) * (N / 2);
     T *filt = (T *)workspace(sizeof(T) * (n2max + 1), 106);
-    double *dtab = (double *)workspace(sizeof(double) * 3 * k_size, 107);
-    double *acc = (opt && opt->acc) ? opt->acc
-                                    : (double *)workspace(sizeof(double) * 3 * (size_t)cfg->pk_bins + 2 * sizeof(double), 104);
+    double *dtab = (opt && opt->dtab) ? opt->dtab : (double *)workspace(sizeof(double) * 3 * k_size, 107);
+    double *acc = (opt && opt->acc) ? opt->acc : (double *)workspace(sizeof(double) * acc_stride, 104);
     if (!filt || !dtab || !acc) return 5;
     double *red = acc + 3 * cfg->pk_bins;
 
@@ -184,21 +214,11 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
 
     // S1: noise (src/mitos.c:148,220-224 + generatePerturbationGrid)
     uint64_t st[4];
-    {
-        // splitmix64 seeding (include/random_xorshift.h:38-59) of Seed + rank 0
-        uint64_t s = cfg->seed;
-        for (int i = 0; i < 4; i++) {
-            uint64_t r = s;
-            s = r + 0x9E3779B97f4A7C15ULL;
-            r = (r ^ (r >> 30)) * 0xBF58476D1CE4E5B9ULL;
-            r = (r ^ (r >> 27)) * 0x94D049BB133111EBULL;
-            st[i] = r ^ (r >> 31);
-        }
-    }
+    seed_state(cfg->seed, st);
     int e;
     void *dens_k = ma ? Sk : phi;  // Monge-Ampere keeps delta(k) to build rho(x)
-    e = noise_generate(g, prec, L, st, filt, dens_k);
-    if (!e) e = hermitian_planes(g, prec, dens_k);
+    e = noise_generate(g, prec, L, st, filt, dens_k, B > 1 ? opt->states : nullptr, B, bs);
+    if (!e) e = hermitian_planes(g, prec, dens_k, B, bs);
     if (e) return e;
     tim.mark();
 
@@ -209,11 +229,11 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     double last_rel = 0;
     if (cfg->method == MITOS_METHOD_2LPT) {
         // S2: Hessians + source
-        e = grid_hessian(g, prec, L, phi, ZOP_HESS_2LPT, nullptr, S, nullptr, 0);
+        e = grid_hessian(g, prec, L, phi, ZOP_HESS_2LPT, nullptr, S, nullptr, 0, nullptr, B, bs);
         if (e) return e;
         tim.mark();
         // S3: S r2c -> phi = f1 phi1 + f2 (-1/k^2) S, TSC window undone (src/2lpt.c:125-136)
-        memset(&a, 0, sizeof a);
+        reset(a);
         a.dk = dk;
         a.scale = 1.0;
         a.in[0] = S;
@@ -254,7 +274,7 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
             MITOS_CUDA(cudaMemsetAsync(red, 0, 2 * sizeof(double), stream()));
             e = grid_hessian(g, prec, L, phi, ZOP_HESS_MA, rhoR, S, red, 0);
             if (e) return e;
-            memset(&a, 0, sizeof a);
+            reset(a);
             a.dk = dk;
             a.scale = 1.0;
             a.in[0] = S;
@@ -283,7 +303,7 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     }
 
     // S4: displacement grids d_i = c2r(i k_i phi W^-3) (src/mitos.c:395-416)
-    memset(&a, 0, sizeof a);
+    reset(a);
     a.dk = dk;
     a.scale = 1.0;
     a.window_order = win_disp;
@@ -327,11 +347,11 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     }
     // the aligned deposit uses a row pitch of N + 4 reals (16-byte aligned rows for vector reductions)
     const int rho_pitch = aligned ? N + 4 : N + 2;
-    const size_t rho_bytes = (size_t)N * N * rho_pitch * (sizeof(T));
+    const size_t rho_bytes = B > 1 ? db : (size_t)N * N * rho_pitch * (sizeof(T));
     void *rhoD = aligned ? workspace(rho_bytes, 15) : rho;
     if (!rhoD) return 5;
     MITOS_CUDA(cudaMemsetAsync(rhoD, 0, rho_bytes, stream()));
-    e = aligned ? lattice_deposit(N, L, prec, D0, D1, D2, disp_pitch, rhoD, rho_pitch, dpos)
+    e = aligned ? lattice_deposit(N, L, prec, D0, D1, D2, disp_pitch, rhoD, rho_pitch, dpos, B, bs)
                 : displace_and_deposit(N, M, L, prec, D0, D1, D2, rhoD, dpos);
     if (e) return e;
     if (dpos) {
@@ -345,8 +365,8 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     // S6: overdensity r2c, CIC window undo, P(k) (analyse/src/mitos_read.c:364-419)
     const int *bins = bin_table(N, cfg->pk_bins, cfg->pk_linear, L);
     if (!bins) return 5;
-    MITOS_CUDA(cudaMemsetAsync(acc, 0, sizeof(double) * 3 * cfg->pk_bins, stream()));
-    memset(&a, 0, sizeof a);
+    MITOS_CUDA(cudaMemsetAsync(acc, 0, sizeof(double) * ((size_t)(B - 1) * acc_stride + 3 * cfg->pk_bins), stream()));
+    reset(a);
     a.dk = dk;
     a.scale = 1.0;
     a.in[0] = rhoD;

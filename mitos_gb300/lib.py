@@ -473,12 +473,14 @@ def manet_training_pair(pot, dens, work, cycles: int, delta, phi1, phi2, sigma) 
 class Ensemble:
     """ic_ensemble_create / run / result / destroy over a list of ICConfig"""
 
-    def __init__(self, cfgs, spline: Spline, streams: int = 8):
+    def __init__(self, cfgs, spline: Spline, streams: int = 8, max_batch: int = 0):
+        """max_batch: realisations per batched unit (1: none; 0: the library's default)"""
         self.n = len(cfgs)
         self.cfgs = (ICConfig * self.n)(*cfgs)
         self.spline = spline
         self.h = ctypes.c_void_p()
-        _check(load().ic_ensemble_create(ctypes.byref(self.h), self.cfgs, self.n, ctypes.byref(spline.sp), streams))
+        _check(load().ic_ensemble_create_batched(ctypes.byref(self.h), self.cfgs, self.n, ctypes.byref(spline.sp),
+                                                 streams, max_batch))
 
     def run(self) -> float:
         ms = ctypes.c_double(0)
@@ -487,6 +489,9 @@ class Ensemble:
 
     def launches(self) -> int:
         return load().ic_ensemble_launches(self.h)
+
+    def units(self) -> int:
+        return load().ic_ensemble_units(self.h)
 
     def result(self, i: int) -> dict:
         bins = self.cfgs[i].pk_bins

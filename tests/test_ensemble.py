@@ -29,7 +29,9 @@ def test_graph_replay_matches_single_runs(table, spline):
     try:
         ens.run()
         ms = ens.run()
-        assert ms > 0 and ens.launches() >= 14 * len(cfgs)
+        # the members of each size form one batched unit: 14 launches or more per unit
+        assert ens.units() == len(SIZES)
+        assert ms > 0 and ens.launches() >= 14 * ens.units()
         for i, c in enumerate(cfgs):
             ref = ml.ic_pipeline_run(c, spline)
             got = ens.result(i)
@@ -39,6 +41,33 @@ def test_graph_replay_matches_single_runs(table, spline):
             assert np.allclose(got["pk_p"], ref["pk_p"], rtol=1e-5, atol=0, equal_nan=True), i
     finally:
         ens.close()
+
+
+@pytest.mark.parametrize("max_batch", [1, 3])
+def test_batched_units_match_unbatched_runs(table, spline, max_batch):
+    """members interleaved across sizes and seeds; batches of 1 (every member its own run) and 3
+    (ragged units of 3 + 1 + ...) give the P(k) of the default batching"""
+    base = _cfgs(table, 4, seed0=77)
+    cfgs = base[::2] + base[1::2]  # interleave: members of one size are not adjacent
+    ref = ml.Ensemble(cfgs, spline, streams=3)
+    ens = ml.Ensemble(cfgs, spline, streams=5, max_batch=max_batch)
+    try:
+        ref.run()
+        ens.run()
+        per = 4
+        want_units = len(SIZES) * (per if max_batch == 1 else -(-per // max_batch))
+        assert ens.units() == want_units and ref.units() == len(SIZES)
+        for i in range(len(cfgs)):
+            a, b = ens.result(i), ref.result(i)
+            assert np.array_equal(a["pk_obs"], b["pk_obs"])
+            assert np.allclose(a["pk_p"], b["pk_p"], rtol=1e-5, atol=0, equal_nan=True), i
+        # distinct seeds give distinct spectra (no member reads another's grids)
+        p = [ens.result(i)["pk_p"][1:] for i in range(len(cfgs))]
+        assert all(not np.allclose(p[i], p[j]) for i in range(len(p)) for j in range(i)
+                   if cfgs[i].N == cfgs[j].N)
+    finally:
+        ens.close()
+        ref.close()
 
 
 def test_autotuner_keeps_results(table, spline):
