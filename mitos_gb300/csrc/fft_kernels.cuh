@@ -24,8 +24,14 @@ template <int AXIS, int OP, int NL> constexpr bool strided_heavy() {
     return NL > 0 && AXIS == 1 && (OP == YOP_HESS || OP == YOP_DISP);
 }
 
+// The Hessian X pass of the compile-time lengths runs one 512-thread block per SM with up to 128
+// registers (at 64 it spills 216 bytes a thread; measured at 512^3: 0.70 ms against 0.85).
+template <int AXIS, int OP, int NL> constexpr int strided_min_blocks() {
+    return (NL > 0 && AXIS == 0 && OP == XOP_HESS) ? 1 : 2;
+}
+
 template <typename T, int E, int SIGN, int AXIS, int OP, int NL, int PC>
-__global__ void __launch_bounds__(strided_heavy<AXIS, OP, NL>() ? 256 : 512, 2) k_strided(GridGeom g, PassArgs a, const T *__restrict__ win) {
+__global__ void __launch_bounds__(strided_heavy<AXIS, OP, NL>() ? 256 : 512, strided_min_blocks<AXIS, OP, NL>()) k_strided(GridGeom g, PassArgs a, const T *__restrict__ win) {
     extern __shared__ __align__(16) unsigned char smraw[];
     cplx<T> *sm = reinterpret_cast<cplx<T> *>(smraw);
     const FFTPlan &pl = g.plN;
@@ -55,8 +61,8 @@ __global__ void __launch_bounds__(strided_heavy<AXIS, OP, NL>() ? 256 : 512, 2) 
         iz = kz;
     }
     const cplx<T> *tw = reinterpret_cast<const cplx<T> *>(g.twN);
-    const T dk = (T)a.dk;
-    const T scale = (T)a.scale;
+    const T dk = parg<T>(a.dk, a.fdk);
+    const T scale = parg<T>(a.scale, a.fscale);
     cplx<T> *psm = sm + p;
     const size_t bo = (size_t)blockIdx.y * (size_t)a.bstride;  // realisation of a batched launch
 
@@ -138,22 +144,22 @@ __global__ void __launch_bounds__(strided_heavy<AXIS, OP, NL>() ? 256 : 512, 2) 
                         if (win) r = cscale<T>(r, win[jx + N / 2] * win[iy + N / 2] * win[iz + N / 2]);
                         const int bin = valid ? a.bin_of_n2[n2] : -1;
                         const T mult = (iz == 0 || iz == N / 2) ? (T)1 : (T)2;
-                        const T pw = mult * (r.x * r.x + r.y * r.y);
-                        // per distinct bin of the warp: a butterfly sum, added by one lane into
-                        // the warp's own histogram (no atomics: no other warp writes it)
+                        T pw = valid ? mult * (r.x * r.x + r.y * r.y) : (T)0;
+                        // runs of equal bins in lane order (the lanes of a warp hold consecutive
+                        // x indices of a pencil, so a bin covers a run of lanes): a segmented
+                        // inclusive scan over the run, whose last lane adds the run's sum to the
+                        // warp's histogram (shared atomics: two runs of one warp may share a bin)
                         const int lane = threadIdx.x & 31;
-                        unsigned todo = __ballot_sync(0xffffffffu, bin >= 0);
-                        while (todo) {
-                            const int leader = __ffs(todo) - 1;
-                            const int b0 = __shfl_sync(0xffffffffu, bin, leader);
-                            const bool in = bin == b0 && ((todo >> lane) & 1u);
-                            T sum = in ? pw : (T)0;
+                        const int prev = __shfl_up_sync(0xffffffffu, bin, 1);
+                        const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || prev != bin);
+                        const int start = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
 #pragma unroll
-                            for (int off = 16; off > 0; off >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, off);
-                            if (lane == leader) hp[b0] += sum;
-                            todo &= ~__ballot_sync(0xffffffffu, in);
+                        for (int off = 1; off < 32; off <<= 1) {
+                            const T y = __shfl_up_sync(0xffffffffu, pw, off);
+                            if (lane - off >= start) pw += y;
                         }
-                        __syncwarp();  // a later leader of the same bin may be another lane
+                        const bool last = lane == 31 || ((heads >> (lane + 1)) & 1u);
+                        if (last && bin >= 0) atomicAdd(hp + bin, pw);
                         if (valid && a.out[0]) dst[idx] = r;
                     } else {
                         const T kk2 = (T)n2 * dk * dk;
@@ -161,7 +167,7 @@ __global__ void __launch_bounds__(strided_heavy<AXIS, OP, NL>() ? 256 : 512, 2) 
                         const cplx<T> q = bat<const cplx<T>>(a.in2, bo)[idx];
                         cplx<T> o;
                         if constexpr (OP == XOP_COMBINE_2LPT) {
-                            const T f1 = (T)a.f1, f2 = (T)a.f2;
+                            const T f1 = parg<T>(a.f1, a.ff1), f2 = parg<T>(a.f2, a.ff2);
                             o = mk<T>(f1 * q.x + f2 * G * r.x, f1 * q.y + f2 * G * r.y);
                         } else {
                             o = mk<T>(q.x + G * r.x, q.y + G * r.y);
@@ -180,10 +186,12 @@ __global__ void __launch_bounds__(strided_heavy<AXIS, OP, NL>() ? 256 : 512, 2) 
         const size_t off = (size_t)P * spad_len(N) * sizeof(cplx<T>);
         const T *hist = reinterpret_cast<const T *>(smraw + off);
         const int nw = blockDim.x >> 5;
+        // the warps' histograms summed in the kernel's precision (one FP64 conversion and atomic
+        // per bin and block: FP64 arithmetic runs at a small fraction of the FP32 rate)
         for (int i = tid; i < a.nbins; i += blockDim.x) {
-            double sum = 0;
-            for (int w = 0; w < nw; w++) sum += (double)hist[w * a.nbins + i];
-            if (sum != 0) atomicAdd(a.bin_p + (size_t)blockIdx.y * a.acc_stride + i, sum);
+            T sum = 0;
+            for (int w = 0; w < nw; w++) sum += hist[w * a.nbins + i];
+            if (sum != (T)0) atomicAdd(a.bin_p + (size_t)blockIdx.y * a.acc_stride + i, (double)sum);
         }
     }
 }
@@ -207,7 +215,8 @@ __global__ void __launch_bounds__(512, 2) k_x_combine_disp(GridGeom g, PassArgs 
     if (!valid) col = 0;
     const int iy = kint((int)(col / H), N), iz = (int)(col % H);
     const cplx<T> *tw = reinterpret_cast<const cplx<T> *>(g.twN);
-    const T dk = (T)a.dk, scale = (T)a.scale, f1 = (T)a.f1, f2 = (T)a.f2;
+    const T dk = parg<T>(a.dk, a.fdk), scale = parg<T>(a.scale, a.fscale), f1 = parg<T>(a.f1, a.ff1),
+            f2 = parg<T>(a.f2, a.ff2);
     const T *stn = reinterpret_cast<const T *>(a.stencil);
     cplx<T> *psm = sm + p;
     const size_t bo = (size_t)blockIdx.y * (size_t)a.bstride;
@@ -272,22 +281,23 @@ __global__ void __launch_bounds__(256, OP == ZOP_HESS_MA ? 1 : 2) k_z_c2r(GridGe
     const bool valid = row < (long)N * N;
     if (!valid) row = 0;
     const cplx<T> *tw = reinterpret_cast<const cplx<T> *>(g.twN);
-    const T dk = (T)a.dk;
-    const T scale = (T)a.scale;
+    // the 2LPT source pass converts the double copies: its 128-register allocation then keeps the
+    // transforms free of spills (measured at 512^3: 1.29 ms, against 1.42 with the FP32 copies)
+    const T dk = OP == ZOP_HESS_2LPT ? (T)a.dk : parg<T>(a.dk, a.fdk);
+    const T scale = OP == ZOP_HESS_2LPT ? (T)a.scale : parg<T>(a.scale, a.fscale);
     cplx<T> *psm = sm + (long)p * spad_len(h);
     const size_t bo = (size_t)blockIdx.y * (size_t)a.bstride;
 
     constexpr int NIN = (OP == ZOP_C2R) ? 1 : (OP == ZOP_DISP) ? 3 : 6;
     // inputs of the Hessian passes are [xx, xy, xz, yy, yz, zz]; the 2LPT source is accumulated
     // in the reference's term order (src/2lpt.c:111-112): zz yy + zz xx + yy xx - xy^2 - yz^2 - xz^2
-    constexpr int ORDER_2LPT[6] = {0, 3, 5, 1, 4, 2};
     constexpr int NKEEP = (OP == ZOP_HESS_MA) ? 6 : (OP == ZOP_HESS_2LPT) ? 2 : 1;
     cplx<T> o[NKEEP][E];
     cplx<T> acc[E];
     T *dst_row = nullptr;
 #pragma unroll
     for (int q = 0; q < NIN; q++) {
-        const int f = (OP == ZOP_HESS_2LPT) ? ORDER_2LPT[q] : q;
+        const int f = (OP == ZOP_HESS_2LPT) ? (q == 0 ? 0 : q == 1 ? 3 : q == 2 ? 5 : q == 3 ? 1 : q == 4 ? 4 : 2) : q;
         // kz factor of input f: 0 -> 1, 1 -> i kz, 2 -> -kz^2
         int fac = 0;
         if (OP == ZOP_HESS_2LPT || OP == ZOP_HESS_MA) fac = (f == 2 || f == 4) ? 1 : (f == 5 ? 2 : 0);
@@ -421,7 +431,7 @@ __global__ void __launch_bounds__(256) k_z_r2c(GridGeom g, PassArgs a) {
     if (!valid) row = 0;
     const cplx<T> *tw = reinterpret_cast<const cplx<T> *>(g.twN);
     cplx<T> *psm = sm + (long)p * spad_len(h);
-    const T ra = (T)a.rho_a, rb = (T)a.rho_b;
+    const T ra = parg<T>(a.rho_a, a.frho_a), rb = parg<T>(a.rho_b, a.frho_b);
     const size_t bo = (size_t)blockIdx.y * (size_t)a.bstride;
     const T *src = bat<const T>(a.in[0], bo) + row * a.rp_in;
     cplx<T> v[E];
@@ -429,7 +439,7 @@ __global__ void __launch_bounds__(256) k_z_r2c(GridGeom g, PassArgs a) {
     for (int e = 0; e < E; e++) {
         const int n = nin_any<NL, E>(pl, t, e);
         cplx<T> z = *reinterpret_cast<const cplx<T> *>(src + 2 * n);
-        if (a.rho_a != 1.0 || a.rho_b != 0.0) z = mk<T>(z.x * ra + rb, z.y * ra + rb);
+        if (ra != (T)1 || rb != (T)0) z = mk<T>(z.x * ra + rb, z.y * ra + rb);
         v[e] = z;
     }
     fft_any<T, E, -1, NL, 1>(pl, v, psm, 1, t, tw);
@@ -452,6 +462,7 @@ __global__ void __launch_bounds__(256) k_z_r2c(GridGeom g, PassArgs a) {
 // ------------------------------------------------------------------------------------------
 // launchers (NL = 0: runtime plan; NL > 0: the compile-time specialisation for that length)
 // ------------------------------------------------------------------------------------------
+
 template <typename T, int E, int SIGN, int AXIS, int OP, int NL, int PC>
 static int launch_strided_e(const GridGeom &g, const PassArgs &a, const T *win) {
     const int P = PC > 0 ? PC : g.P_xy;
@@ -463,7 +474,7 @@ static int launch_strided_e(const GridGeom &g, const PassArgs &a, const T *win) 
     if (smem > 48 * 1024) MITOS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     launch_begin(AXIS == 0 ? (OP == XOP_HESS ? "x_hess" : OP == XOP_DISP ? "x_disp" : OP == XOP_COMBINE_2LPT ? "x_combine" : OP == XOP_ADD_POISSON ? "x_add_poisson" : OP == XOP_PK ? "x_pk" : "x_plain")
                         : (OP == YOP_HESS ? "y_hess" : OP == YOP_DISP ? "y_disp" : "y_plain"));
-    kern<<<dim3((unsigned)blocks, a.batch > 1 ? a.batch : 1), threads, smem, stream()>>>(g, a, win);
+    kern<<<dim3((unsigned)blocks, a.batch > 1 ? a.batch : 1), threads, smem, stream()>>>(g, with_f32(a), win);
     count_launch();
     MITOS_LAUNCH_CHECK("strided FFT pass");
     return 0;
@@ -503,11 +514,11 @@ int launch_x_t(const GridGeom &g, XOp op, int sign, const PassArgs &a) {
         if (NL > 0 || g.E == 8) {
             auto kern = k_x_combine_disp<T, 8, NL, PC>;
             if (smem > 48 * 1024) MITOS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            kern<<<dim3((unsigned)blocks, a.batch > 1 ? a.batch : 1), threads, smem, stream()>>>(g, a, win);
+            kern<<<dim3((unsigned)blocks, a.batch > 1 ? a.batch : 1), threads, smem, stream()>>>(g, with_f32(a), win);
         } else {
             auto kern = k_x_combine_disp<T, 12, 0, 0>;
             if (smem > 48 * 1024) MITOS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            kern<<<dim3((unsigned)blocks, a.batch > 1 ? a.batch : 1), threads, smem, stream()>>>(g, a, win);
+            kern<<<dim3((unsigned)blocks, a.batch > 1 ? a.batch : 1), threads, smem, stream()>>>(g, with_f32(a), win);
         }
         count_launch();
         MITOS_LAUNCH_CHECK("x combine + displacement pass");
@@ -540,7 +551,7 @@ static int launch_zc_e(const GridGeom &g, const PassArgs &a) {
     auto kern = k_z_c2r<T, E, OP, NLZ>;
     if (smem > 48 * 1024) MITOS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     launch_begin(OP == ZOP_C2R ? "z_c2r" : OP == ZOP_HESS_2LPT ? "z_hess_2lpt" : OP == ZOP_HESS_MA ? "z_hess_ma" : "z_disp");
-    kern<<<dim3((unsigned)((rows + P - 1) / P), a.batch > 1 ? a.batch : 1), threads, smem, stream()>>>(g, a);
+    kern<<<dim3((unsigned)((rows + P - 1) / P), a.batch > 1 ? a.batch : 1), threads, smem, stream()>>>(g, with_f32(a));
     count_launch();
     MITOS_LAUNCH_CHECK("z c2r pass");
     return 0;
@@ -576,7 +587,7 @@ static int launch_zr_e(const GridGeom &g, const PassArgs &a) {
     auto kern = k_z_r2c<T, E, NLZ>;
     if (smem > 48 * 1024) MITOS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     launch_begin("z_r2c");
-    kern<<<dim3((unsigned)((rows + P - 1) / P), a.batch > 1 ? a.batch : 1), P * tpp, smem, stream()>>>(g, a);
+    kern<<<dim3((unsigned)((rows + P - 1) / P), a.batch > 1 ? a.batch : 1), P * tpp, smem, stream()>>>(g, with_f32(a));
     count_launch();
     MITOS_LAUNCH_CHECK("z r2c pass");
     return 0;

@@ -76,7 +76,26 @@ struct PassArgs {
     int batch;            // 0 or 1: one realisation
     long long bstride;
     int acc_stride;
+    // FP32 copies of scale, dk, f1, f2, rho_a, rho_b, filled at launch (with_f32): the FP32
+    // kernels read these, as a double -> float conversion per thread runs on the FP64 pipe
+    float fscale, fdk, ff1, ff2, frho_a, frho_b;
 };
+
+// the kernel's copy of a with the FP32 scalars filled
+inline PassArgs with_f32(const PassArgs &a) {
+    PassArgs b = a;
+    b.fscale = (float)a.scale;
+    b.fdk = (float)a.dk;
+    b.ff1 = (float)a.f1;
+    b.ff2 = (float)a.f2;
+    b.frho_a = (float)a.rho_a;
+    b.frho_b = (float)a.rho_b;
+    return b;
+}
+// a scalar of PassArgs in the kernel's precision
+template <typename T> __device__ __forceinline__ T parg(double d, float f);
+template <> __device__ __forceinline__ float parg<float>(double, float f) { return f; }
+template <> __device__ __forceinline__ double parg<double>(double d, float) { return d; }
 
 // pointer p shifted by bo bytes (null stays null)
 template <typename P> __host__ __device__ __forceinline__ P *bat(const void *p, size_t bo) {

@@ -237,10 +237,17 @@ __device__ __forceinline__ double gauss64(uint64_t A, uint64_t B) {
 // ~A), t in (0, 1/2]; ln u = ln t for u < 1/2 (|ln t| >= ln 2, so the hardware log2 keeps full
 // relative precision) and ln u = ln(1 - t) = -2 atanh(s), s = t / (2 - t) <= 1/3, for u >= 1/2
 // (the atanh series through s^15; the next term is below 4e-9 relative)
+//
+// No 64-bit integer -> float conversions (they run on the FP64 pipe, a small fraction of the FP32
+// rate on this part): the uniform is hi 2^32 + lo from the two 32-bit halves (one FMA: within an
+// ulp of the rounded 64-bit value, 2^-24 relative at every magnitude), the cosine argument the
+// top 32 bits (absolute error below 2^-32).
 __device__ __forceinline__ float gauss32(uint64_t A, uint64_t B) {
     const float inv64 = 5.42101086242752217e-20f;  // 2^-64
     const bool hi = (A >> 63) != 0;
-    const float t = (__ull2float_rn(hi ? ~A : A) + 0.5f) * inv64;
+    const uint64_t a = hi ? ~A : A;
+    const float af = fmaf((float)(unsigned)(a >> 32), 4294967296.f, (float)(unsigned)a);
+    const float t = (af + 0.5f) * inv64;
     const float s = __fdividef(t, 2.f - t), s2 = s * s;
     float p = 1.f / 15.f;
     p = fmaf(p, s2, 1.f / 13.f);
@@ -253,7 +260,7 @@ __device__ __forceinline__ float gauss32(uint64_t A, uint64_t B) {
     const float lnu = hi ? -2.f * s * p : __logf(t);
     const float x = -2.f * lnu;  // > 0
     // cos(2 pi v) = -cos(2 pi (v - 1/2)), argument in (-pi, pi) for the hardware cosine
-    const float w = ((float)(long long)(B - 0x8000000000000000ULL) + 0.5f) * inv64;
+    const float w = ((float)(int)((unsigned)(B >> 32) ^ 0x80000000u) + 0.5f) * 2.3283064365386963e-10f;  // 2^-32
     return -(x * rsqrtf(x)) * __cosf(6.28318530717958647692f * w);
 }
 

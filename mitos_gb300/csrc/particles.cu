@@ -23,12 +23,34 @@ template <typename T> __device__ __forceinline__ int ifloor(T x);
 template <> __device__ __forceinline__ int ifloor<float>(float x) { return __float2int_rd(x); }
 template <> __device__ __forceinline__ int ifloor<double>(double x) { return __double2int_rd(x); }
 
+// floor of x as an int and as a real.  FP32: one round-down add of 1.5 * 2^23 (the sum's unit bit
+// is floor(x)'s for |x| < 2^22; the lattice path's grid coordinates stay far inside that), which
+// replaces a float -> int and an int -> float conversion (quarter-rate or slower) by full-rate
+// adds; identical results to __float2int_rd and its cast back.
+template <typename T> __device__ __forceinline__ int floor_split(T x, T &f);
+template <> __device__ __forceinline__ int floor_split<float>(float x, float &f) {
+    const float m = __fadd_rd(x, 12582912.f);
+    f = m - 12582912.f;
+    return __float_as_int(m) - 0x4B400000;
+}
+template <> __device__ __forceinline__ int floor_split<double>(double x, double &f) {
+    const int i = __double2int_rd(x);
+    f = (double)i;
+    return i;
+}
+// (float)i for 0 <= i < 2^23, without a conversion
+__device__ __forceinline__ float small_int_to_float(int i) { return __int_as_float(0x4B000000 + i) - 8388608.f; }
+
 // CIC region accumulators: 32-bit fixed point with 2^23 per mean density in FP32 (native
 // integer shared atomics; exact, order independent), doubles in FP64
 template <typename T> struct RegAcc;
 template <> struct RegAcc<float> {
     using type = unsigned int;
-    static __device__ __forceinline__ void add(unsigned int *c, float w) { atomicAdd(c, (unsigned int)__float2uint_rn(w * 8388608.f)); }
+    // w in [0, 1]: round-to-nearest-even of w 2^23 as the low bits of w 2^23 + 2^23 (one FMA; the
+    // same integer as __float2uint_rn(w * 2^23), without the conversion)
+    static __device__ __forceinline__ void add(unsigned int *c, float w) {
+        atomicAdd(c, __float_as_uint(fmaf(w, 8388608.f, 8388608.f)) - 0x4B000000u);
+    }
     static __device__ __forceinline__ float value(unsigned int c) { return (float)c * (1.f / 8388608.f); }
 };
 template <> struct RegAcc<double> {
@@ -302,26 +324,30 @@ k_lattice_cic(int N, int rpd, int rpo, float spacing, float Lf, T ginv, const T 
         for (int rep = 0; rep < (LB_X * LB_Y * LB_Z) / LB_THREADS; rep++) {
             const int lx = lxb + rep * (LB_THREADS / (LB_Z * LB_Y));
             const int x = x0 + lx, y = y0 + ly, z = z0 + lz;
-            float p0 = x * spacing, p1 = y * spacing, p2 = z * spacing;  // src/particle.c:114-116
+            // src/particle.c:114-116
+            float p0 = small_int_to_float(x) * spacing, p1 = small_int_to_float(y) * spacing,
+                  p2 = small_int_to_float(z) * spacing;
             // direction 0: on nodes (stencil folded into d0)
             p0 = (float)((T)p0 - t0[(lx * LB_Y + ly) * LB_Z + lz]);
             // direction 1: x off node (src/grids_interp.c:269-306), y and z on nodes (folded into d1)
             const T Xg = (T)p0 * ginv;
-            const int nx = ifloor<T>(Xg + (T)0.5);
+            T fnx;
+            const int nx = floor_split<T>(Xg + (T)0.5, fnx);
             const int ix = nx - 1 - (x0 - TH);  // tile x index of the first stencil node
             bool tiled = ix >= 0 && ix + 2 < T1X;
             T wx[3], wy[3];
             if (tiled) {
-                tsc_w<T>(Xg - (T)nx, wx);
+                tsc_w<T>(Xg - fnx, wx);
                 const T *r1 = t1 + (ix * LB_Y + ly) * LB_Z + lz;
                 p1 = (float)((T)p1 - (wx[0] * r1[0] + wx[1] * r1[LB_Y * LB_Z] + wx[2] * r1[2 * LB_Y * LB_Z]));
                 // direction 2: x and y off nodes, z on nodes (folded into d2)
                 const T Yg = (T)p1 * ginv;
-                const int ny = ifloor<T>(Yg + (T)0.5);
+                T fny;
+                const int ny = floor_split<T>(Yg + (T)0.5, fny);
                 const int iy = ny - 1 - (y0 - TH);
                 tiled = iy >= 0 && iy + 2 < T2Y;
                 if (tiled) {
-                    tsc_w<T>(Yg - (T)ny, wy);
+                    tsc_w<T>(Yg - fny, wy);
                     T sv = 0;
 #pragma unroll
                     for (int i = 0; i < 3; i++) {
@@ -348,9 +374,14 @@ k_lattice_cic(int N, int rpd, int rpo, float spacing, float Lf, T ginv, const T 
             }
             // CIC (analyse/src/mitos_read.c:288-333), one unit of mean density per particle (M = N)
             const T X = (T)p0 * ginv, Y = (T)p1 * ginv, Z = (T)p2 * ginv;
-            const int iX = ifloor<T>(X), iY = ifloor<T>(Y), iZ = ifloor<T>(Z);
-            const T dx = X - iX, dy = Y - iY, dz = Z - iZ;
-            const int rx = wrapn(iX - x0 + 1, N), ry = wrapn(iY - y0 + 1, N), rz = wrapn(iZ - z0 + LR_Z0, N);
+            T fX, fY, fZ;
+            const int iX = floor_split<T>(X, fX), iY = floor_split<T>(Y, fY), iZ = floor_split<T>(Z, fZ);
+            const T dx = X - fX, dy = Y - fY, dz = Z - fZ;
+            // region indices; the periodic wrap only for the bricks on the box faces
+            int rx = iX - x0 + 1, ry = iY - y0 + 1, rz = iZ - z0 + LR_Z0;
+            if ((unsigned)rx >= (unsigned)N) rx = wrapn(rx, N);
+            if ((unsigned)ry >= (unsigned)N) ry = wrapn(ry, N);
+            if ((unsigned)rz >= (unsigned)N) rz = wrapn(rz, N);
             if (rx < LR_X - 1 && ry < LR_Y - 1 && rz < LR_Z - 1) {
                 A *c = reg + (rx * LR_Y + ry) * LR_Z + rz;
                 const T tx = 1 - dx, ty = 1 - dy, tz = 1 - dz;
