@@ -9,8 +9,9 @@
 // xoshiro256** is linear over GF(2) on its 256-bit state, so the state after J steps is
 // q_J(A) s0, with A the one-step transition and q_J(x) = x^J mod p(x), p the characteristic
 // polynomial of A.  p is recovered once with Berlekamp-Massey from 512 output bits; the
-// polynomials of all column offsets are computed on the host (cached per N) and each thread
-// evaluates q_c(A) s0 by Horner's rule with 256 transition steps.
+// polynomials of all column offsets are computed on the host (cached per N); on the GPU each
+// block tabulates A^i s0 (i < 256) and a thread's start state q_c(A) s0 is the XOR of the entries
+// selected by the bits of q_c.  A thread then generates consecutive columns from that state.
 #include <math.h>
 #include <string.h>
 
@@ -271,7 +272,26 @@ template <> __device__ __forceinline__ double gauss<double>(uint64_t A, uint64_t
 #define NOISE_THREADS 128
 #define NOISE_CHUNK 16
 
-template <typename T>
+// Column start states.  A column's state is sum_i q_i A^i s0 over the bits q_i of its jump
+// polynomial (A: one xoshiro256** step, sums in GF(2)).  Each block tabulates A^i s0 for
+// i = 0..255 in shared memory once; a column's state is then the XOR of the entries its bits select
+// (a broadcast load and an and-xor per word and bit, against a full state step per bit for
+// Horner's rule).
+__device__ __forceinline__ void noise_state_table(const RngState &s0, ulonglong4 *tab) {
+    if (threadIdx.x == 0) {
+        uint64_t a0 = s0.s[0], a1 = s0.s[1], a2 = s0.s[2], a3 = s0.s[3];
+        for (int i = 0; i < 256; i++) {
+            tab[i] = make_ulonglong4(a0, a1, a2, a3);
+            dnext(a0, a1, a2, a3);
+        }
+    }
+    __syncthreads();
+}
+
+// One thread generates COLS consecutive columns (x, y) of the half-complex grid, z fastest: the
+// reference draws them in that order, so column c + 1 starts where column c ends and only the
+// first column of a thread needs a jump.  Values are staged per chunk of z and written as rows.
+template <typename T, int COLS>
 __global__ void __launch_bounds__(NOISE_THREADS)
 k_noise(int N, const uint64_t *__restrict__ polys, RngState s0, T factor, const T *__restrict__ filt,
         cplx<T> *__restrict__ out, const RngState *__restrict__ states, size_t ostride) {
@@ -281,76 +301,78 @@ k_noise(int N, const uint64_t *__restrict__ polys, RngState s0, T factor, const 
         out = bat<cplx<T>>(out, (size_t)blockIdx.y * ostride);
     }
     __shared__ cplx<T> stage[NOISE_THREADS][NOISE_CHUNK + 1];
+    __shared__ ulonglong4 tab[256];
+    noise_state_table(s0, tab);
     const int H = N / 2 + 1;
     const long ncol = (long)N * N;
-    const long c = (long)blockIdx.x * NOISE_THREADS + threadIdx.x;
-    const bool valid = c < ncol;
+    const long cblock = (long)blockIdx.x * NOISE_THREADS * COLS;  // first column of the block
+    const long c0 = cblock + (long)threadIdx.x * COLS;
+    const bool valid = c0 < ncol;
     uint64_t r0 = 0, r1 = 0, r2 = 0, r3 = 0;
-    int ky = 0, kx = 0;
     if (valid) {
-        const uint64_t q0 = polys[4 * c], q1 = polys[4 * c + 1], q2 = polys[4 * c + 2], q3 = polys[4 * c + 3];
-        // Horner: r = sum_i q_i A^i s0
-#pragma unroll 4
-        for (int i = 255; i >= 0; i--) {
-            const uint64_t t = r1 << 17;
-            r2 ^= r0;
-            r3 ^= r1;
-            r1 ^= r2;
-            r0 ^= r3;
-            r2 ^= t;
-            r3 = drotl(r3, 45);
-            const uint64_t w = (i >= 192) ? q3 : (i >= 128) ? q2 : (i >= 64) ? q1 : q0;
-            const uint64_t m = 0ULL - ((w >> (i & 63)) & 1ULL);
-            r0 ^= s0.s[0] & m;
-            r1 ^= s0.s[1] & m;
-            r2 ^= s0.s[2] & m;
-            r3 ^= s0.s[3] & m;
+#pragma unroll 1
+        for (int wq = 0; wq < 4; wq++) {
+            const unsigned long long w = polys[4 * c0 + wq];
+            const unsigned lo = (unsigned)w, hi = (unsigned)(w >> 32);
+#pragma unroll 8
+            for (int bit = 0; bit < 64; bit++) {
+                const unsigned m = 0u - (((bit < 32 ? lo : hi) >> (bit & 31)) & 1u);
+                const uint64_t mm = ((uint64_t)m << 32) | m;
+                const ulonglong4 e = tab[wq * 64 + bit];
+                r0 ^= e.x & mm;
+                r1 ^= e.y & mm;
+                r2 ^= e.z & mm;
+                r3 ^= e.w & mm;
+            }
         }
-        kx = kint((int)(c / N), N);
-        ky = kint((int)(c % N), N);
     }
-    const long rowbase0 = ((long)blockIdx.x * NOISE_THREADS) * H;
-    for (int z0 = 0; z0 < H; z0 += NOISE_CHUNK) {
-        const int cz = (H - z0) < NOISE_CHUNK ? (H - z0) : NOISE_CHUNK;
-        if (valid) {
-            for (int j = 0; j < cz; j++) {
-                const int z = z0 + j;
-                cplx<T> val = mk<T>(0, 0);
-                const int n2 = kx * kx + ky * ky + z * z;
-                if (n2 > 0) {
-                    const uint64_t A = dnext(r0, r1, r2, r3), B = dnext(r0, r1, r2, r3);
-                    const uint64_t C2 = dnext(r0, r1, r2, r3), D = dnext(r0, r1, r2, r3);
-                    T a = gauss<T>(A, B) * factor;
-                    T b = gauss<T>(C2, D) * factor;
-                    if (filt) {
-                        const T f = filt[n2];
-                        a *= f;
-                        b *= f;
+#pragma unroll 1
+    for (int k = 0; k < COLS; k++) {
+        const long c = c0 + k;
+        const int kx = valid ? kint((int)(c / N), N) : 0;
+        const int ky = valid ? kint((int)(c % N), N) : 0;
+        for (int z0 = 0; z0 < H; z0 += NOISE_CHUNK) {
+            const int cz = (H - z0) < NOISE_CHUNK ? (H - z0) : NOISE_CHUNK;
+            if (valid) {
+                for (int j = 0; j < cz; j++) {
+                    const int z = z0 + j;
+                    cplx<T> val = mk<T>(0, 0);
+                    const int n2 = kx * kx + ky * ky + z * z;
+                    if (n2 > 0) {
+                        const uint64_t A = dnext(r0, r1, r2, r3), B = dnext(r0, r1, r2, r3);
+                        const uint64_t C2 = dnext(r0, r1, r2, r3), D = dnext(r0, r1, r2, r3);
+                        T a = gauss<T>(A, B) * factor;
+                        T b = gauss<T>(C2, D) * factor;
+                        if (filt) {
+                            const T f = filt[n2];
+                            a *= f;
+                            b *= f;
+                        }
+                        val = mk<T>(a, b);
                     }
-                    val = mk<T>(a, b);
+                    stage[threadIdx.x][j] = val;
                 }
-                stage[threadIdx.x][j] = val;
             }
-        }
-        __syncthreads();
-        // coalesced write-out: the block's rows are contiguous in memory
-        if (cz == NOISE_CHUNK) {
-            static_assert((NOISE_CHUNK & (NOISE_CHUNK - 1)) == 0, "chunk is a power of two");
-            constexpr int SH = __builtin_ctz(NOISE_CHUNK);
+            __syncthreads();
+            // write-out: row of thread rr is column cblock + rr COLS + k
+            if (cz == NOISE_CHUNK) {
+                static_assert((NOISE_CHUNK & (NOISE_CHUNK - 1)) == 0, "chunk is a power of two");
+                constexpr int SH = __builtin_ctz(NOISE_CHUNK);
 #pragma unroll 4
-            for (int idx = threadIdx.x; idx < NOISE_THREADS * NOISE_CHUNK; idx += NOISE_THREADS) {
-                const int rr = idx >> SH, j = idx & (NOISE_CHUNK - 1);
-                if ((long)blockIdx.x * NOISE_THREADS + rr < ncol)
-                    out[rowbase0 + (long)rr * H + z0 + j] = stage[rr][j];
+                for (int idx = threadIdx.x; idx < NOISE_THREADS * NOISE_CHUNK; idx += NOISE_THREADS) {
+                    const int rr = idx >> SH, j = idx & (NOISE_CHUNK - 1);
+                    const long cc = cblock + (long)rr * COLS + k;
+                    if (cc < ncol) out[cc * H + z0 + j] = stage[rr][j];
+                }
+            } else {
+                for (int idx = threadIdx.x; idx < NOISE_THREADS * cz; idx += NOISE_THREADS) {
+                    const int rr = idx / cz, j = idx % cz;
+                    const long cc = cblock + (long)rr * COLS + k;
+                    if (cc < ncol) out[cc * H + z0 + j] = stage[rr][j];
+                }
             }
-        } else {
-            for (int idx = threadIdx.x; idx < NOISE_THREADS * cz; idx += NOISE_THREADS) {
-                const int rr = idx / cz, j = idx % cz;
-                if ((long)blockIdx.x * NOISE_THREADS + rr < ncol)
-                    out[rowbase0 + (long)rr * H + z0 + j] = stage[rr][j];
-            }
+            __syncthreads();
         }
-        __syncthreads();
     }
 }
 
@@ -386,16 +408,23 @@ int noise_generate(const GridGeom &g, int precision, double boxlen, uint64_t st[
     const double boxvol = boxlen * boxlen * boxlen;
     const double factor = sqrt(boxvol / 2);  // src/grf.c:33
     const long ncol = (long)g.N * g.N;
-    const unsigned blocks = (unsigned)((ncol + NOISE_THREADS - 1) / NOISE_THREADS);
-    const dim3 grid(blocks, states && batch > 1 ? batch : 1);
+    const int nb = states && batch > 1 ? batch : 1;
+    // two columns a thread when that still leaves 14 warps per SM (152 SMs) across the launch
+    // (384^3 and up); one otherwise
+    const int cols = (ncol * nb >= 2L * 152 * 448 && ncol % 2 == 0) ? 2 : 1;
+    const unsigned blocks = (unsigned)((ncol / cols + NOISE_THREADS - 1) / NOISE_THREADS);
+    const dim3 grid(blocks, nb);
     const RngState *sts = (const RngState *)states;
     launch_begin("noise");
-    if (precision == MITOS_FP32)
-        k_noise<float><<<grid, NOISE_THREADS, 0, stream()>>>(g.N, polys, s0, (float)factor,
-                                                             (const float *)filter_by_n2, (float2 *)fbox, sts, bstride);
-    else
-        k_noise<double><<<grid, NOISE_THREADS, 0, stream()>>>(g.N, polys, s0, factor,
-                                                              (const double *)filter_by_n2, (double2 *)fbox, sts, bstride);
+    if (precision == MITOS_FP32) {
+        auto kern = cols == 2 ? k_noise<float, 2> : k_noise<float, 1>;
+        kern<<<grid, NOISE_THREADS, 0, stream()>>>(g.N, polys, s0, (float)factor, (const float *)filter_by_n2,
+                                                   (float2 *)fbox, sts, bstride);
+    } else {
+        auto kern = cols == 2 ? k_noise<double, 2> : k_noise<double, 1>;
+        kern<<<grid, NOISE_THREADS, 0, stream()>>>(g.N, polys, s0, factor, (const double *)filter_by_n2,
+                                                   (double2 *)fbox, sts, bstride);
+    }
     count_launch();
     MITOS_LAUNCH_CHECK("noise");
     return 0;

@@ -235,6 +235,23 @@ __device__ __noinline__ void displace_global(int N, int rpd, T ginv, const T *d1
     p2 = (float)((T)p2 - sv);
 }
 
+// unsigned division n / d for n < 2^31 by a multiply-high and a shift (Granlund and Montgomery,
+// "Division by invariant integers using multiplication", 1994): m = floor(2^32 (2^s - d) / d) + 1
+// with s = ceil(log2 d), q = (umulhi(n, m) + n) >> s.  The brick decode of the persistent deposit
+// ran three runtime divisions per brick.
+struct FastDiv {
+    unsigned m;
+    int s;
+};
+static FastDiv make_fastdiv(unsigned d) {
+    FastDiv f;
+    f.s = 0;
+    while ((1u << f.s) < d) f.s++;
+    f.m = (unsigned)(((1ULL << 32) * ((1ULL << f.s) - d)) / d + 1);
+    return f;
+}
+__device__ __forceinline__ unsigned fdiv(unsigned n, FastDiv f) { return (__umulhi(n, f.m) + n) >> f.s; }
+
 // tiles of the brick: d0 on the brick, d1 with an x halo of 2, d2 with x and y halos of 2
 #define TH 2
 #define T1X (LB_X + 2 * TH)
@@ -280,7 +297,8 @@ __device__ __forceinline__ void stage_tiles(T *tiles, int N, int rpd, int x0, in
 template <typename T>
 __global__ void __launch_bounds__(LB_THREADS, 2)
 k_lattice_cic(int N, int rpd, int rpo, float spacing, float Lf, T ginv, const T *__restrict__ d0, const T *__restrict__ d1,
-              const T *__restrict__ d2, T *__restrict__ rho, float *__restrict__ pos_out, size_t bstride) {
+              const T *__restrict__ d2, T *__restrict__ rho, float *__restrict__ pos_out, size_t bstride, FastDiv div_bx,
+              FastDiv div_by) {
     // batched launches: realisation blockIdx.y (its grids bstride bytes apart)
     if (gridDim.y > 1) {
         const size_t bo = (size_t)blockIdx.y * bstride;
@@ -298,20 +316,30 @@ k_lattice_cic(int N, int rpd, int rpo, float spacing, float Lf, T ginv, const T 
     const int bx_n = N / LB_X, by_n = N / LB_Y;
     const int nbricks = bx_n * by_n * (N / LB_Z);
     for (int i = threadIdx.x; i < LR_X * LR_Y * LR_Z; i += LB_THREADS) reg[i] = 0;
+    // brick b -> (bx, by, bz), x fastest
+    auto decode = [&](int b, int &bx, int &by, int &bz) {
+        const int q = (int)fdiv((unsigned)b, div_bx);
+        bx = b - q * bx_n;
+        bz = (int)fdiv((unsigned)q, div_by);
+        by = q - bz * by_n;
+    };
     int b = blockIdx.x;
     if (b < nbricks) {
-        const int bx = b % bx_n, by = (b / bx_n) % by_n, bz = b / (bx_n * by_n);
+        int bx, by, bz;
+        decode(b, bx, by, bz);
         stage_tiles<T>(tbuf, N, rpd, bx * LB_X, by * LB_Y, bz * LB_Z, d0, d1, d2);
     }
     cp_async_commit();
     const int lz = threadIdx.x % LB_Z, ly = (threadIdx.x / LB_Z) % LB_Y, lxb = threadIdx.x / (LB_Z * LB_Y);
 #pragma unroll 1
     for (int buf = 0; b < nbricks; b += gridDim.x, buf ^= 1) {
-        const int bx = b % bx_n, by = (b / bx_n) % by_n, bz = b / (bx_n * by_n);
+        int bx, by, bz;
+        decode(b, bx, by, bz);
         const int x0 = bx * LB_X, y0 = by * LB_Y, z0 = bz * LB_Z;
         const int bn = b + gridDim.x;
         if (bn < nbricks) {
-            const int nx = bn % bx_n, ny = (bn / bx_n) % by_n, nz = bn / (bx_n * by_n);
+            int nx, ny, nz;
+            decode(bn, nx, ny, nz);
             stage_tiles<T>(tbuf + (buf ^ 1) * TILE_ELEMS, N, rpd, nx * LB_X, ny * LB_Y, nz * LB_Z, d0, d1, d2);
         }
         cp_async_commit();
@@ -451,7 +479,8 @@ static int lattice_launch(int N, int rpd, int rpo, float spacing, float Lf, doub
     const int nb = batch > 1 ? batch : 1;
     const unsigned blocks = (unsigned)std::max<long>(1, std::min<long>(nbricks, (long)sms * bps / nb));
     kern<<<dim3(blocks, nb), LB_THREADS, smem, stream()>>>(N, rpd, rpo, spacing, Lf, (T)ginv, (const T *)d0,
-                                                           (const T *)d1, (const T *)d2, (T *)rho, pos_out, bstride);
+                                                           (const T *)d1, (const T *)d2, (T *)rho, pos_out, bstride,
+                                                           make_fastdiv((unsigned)(N / LB_X)), make_fastdiv((unsigned)(N / LB_Y)));
     return 0;
 }
 
