@@ -139,7 +139,9 @@ __global__ void __launch_bounds__(strided_heavy<AXIS, OP, NL>() ? 256 : 512, str
                 if constexpr (AXIS == 0 && (OP == XOP_COMBINE_2LPT || OP == XOP_ADD_POISSON ||
                                             OP == XOP_PK)) {
                     const int jx = kint(n, N);
-                    const long n2 = (long)jx * jx + (long)iy * iy + (long)iz * iz;
+                    // |n|^2 <= 3 (N/2)^2 fits an int; a 64-bit integer -> float conversion would
+                    // run on the FP64 pipe
+                    const int n2 = jx * jx + iy * iy + iz * iz;
                     if constexpr (OP == XOP_PK) {
                         if (win) r = cscale<T>(r, win[jx + N / 2] * win[iy + N / 2] * win[iz + N / 2]);
                         const int bin = valid ? a.bin_of_n2[n2] : -1;
@@ -231,7 +233,7 @@ __global__ void __launch_bounds__(512, 2) k_x_combine_disp(GridGeom g, PassArgs 
     for (int e = 0; e < E; e++) {
         const int n = nout_any<NL, E>(pl, t, e);
         const int jx = kint(n, N);
-        const long n2 = (long)jx * jx + (long)iy * iy + (long)iz * iz;
+        const int n2 = jx * jx + iy * iy + iz * iz;  // int: see the strided X passes
         const T G = (n2 > 0) ? (T)-1 / ((T)n2 * dk * dk) : (T)1;
         const cplx<T> q = valid ? phi1[col + (long)n * g.plane] : mk<T>(0, 0);
         const cplx<T> r = cscale<T>(v[e], scale);

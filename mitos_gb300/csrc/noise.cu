@@ -11,7 +11,7 @@
 // polynomial of A.  p is recovered once with Berlekamp-Massey from 512 output bits; the
 // polynomials of all column offsets are computed on the host (cached per N); on the GPU each
 // block tabulates A^i s0 (i < 256) and a thread's start state q_c(A) s0 is the XOR of the entries
-// selected by the bits of q_c.  A thread then generates consecutive columns from that state.
+// selected by the bits of q_c.
 #include <math.h>
 #include <string.h>
 
@@ -288,10 +288,11 @@ __device__ __forceinline__ void noise_state_table(const RngState &s0, ulonglong4
     __syncthreads();
 }
 
-// One thread generates COLS consecutive columns (x, y) of the half-complex grid, z fastest: the
-// reference draws them in that order, so column c + 1 starts where column c ends and only the
-// first column of a thread needs a jump.  Values are staged per chunk of z and written as rows.
-template <typename T, int COLS>
+// One thread generates one column (x, y) of the half-complex grid, z fastest, from its jumped
+// state.  (Two consecutive columns a thread, the second continuing the first's stream without a
+// jump, measured slower at 512^3: 0.678 against 0.660 ms, with half the warps to hide the
+// xoshiro dependency chains.)  Values are staged per chunk of z and written as rows.
+template <typename T>
 __global__ void __launch_bounds__(NOISE_THREADS)
 k_noise(int N, const uint64_t *__restrict__ polys, RngState s0, T factor, const T *__restrict__ filt,
         cplx<T> *__restrict__ out, const RngState *__restrict__ states, size_t ostride) {
@@ -305,8 +306,8 @@ k_noise(int N, const uint64_t *__restrict__ polys, RngState s0, T factor, const 
     noise_state_table(s0, tab);
     const int H = N / 2 + 1;
     const long ncol = (long)N * N;
-    const long cblock = (long)blockIdx.x * NOISE_THREADS * COLS;  // first column of the block
-    const long c0 = cblock + (long)threadIdx.x * COLS;
+    const long cblock = (long)blockIdx.x * NOISE_THREADS;  // first column of the block
+    const long c0 = cblock + threadIdx.x;
     const bool valid = c0 < ncol;
     uint64_t r0 = 0, r1 = 0, r2 = 0, r3 = 0;
     if (valid) {
@@ -326,9 +327,8 @@ k_noise(int N, const uint64_t *__restrict__ polys, RngState s0, T factor, const 
             }
         }
     }
-#pragma unroll 1
-    for (int k = 0; k < COLS; k++) {
-        const long c = c0 + k;
+    {
+        const long c = c0;
         const int kx = valid ? kint((int)(c / N), N) : 0;
         const int ky = valid ? kint((int)(c % N), N) : 0;
         for (int z0 = 0; z0 < H; z0 += NOISE_CHUNK) {
@@ -354,20 +354,20 @@ k_noise(int N, const uint64_t *__restrict__ polys, RngState s0, T factor, const 
                 }
             }
             __syncthreads();
-            // write-out: row of thread rr is column cblock + rr COLS + k
+            // write-out: row of thread rr is column cblock + rr
             if (cz == NOISE_CHUNK) {
                 static_assert((NOISE_CHUNK & (NOISE_CHUNK - 1)) == 0, "chunk is a power of two");
                 constexpr int SH = __builtin_ctz(NOISE_CHUNK);
 #pragma unroll 4
                 for (int idx = threadIdx.x; idx < NOISE_THREADS * NOISE_CHUNK; idx += NOISE_THREADS) {
                     const int rr = idx >> SH, j = idx & (NOISE_CHUNK - 1);
-                    const long cc = cblock + (long)rr * COLS + k;
+                    const long cc = cblock + rr;
                     if (cc < ncol) out[cc * H + z0 + j] = stage[rr][j];
                 }
             } else {
                 for (int idx = threadIdx.x; idx < NOISE_THREADS * cz; idx += NOISE_THREADS) {
                     const int rr = idx / cz, j = idx % cz;
-                    const long cc = cblock + (long)rr * COLS + k;
+                    const long cc = cblock + rr;
                     if (cc < ncol) out[cc * H + z0 + j] = stage[rr][j];
                 }
             }
@@ -409,20 +409,15 @@ int noise_generate(const GridGeom &g, int precision, double boxlen, uint64_t st[
     const double factor = sqrt(boxvol / 2);  // src/grf.c:33
     const long ncol = (long)g.N * g.N;
     const int nb = states && batch > 1 ? batch : 1;
-    // two columns a thread when that still leaves 14 warps per SM (152 SMs) across the launch
-    // (384^3 and up); one otherwise
-    const int cols = (ncol * nb >= 2L * 152 * 448 && ncol % 2 == 0) ? 2 : 1;
-    const unsigned blocks = (unsigned)((ncol / cols + NOISE_THREADS - 1) / NOISE_THREADS);
+    const unsigned blocks = (unsigned)((ncol + NOISE_THREADS - 1) / NOISE_THREADS);
     const dim3 grid(blocks, nb);
     const RngState *sts = (const RngState *)states;
     launch_begin("noise");
     if (precision == MITOS_FP32) {
-        auto kern = cols == 2 ? k_noise<float, 2> : k_noise<float, 1>;
-        kern<<<grid, NOISE_THREADS, 0, stream()>>>(g.N, polys, s0, (float)factor, (const float *)filter_by_n2,
+        k_noise<float><<<grid, NOISE_THREADS, 0, stream()>>>(g.N, polys, s0, (float)factor, (const float *)filter_by_n2,
                                                    (float2 *)fbox, sts, bstride);
     } else {
-        auto kern = cols == 2 ? k_noise<double, 2> : k_noise<double, 1>;
-        kern<<<grid, NOISE_THREADS, 0, stream()>>>(g.N, polys, s0, factor, (const double *)filter_by_n2,
+        k_noise<double><<<grid, NOISE_THREADS, 0, stream()>>>(g.N, polys, s0, factor, (const double *)filter_by_n2,
                                                    (double2 *)fbox, sts, bstride);
     }
     count_launch();

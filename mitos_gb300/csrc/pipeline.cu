@@ -40,6 +40,40 @@ __global__ void k_filter(long n2max, double dk, double A_s, double n_s, double k
     }
 }
 
+// The same table for FP32 grids in FP32 arithmetic (the FP64 pipe runs at a small fraction of the
+// FP32 rate): the node search runs on the double table with k rounded to float; the power law,
+// the interpolation weights and the products in float (a few ulp of the FP64 table's values).
+__global__ void k_filter32(int n2max, float dk, float A_s, float ns1, float inv_kp, const double *__restrict__ tab,
+                           int k_size, float u_tau, float rescale, int poisson, float *__restrict__ out) {
+    for (int n2 = blockIdx.x * blockDim.x + threadIdx.x; n2 <= n2max; n2 += gridDim.x * blockDim.x) {
+        if (n2 == 0) { out[0] = 0; continue; }
+        const float k = sqrtf((float)n2) * dk;
+        float v = sqrtf(A_s * powf(k * inv_kp, ns1) * k * (float)(2. * M_PI * M_PI));
+        // transfer_at with the search on doubles (kspace.cuh)
+        const double *kt = tab, *lo = tab + k_size, *hi = tab + 2 * k_size;
+        const double kd = (double)k;
+        int i;
+        float u;
+        if (kd > kt[k_size - 1]) {
+            i = k_size - 2;
+            u = 1.f;
+        } else {
+            int a = 0, b = k_size - 1;
+            while (b - a > 1) {
+                const int m = (a + b) >> 1;
+                if (kt[m] <= kd) a = m; else b = m;
+            }
+            i = a;
+            u = (float)(kd - kt[i]) / (float)(kt[i + 1] - kt[i]);
+        }
+        const float T11 = (float)lo[i], T21 = (float)lo[i + 1], T12 = (float)hi[i], T22 = (float)hi[i + 1];
+        v *= (1.f - u_tau) * ((1.f - u) * T11 + u * T21) + u_tau * ((1.f - u) * T12 + u * T22);
+        v *= rescale;
+        if (poisson) v *= -1.f / k / k;
+        out[n2] = v;
+    }
+}
+
 static double g_stage_ms[16];
 static int g_nstages = 0;
 
@@ -205,8 +239,13 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
         int blocks = (int)((n2max + 256) / 256);
         if (blocks > 4096) blocks = 4096;
         launch_begin("filter");
-        k_filter<T><<<blocks, 256, 0, stream()>>>(n2max, dk, cfg->A_s, cfg->n_s, cfg->k_pivot, dtab, k_size, u_tau,
-                                                  1.0, ma ? 0 : 1, filt);
+        if constexpr (sizeof(T) == 4)
+            k_filter32<<<blocks, 256, 0, stream()>>>((int)n2max, (float)dk, (float)cfg->A_s, (float)(cfg->n_s - 1.),
+                                                     (float)(1. / cfg->k_pivot), dtab, k_size, (float)u_tau, 1.f,
+                                                     ma ? 0 : 1, (float *)filt);
+        else
+            k_filter<T><<<blocks, 256, 0, stream()>>>(n2max, dk, cfg->A_s, cfg->n_s, cfg->k_pivot, dtab, k_size,
+                                                      u_tau, 1.0, ma ? 0 : 1, filt);
         count_launch();
         MITOS_LAUNCH_CHECK("filter table");
     }

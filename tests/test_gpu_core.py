@@ -37,9 +37,9 @@ def test_noise_fp64_matches_stream(N):
     ml.free_local_grid(g)
 
 
-def test_noise_two_columns_per_thread_matches_stream():
-    """at N^2 >= 2 x 152 x 448 columns a thread generates two consecutive columns from one jump
-    (the second continues the first's stream): 384^3 takes that path"""
+def test_noise_384_matches_stream():
+    """a production-sized grid: 147456 column jumps from the block tables, every column checked
+    (the odd ones separately, as a column-pairing mistake would show there)"""
     N, L = 384, 1536.0
     ref = oracle.grf(N, L, 11, hermitian=False)
     for prec, tol in ((ml.FP64, 1e-14), (ml.FP32, 2e-6)):
@@ -47,7 +47,6 @@ def test_noise_two_columns_per_thread_matches_stream():
         ml.generate_complex_grf(g, ml.rng_init(11))
         got = ml.get_fbox(g).astype(np.complex128)
         assert rel_err(got, ref) < tol, prec
-        # the odd columns (each thread's second) carry the stream too, not just the even ones
         assert rel_err(got.reshape(N * N, -1)[1::2], ref.reshape(N * N, -1)[1::2]) < tol, prec
         ml.free_local_grid(g)
 
