@@ -255,6 +255,17 @@ template <int NL, int SN> __device__ __forceinline__ int xpos(int i) {
     else return spad(i);
 }
 
+// Barrier of a stage exchange.  A pencil held by one warp or half-warp (SN == 1: pencils are not
+// interleaved across lanes) exchanges only within that warp: __syncwarp.  Otherwise the block's.
+// (Blocks are whole warps: the tile setter rejects others.)
+template <int NL, int E, int SN> constexpr bool warp_pencil() {
+    return SN == 1 && NL / E <= 32 && 32 % (NL / E) == 0;
+}
+template <int NL, int E, int SN> __device__ __forceinline__ void pencil_sync() {
+    if constexpr (warp_pencil<NL, E, SN>()) __syncwarp();
+    else __syncthreads();
+}
+
 template <typename T, int E, int SIGN, int NL, int SN, int S>
 struct CTStage {
     using Sch = CTSched<NL, E>;
@@ -287,7 +298,7 @@ struct CTStage {
                     }
                 }
             }
-            __syncthreads();
+            pencil_sync<NL, E, SN>();
 #pragma unroll
             for (int b = 0; b < E / R; b++) {
                 const int j = t + b * (NL / E);
@@ -309,7 +320,7 @@ struct CTStage {
                 }
                 dft<T, R, SIGN>(v + b * R);
             }
-            __syncthreads();
+            pencil_sync<NL, E, SN>();
             CTStage<T, E, SIGN, NL, SN, S + 1>::run(v, sm, t, tw, tw_scale);
         }
     }

@@ -447,7 +447,8 @@ __global__ void __launch_bounds__(256) k_z_r2c(GridGeom g, PassArgs a) {
     fft_any<T, E, -1, NL, 1>(pl, v, psm, 1, t, tw);
 #pragma unroll
     for (int e = 0; e < E; e++) psm[xpos<NL, 1>(nout_any<NL, E>(pl, t, e))] = v[e];
-    __syncthreads();
+    if constexpr (NL > 0) pencil_sync<NL, E, 1>();
+    else __syncthreads();
     if (!valid) return;
     cplx<T> *dst = bat<cplx<T>>(a.out[0], bo) + row * H;
     for (int k = t; k <= h; k += tpp) {
