@@ -24,14 +24,21 @@ template <int AXIS, int OP, int NL> constexpr bool strided_heavy() {
     return NL > 0 && AXIS == 1 && (OP == YOP_HESS || OP == YOP_DISP);
 }
 
-// The Hessian X pass of the compile-time lengths runs one 512-thread block per SM with up to 128
-// registers (at 64 it spills 216 bytes a thread; measured at 512^3: 0.70 ms against 0.85).
-template <int AXIS, int OP, int NL> constexpr int strided_min_blocks() {
-    return (NL > 0 && AXIS == 0 && OP == XOP_HESS) ? 1 : 2;
+// Blocks per SM the register allocation is sized for (measured at 512^3): the Hessian X pass one
+// 512-thread block with up to 128 registers (at 64 it spills 216 bytes a thread: 0.70 ms against
+// 0.85); the displacement Y pass three 256-thread blocks (79 registers, no spills: 0.905 ms against
+// 0.972 with two); the Hessian Y pass two (at three it spills 132 bytes: 1.92 ms against 1.66).
+// (The X passes keep 8 pencils a block: 64-byte row segments.  With 4 pencils in 256-thread blocks,
+// three a SM, x_combine_disp ran 1.00 ms against 0.87 and x_hess 1.05 against 0.70.)
+template <int AXIS, int OP, int NL, int PC, int E> constexpr int strided_threads() {
+    return NL > 0 ? PC * (NL / E) : (strided_heavy<AXIS, OP, NL>() ? 256 : 512);
+}
+template <int AXIS, int OP, int NL, int PC, int E> constexpr int strided_min_blocks() {
+    return (NL > 0 && AXIS == 0 && OP == XOP_HESS) ? 1 : (NL > 0 && AXIS == 1 && OP == YOP_DISP) ? 3 : 2;
 }
 
 template <typename T, int E, int SIGN, int AXIS, int OP, int NL, int PC>
-__global__ void __launch_bounds__(strided_heavy<AXIS, OP, NL>() ? 256 : 512, strided_min_blocks<AXIS, OP, NL>()) k_strided(GridGeom g, PassArgs a, const T *__restrict__ win) {
+__global__ void __launch_bounds__(strided_threads<AXIS, OP, NL, PC, E>(), strided_min_blocks<AXIS, OP, NL, PC, E>()) k_strided(GridGeom g, PassArgs a, const T *__restrict__ win) {
     extern __shared__ __align__(16) unsigned char smraw[];
     cplx<T> *sm = reinterpret_cast<cplx<T> *>(smraw);
     const FFTPlan &pl = g.plN;
