@@ -93,9 +93,25 @@ int grid_hessian(const GridGeom &g, int prec, double boxlen, const void *phi, in
     int e = prec == MITOS_FP32 ? launch_x<float>(g, XOP_HESS, +1, a) : launch_x<double>(g, XOP_HESS, +1, a);
     if (e) return e;
     a.window_order = 0;
-    for (int i = 0; i < 3; i++) a.in[i] = A[i];
     for (int i = 0; i < 6; i++) a.out[i] = B[i];
-    e = prec == MITOS_FP32 ? launch_y<float>(g, YOP_HESS, +1, a) : launch_y<double>(g, YOP_HESS, +1, a);
+    // Y: one pass per X output, [xx, xy, xz, yy, yz, zz] = [A2, i ky A1, A1, -ky^2 A0, i ky A0, A0]
+    // (single-input passes fit three 256-thread blocks an SM where one three-input pass needs 128
+    // registers and runs two; the plain pass of A2 runs the wider 512-thread tiles)
+    {
+        auto ly = [&](YOp op) { return prec == MITOS_FP32 ? launch_y<float>(g, op, +1, a) : launch_y<double>(g, op, +1, a); };
+        a.in[0] = A[0];
+        a.out[0] = B[3];
+        a.out[1] = B[4];
+        a.out[2] = B[5];
+        e = ly(YOP_HESS_A);
+        a.in[0] = A[1];
+        a.out[0] = B[1];
+        a.out[1] = B[2];
+        if (!e) e = ly(YOP_HESS_B);
+        a.in[0] = A[2];
+        a.out[0] = B[0];
+        if (!e) e = ly(YOP_PLAIN);
+    }
     if (e) return e;
     for (int i = 0; i < 6; i++) a.in[i] = B[i];
     a.out[0] = out;

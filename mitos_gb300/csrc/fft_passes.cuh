@@ -41,8 +41,9 @@ enum XOp {
 };
 enum YOp {
     YOP_PLAIN = 0,    // out = FFT(in) * scale
-    YOP_HESS,         // 3 in -> 6 out: A2, i ky A1, A1, -ky^2 A0, i ky A0, A0
-    YOP_DISP          // 2 in -> 3 out: C1, i ky C0, C0
+    YOP_DISP,         // 2 in -> 3 out: C1, i ky C0, C0
+    YOP_HESS_A,       // 1 in -> 3 out: -ky^2 A, i ky A, A (the Hessian's yy, yz, zz chains)
+    YOP_HESS_B        // 1 in -> 2 out: i ky A, A (xy, xz)
 };
 enum ZOp {
     ZOP_C2R = 0,      // real out = c2r(in) * scale
