@@ -20,14 +20,15 @@ template <> __device__ __forceinline__ double dev_sqrt<double>(double x) { retur
 // (the X passes need the wider pencil groups for coalescing: their pencils are adjacent columns of
 // an x-plane).
 template <int AXIS, int OP, int NL> constexpr bool strided_heavy() {
-    return NL > 0 && AXIS == 1 && (OP == YOP_DISP || OP == YOP_HESS_A || OP == YOP_HESS_B);
+    return NL > 0 && AXIS == 1 && (OP == YOP_DISP_A || OP == YOP_HESS_A || OP == YOP_HESS_B);
 }
 
 // Blocks per SM the register allocation is sized for (measured at 512^3): the Hessian X pass one
 // 512-thread block with up to 128 registers (at 64 it spills 216 bytes a thread: 0.70 ms against
 // 0.85); the displacement Y pass three 256-thread blocks (79 registers, no spills: 0.905 ms against
 // 0.972 with two) and so do the single-input Hessian Y passes (a three-input pass needed 128
-// registers at two blocks: 1.66 ms, against 1.41 for the three single-input passes).
+// registers at two blocks: 1.66 ms, against 1.41 for the three single-input passes).  The
+// displacement Y step is split the same way (a two-input pass and a stencil-only pass).
 // (The X passes keep 8 pencils a block: 64-byte row segments.  With 4 pencils in 256-thread blocks,
 // three a SM, x_combine_disp ran 1.00 ms against 0.87 and x_hess 1.05 against 0.70.)
 template <int AXIS, int OP, int NL, int PC, int E> constexpr int strided_threads() {
@@ -35,7 +36,7 @@ template <int AXIS, int OP, int NL, int PC, int E> constexpr int strided_threads
 }
 template <int AXIS, int OP, int NL, int PC, int E> constexpr int strided_min_blocks() {
     return (NL > 0 && AXIS == 0 && OP == XOP_HESS) ? 1
-           : (NL > 0 && AXIS == 1 && (OP == YOP_DISP || OP == YOP_HESS_A || OP == YOP_HESS_B)) ? 3 : 2;
+           : (NL > 0 && AXIS == 1 && (OP == YOP_DISP_A || OP == YOP_HESS_A || OP == YOP_HESS_B)) ? 3 : 2;
 }
 
 template <typename T, int E, int SIGN, int AXIS, int OP, int NL, int PC>
@@ -86,7 +87,7 @@ __global__ void __launch_bounds__(strided_threads<AXIS, OP, NL, PC, E>(), stride
         __syncthreads();
     }
 
-    constexpr int NIN = (AXIS == 1 && OP == YOP_DISP) ? 2 : 1;
+    constexpr int NIN = 1;
     cplx<T> raw[E];
     cplx<T> v[E];
 #pragma unroll 1
@@ -106,21 +107,18 @@ __global__ void __launch_bounds__(strided_threads<AXIS, OP, NL, PC, E>(), stride
         int outs[3] = {0, 0, 0}, facs[3] = {0, 0, 0};
         if (AXIS == 0 && OP == XOP_HESS) { nout = 3; outs[1] = 1; outs[2] = 2; facs[1] = 1; facs[2] = 2; }
         if (AXIS == 0 && OP == XOP_DISP) { nout = 2; outs[1] = 1; facs[1] = 1; }
-        if (AXIS == 1 && OP == YOP_DISP) {
-            if (i == 0) { nout = 2; outs[0] = 1; facs[0] = 1; outs[1] = 2; }
-            if (i == 1) { nout = 1; outs[0] = 0; }
-        }
+        if (AXIS == 1 && OP == YOP_DISP_A) { nout = 2; outs[1] = 1; facs[0] = 1; }
         if (AXIS == 1 && OP == YOP_HESS_A) { nout = 3; outs[1] = 1; outs[2] = 2; facs[0] = 2; facs[1] = 1; }
         if (AXIS == 1 && OP == YOP_HESS_B) { nout = 2; outs[1] = 1; facs[0] = 1; }
-        constexpr int MU = (OP == YOP_HESS_A || OP == YOP_HESS_B) ? 3 : 1;
+        constexpr int MU = (OP == YOP_HESS_A || OP == YOP_HESS_B || OP == YOP_DISP_A) ? 3 : 1;
 #pragma unroll MU
         for (int m = 0; m < nout; m++) {
             const int fac = facs[m];
             // on-node TSC stencil of the displacement passes, applied to the k-space input:
             // x for the d_x chain (X output 1), y for the d_x and d_y chains (Y outputs 0, 1)
             const T *stn = nullptr;
-            if constexpr ((AXIS == 0 && OP == XOP_DISP) || (AXIS == 1 && OP == YOP_DISP)) {
-                if ((AXIS == 0 && outs[m] == 1) || (AXIS == 1 && outs[m] <= 1))
+            if constexpr ((AXIS == 0 && OP == XOP_DISP) || (AXIS == 1 && (OP == YOP_DISP_A || OP == YOP_STN))) {
+                if ((AXIS == 0 && outs[m] == 1) || (AXIS == 1 && outs[m] == 0))
                     stn = reinterpret_cast<const T *>(a.stencil);
             }
 #pragma unroll
@@ -482,7 +480,7 @@ static int launch_strided_e(const GridGeom &g, const PassArgs &a, const T *win) 
     auto kern = k_strided<T, E, SIGN, AXIS, OP, NL, PC>;
     if (smem > 48 * 1024) MITOS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     launch_begin(AXIS == 0 ? (OP == XOP_HESS ? "x_hess" : OP == XOP_DISP ? "x_disp" : OP == XOP_COMBINE_2LPT ? "x_combine" : OP == XOP_ADD_POISSON ? "x_add_poisson" : OP == XOP_PK ? "x_pk" : "x_plain")
-                        : (OP == YOP_HESS_A ? "y_hess_a" : OP == YOP_HESS_B ? "y_hess_b" : OP == YOP_DISP ? "y_disp" : "y_plain"));
+                        : (OP == YOP_HESS_A ? "y_hess_a" : OP == YOP_HESS_B ? "y_hess_b" : OP == YOP_DISP_A ? "y_disp_a" : OP == YOP_STN ? "y_stn" : "y_plain"));
     kern<<<dim3((unsigned)blocks, a.batch > 1 ? a.batch : 1), threads, smem, stream()>>>(g, with_f32(a), win);
     count_launch();
     MITOS_LAUNCH_CHECK("strided FFT pass");
@@ -543,7 +541,8 @@ int launch_y_t(const GridGeom &g, YOp op, int sign, const PassArgs &a) {
     switch (op) {
     case YOP_PLAIN:
         return sign < 0 ? launch_strided<T, -1, 1, YOP_PLAIN, NL, PC>(g, a, nullptr) : launch_strided<T, 1, 1, YOP_PLAIN, NL, PC>(g, a, nullptr);
-    case YOP_DISP: return launch_strided<T, 1, 1, YOP_DISP, NL, PCH>(g, a, nullptr);
+    case YOP_DISP_A: return launch_strided<T, 1, 1, YOP_DISP_A, NL, PCH>(g, a, nullptr);
+    case YOP_STN: return launch_strided<T, 1, 1, YOP_STN, NL, PC>(g, a, nullptr);
     case YOP_HESS_A: return launch_strided<T, 1, 1, YOP_HESS_A, NL, PCH>(g, a, nullptr);
     case YOP_HESS_B: return launch_strided<T, 1, 1, YOP_HESS_B, NL, PCH>(g, a, nullptr);
     }

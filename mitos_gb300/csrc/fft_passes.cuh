@@ -41,7 +41,8 @@ enum XOp {
 };
 enum YOp {
     YOP_PLAIN = 0,    // out = FFT(in) * scale
-    YOP_DISP,         // 2 in -> 3 out: C1, i ky C0, C0
+    YOP_DISP_A,       // 1 in -> 2 out: i ky C (y stencil), C (the displacements' d_y and d_z chains)
+    YOP_STN,          // 1 in -> 1 out: C (y stencil) (the d_x chain)
     YOP_HESS_A,       // 1 in -> 3 out: -ky^2 A, i ky A, A (the Hessian's yy, yz, zz chains)
     YOP_HESS_B        // 1 in -> 2 out: i ky A, A (xy, xz)
 };

@@ -354,12 +354,14 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     if (!fused_disp_x) e = launch_x<T>(g, XOP_DISP, +1, a);
     if (e) return e;
     a.window_order = 0;
+    // Y: [B0, B1, B2] = [A1, i ky A0, A0], the y stencil on the d_x and d_y chains (B0, B1)
     a.in[0] = A0;
-    a.in[1] = A1;
+    a.out[0] = B1;
+    a.out[1] = B2;
+    e = launch_y<T>(g, YOP_DISP_A, +1, a);
+    a.in[0] = A1;
     a.out[0] = B0;
-    a.out[1] = B1;
-    a.out[2] = B2;
-    e = launch_y<T>(g, YOP_DISP, +1, a);
+    if (!e) e = launch_y<T>(g, YOP_STN, +1, a);
     if (e) return e;
     a.in[0] = B0;
     a.in[1] = B1;
