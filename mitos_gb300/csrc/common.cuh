@@ -45,6 +45,9 @@ template <typename T> __host__ __device__ __forceinline__ cplx<T> cconj(cplx<T> 
 void set_error(int code, const char *fmt, ...);
 int check_cuda(cudaError_t e, const char *what);
 
+// prefetch the 32-byte sector at p into L2 (no register is written; p must lie in an allocation)
+__device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
 #define MITOS_CUDA(call)                                                                  \
     do {                                                                                  \
         cudaError_t _e = (call);                                                          \

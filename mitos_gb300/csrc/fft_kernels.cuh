@@ -228,6 +228,10 @@ __global__ void __launch_bounds__(512, 2) k_x_combine_disp(GridGeom g, PassArgs 
     const size_t bo = (size_t)blockIdx.y * (size_t)a.bstride;
     const cplx<T> *src = bat<const cplx<T>>(a.in[0], bo);
     const cplx<T> *phi1 = bat<const cplx<T>>(a.in2, bo);
+    // phi_1 is read after the forward transform: start its sectors towards L2 now (measured at
+    // 512^3: 0.81 ms against 0.86)
+#pragma unroll
+    for (int e = 0; e < E; e++) prefetch_l2(phi1 + col + (long)nout_any<NL, E>(pl, t, e) * g.plane);
     cplx<T> v[E];
 #pragma unroll
     for (int e = 0; e < E; e++) v[e] = valid ? src[col + (long)nin_any<NL, E>(pl, t, e) * g.plane] : mk<T>(0, 0);
@@ -309,6 +313,16 @@ __global__ void __launch_bounds__(256, OP == ZOP_HESS_MA ? 1 : 2) k_z_c2r(GridGe
         if (OP == ZOP_HESS_2LPT || OP == ZOP_HESS_MA) fac = (f == 2 || f == 4) ? 1 : (f == 5 ? 2 : 0);
         if (OP == ZOP_DISP) fac = (f == 2) ? 1 : 0;
         const cplx<T> *src = bat<const cplx<T>>(a.in[f], bo) + row * H;
+        // the displacement pass starts the next field's row towards L2 while this one is transformed
+        // (one 32-byte sector a lane; measured at 512^3: 0.68 ms against 0.74.  In the 2LPT source
+        // pass the same prefetch cost its register allocation: 1.30 ms against 1.09)
+        if constexpr (OP == ZOP_DISP) {
+            if (q + 1 < NIN) {
+                const char *nxt = reinterpret_cast<const char *>(bat<const cplx<T>>(a.in[q + 1], bo) + row * H);
+                const int nsec = (int)((H * sizeof(cplx<T>) + 31) / 32);
+                for (int sct = t; sct < nsec; sct += tpp) prefetch_l2(nxt + 32 * sct);
+            }
+        }
         cplx<T> v[E];
 #pragma unroll
         for (int e = 0; e < E; e++) {
