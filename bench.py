@@ -191,6 +191,29 @@ def extras(ml, table, spline, args) -> dict:
     out["fp64"] = {"ms_per_ic": ms64, "ic_per_s": 1e3 / ms64,
                    "pk_fp32_vs_fp64": {"max_rel": float(rel.max()), "bins": int(ok.sum()), "target": 1e-4}}
 
+    # particle velocities (the velocity transfer function t_cdm, 2LPT with the reference's velocity
+    # factors, TSC gather at the displaced positions): the 512^3 FP32 IC with positions and velocities
+    # into pinned host buffers, CUDA events on the library stream (the copies run on the copy stream)
+    import torch
+    pv = [torch.empty((N ** 3, 3), dtype=torch.float32, pin_memory=True) for _ in range(2)]
+    kv, pk_, ov = np.zeros(args.bins), np.zeros(args.bins), np.zeros(args.bins, np.int64)
+    rv = ml.ICResult(kv.ctypes.data_as(ml._dp), pk_.ctypes.data_as(ml._dp), ov.ctypes.data_as(ml._lp),
+                     ctypes.cast(pv[0].data_ptr(), ml._fp), 0, 0.0, ctypes.cast(pv[1].data_ptr(), ml._fp))
+    cv = cfg(ml.FP32, args.seed)
+    ml._check(ml.load().ic_pipeline_run(ctypes.byref(cv), ctypes.byref(spline.sp), ctypes.byref(rv)))
+    ml.kernel_timing(True)
+    ml.timer_start()
+    for i in range(3):
+        ml._check(ml.load().ic_pipeline_run(ctypes.byref(cv), ctypes.byref(spline.sp), ctypes.byref(rv)))
+    msv = ml.timer_stop() / 3
+    kt = ml.kernel_times()
+    ml.kernel_timing(False)
+    vg = [t for n, t in kt if n == "vel_gather"]
+    out["velocities"] = {"ms_per_ic": msv, "ic_per_s": 1e3 / msv,
+                         "vel_gather_ms": sum(vg) / max(len(vg), 1),
+                         "vel_rms": float(np.sqrt(np.mean(pv[1].numpy()[::4096] ** 2)))}
+    del pv
+
     # 48 realisations (16 x 64^3 / 256, 16 x 96^3 / 384, 16 x 128^3 / 512 Mpc/h; 4 Mpc/h cells),
     # seeds 1000-1047, one captured CUDA graph over 8 streams, tiles from the autotuner
     sizes = [(64, 256.0), (96, 384.0), (128, 512.0)]

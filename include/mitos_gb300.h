@@ -269,6 +269,8 @@ struct ic_config {
     int pk_linear;      /* 1: linear shells to k_Nyquist; 0: the reference log bins */
     int precision;      /* MITOS_FP32 or MITOS_FP64 */
     int keep_outputs;   /* 1: keep the displacement grids, positions and density on the device */
+    int index_vel;      /* velocity transfer function (TransferFunctionVelocity, src/mitos.c:425-490);
+                           used when res->vel is set */
 };
 struct ic_result {
     double *pk_k;       /* host [pk_bins] */
@@ -277,6 +279,10 @@ struct ic_result {
     float *pos;         /* optional host [M^3 * 3]: positions after the wrap */
     int ma_iterations;  /* Monge-Ampere cycles run */
     double ma_residual; /* last sqrt(sum res^2 / sum rho^2) */
+    float *vel;         /* optional host [M^3 * 3]: particle velocities (src/mitos.c:865-908): the TSC
+                           gather of the velocity grids at the displaced positions; the velocity
+                           potential from 2LPT with the reference's velocity factors (:453-455) for
+                           2LPT configurations, else the inverse Poisson kernel (:457) */
 };
 int ic_pipeline_run(const struct ic_config *cfg, const struct perturb_spline *spline,
                     struct ic_result *res);

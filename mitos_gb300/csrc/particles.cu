@@ -123,7 +123,7 @@ template <typename T>
 __global__ void __launch_bounds__(256)
 k_displace_cic(int N, int M, float spacing, T boxlen, T gfac, T val,
                const T *__restrict__ d0, const T *__restrict__ d1, const T *__restrict__ d2,
-               T *__restrict__ rho, float *__restrict__ pos_out) {
+               T *__restrict__ rho, float *__restrict__ pos_out, float *__restrict__ posraw_out) {
     const long np = (long)M * M * M;
     const long id = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= np) return;
@@ -139,6 +139,11 @@ k_displace_cic(int N, int M, float spacing, T boxlen, T gfac, T val,
         const T disp = tsc_gather<T>(dd[dir], N, (T)p[0] * Nf / boxlen, (T)p[1] * Nf / boxlen,
                                      (T)p[2] * Nf / boxlen);
         p[dir] = (float)((T)p[dir] - disp);
+    }
+    if (posraw_out) {  // before the wrap: the velocity gather's positions (src/mitos.c:865-908)
+        posraw_out[3 * id] = p[0];
+        posraw_out[3 * id + 1] = p[1];
+        posraw_out[3 * id + 2] = p[2];
     }
     const float Lf = (float)boxlen;
 #pragma unroll
@@ -298,7 +303,7 @@ template <typename T>
 __global__ void __launch_bounds__(LB_THREADS, 2)
 k_lattice_cic(int N, int rpd, int rpo, float spacing, float Lf, T ginv, const T *__restrict__ d0, const T *__restrict__ d1,
               const T *__restrict__ d2, T *__restrict__ rho, float *__restrict__ pos_out, size_t bstride, FastDiv div_bx,
-              FastDiv div_by) {
+              FastDiv div_by, float *__restrict__ posraw_out) {
     // batched launches: realisation blockIdx.y (its grids bstride bytes apart)
     if (gridDim.y > 1) {
         const size_t bo = (size_t)blockIdx.y * bstride;
@@ -391,6 +396,12 @@ k_lattice_cic(int N, int rpd, int rpo, float spacing, float Lf, T ginv, const T 
                 p2 = z * spacing;
                 displace_global<T>(N, rpd, ginv, d1, d2, y, z, p0, p1, p2);
             }
+            if (posraw_out) {  // before the wrap: the velocity gather's positions
+                const long id = ((long)x * N + y) * N + z;
+                posraw_out[3 * id] = p0;
+                posraw_out[3 * id + 1] = p1;
+                posraw_out[3 * id + 2] = p2;
+            }
             p0 = fwrapf(p0, Lf);
             p1 = fwrapf(p1, Lf);
             p2 = fwrapf(p2, Lf);
@@ -461,7 +472,7 @@ static size_t lattice_smem(size_t elem) {
 
 template <typename T>
 static int lattice_launch(int N, int rpd, int rpo, float spacing, float Lf, double ginv, const void *d0, const void *d1,
-                          const void *d2, void *rho, float *pos_out, int batch, size_t bstride) {
+                          const void *d2, void *rho, float *pos_out, int batch, size_t bstride, float *posraw_out) {
     static int blocks_per_sm[2] = {0, 0};  // per precision, for the current device
     static int sms = 0;
     const size_t smem = lattice_smem(sizeof(T));
@@ -480,12 +491,14 @@ static int lattice_launch(int N, int rpd, int rpo, float spacing, float Lf, doub
     const unsigned blocks = (unsigned)std::max<long>(1, std::min<long>(nbricks, (long)sms * bps / nb));
     kern<<<dim3(blocks, nb), LB_THREADS, smem, stream()>>>(N, rpd, rpo, spacing, Lf, (T)ginv, (const T *)d0,
                                                            (const T *)d1, (const T *)d2, (T *)rho, pos_out, bstride,
-                                                           make_fastdiv((unsigned)(N / LB_X)), make_fastdiv((unsigned)(N / LB_Y)));
+                                                           make_fastdiv((unsigned)(N / LB_X)), make_fastdiv((unsigned)(N / LB_Y)),
+                                                           posraw_out);
     return 0;
 }
 
 int lattice_deposit(int N, double boxlen, int precision, const void *d0, const void *d1, const void *d2,
-                    int disp_pitch, void *rho, int rho_pitch, float *pos_out, int batch, size_t bstride) {
+                    int disp_pitch, void *rho, int rho_pitch, float *pos_out, int batch, size_t bstride,
+                    float *posraw_out) {
     const size_t es = precision == MITOS_FP32 ? 4 : 8;
     if (N % LB_Z || N % LB_Y || N % LB_X || (rho_pitch * es) % 16 || (disp_pitch * es) % 16 ||
         ((uintptr_t)d0 | (uintptr_t)d1 | (uintptr_t)d2 | (uintptr_t)rho) % 16)
@@ -495,9 +508,9 @@ int lattice_deposit(int N, double boxlen, int precision, const void *d0, const v
     launch_begin("lattice_cic");
     const int e = precision == MITOS_FP32
                       ? lattice_launch<float>(N, disp_pitch, rho_pitch, spacing, Lf, N / boxlen, d0, d1, d2, rho, pos_out,
-                                              batch, bstride)
+                                              batch, bstride, posraw_out)
                       : lattice_launch<double>(N, disp_pitch, rho_pitch, spacing, Lf, N / boxlen, d0, d1, d2, rho, pos_out,
-                                               batch, bstride);
+                                               batch, bstride, posraw_out);
     if (e) return e;
     count_launch();
     MITOS_LAUNCH_CHECK("lattice CIC");
@@ -546,7 +559,7 @@ __global__ void k_cic(long n, int N, T gfac, T val, const float *__restrict__ po
 }
 
 int displace_and_deposit(int N, int M, double boxlen, int precision, const void *d0, const void *d1,
-                         const void *d2, void *rho, float *pos_out) {
+                         const void *d2, void *rho, float *pos_out, float *posraw_out) {
     const long np = (long)M * M * M;
     const float Lf = (float)boxlen;
     const float spacing = Lf / M;  // src/particle.c:102-103
@@ -557,13 +570,81 @@ int displace_and_deposit(int N, int M, double boxlen, int precision, const void 
     if (precision == MITOS_FP32)
         k_displace_cic<float><<<blocks, 256, 0, stream()>>>(N, M, spacing, (float)boxlen, (float)gfac, (float)val,
                                                             (const float *)d0, (const float *)d1, (const float *)d2,
-                                                            (float *)rho, pos_out);
+                                                            (float *)rho, pos_out, posraw_out);
     else
         k_displace_cic<double><<<blocks, 256, 0, stream()>>>(N, M, spacing, boxlen, gfac, val, (const double *)d0,
                                                              (const double *)d1, (const double *)d2, (double *)rho,
-                                                             pos_out);
+                                                             pos_out, posraw_out);
     count_launch();
     MITOS_LAUNCH_CHECK("displace + CIC");
+    return 0;
+}
+
+// Particle velocities (src/mitos.c:865-908): the TSC gather (src/grids_interp.c:267-309) of each
+// velocity grid (pitch N + 2) at the displaced, not yet wrapped position, X = x N / boxlen; float out.
+template <typename T>
+__global__ void k_vel_gather(long np, int N, T boxlen, const float *__restrict__ pos, const T *__restrict__ v0,
+                             const T *__restrict__ v1, const T *__restrict__ v2, float *__restrict__ vel) {
+    const long id = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= np) return;
+    const T Nf = (T)N;
+    const T X = (T)pos[3 * id] * Nf / boxlen, Y = (T)pos[3 * id + 1] * Nf / boxlen, Z = (T)pos[3 * id + 2] * Nf / boxlen;
+    // tsc_gather of the three grids with the node offsets and weights computed once
+    const T half = (T)0.5;
+    const int nx = (int)dfloor<T>(X + half), ny = (int)dfloor<T>(Y + half), nz = (int)dfloor<T>(Z + half);
+    const T dx = X - (T)nx, dy = Y - (T)ny, dz = Z - (T)nz;
+    T wx[3], wy[3], wz[3];
+    wx[0] = half * (half - dx) * (half - dx); wx[1] = (T)0.75 - dx * dx; wx[2] = half * (half + dx) * (half + dx);
+    wy[0] = half * (half - dy) * (half - dy); wy[1] = (T)0.75 - dy * dy; wy[2] = half * (half + dy) * (half + dy);
+    wz[0] = half * (half - dz) * (half - dz); wz[1] = (T)0.75 - dz * dz; wz[2] = half * (half + dz) * (half + dz);
+    int zi[3], yi[3], xi[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        zi[k] = wrapn(nz - 1 + k, N);
+        yi[k] = wrapn(ny - 1 + k, N);
+        xi[k] = wrapn(nx - 1 + k, N);
+    }
+    const long rp = N + 2;
+    T s0 = 0, s1 = 0, s2 = 0;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        T y0 = 0, y1 = 0, y2 = 0;
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            const long row = ((long)xi[i] * N + yi[j]) * rp;
+            T z0 = 0, z1 = 0, z2 = 0;
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                const long o = row + zi[k];
+                z0 += wz[k] * __ldg(v0 + o);
+                z1 += wz[k] * __ldg(v1 + o);
+                z2 += wz[k] * __ldg(v2 + o);
+            }
+            y0 += wy[j] * z0;
+            y1 += wy[j] * z1;
+            y2 += wy[j] * z2;
+        }
+        s0 += wx[i] * y0;
+        s1 += wx[i] * y1;
+        s2 += wx[i] * y2;
+    }
+    vel[3 * id] = (float)s0;
+    vel[3 * id + 1] = (float)s1;
+    vel[3 * id + 2] = (float)s2;
+}
+
+int velocity_gather(long np, int N, double boxlen, int precision, const float *pos, const void *v0, const void *v1,
+                    const void *v2, float *vel) {
+    const unsigned blocks = (unsigned)((np + 255) / 256);
+    launch_begin("vel_gather");
+    if (precision == MITOS_FP32)
+        k_vel_gather<float><<<blocks, 256, 0, stream()>>>(np, N, (float)boxlen, pos, (const float *)v0,
+                                                          (const float *)v1, (const float *)v2, vel);
+    else
+        k_vel_gather<double><<<blocks, 256, 0, stream()>>>(np, N, boxlen, pos, (const double *)v0,
+                                                           (const double *)v1, (const double *)v2, vel);
+    count_launch();
+    MITOS_LAUNCH_CHECK("velocity gather");
     return 0;
 }
 

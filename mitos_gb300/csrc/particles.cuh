@@ -6,14 +6,20 @@ namespace mitos {
 // lattice of M^3 particles, TSC displacement by the three padded displacement grids, wrap,
 // CIC into rho (padded real grid, accumulated, in units of the mean density); pos_out optional
 int displace_and_deposit(int N, int M, double boxlen, int precision, const void *d0, const void *d1,
-                         const void *d2, void *rho, float *pos_out);
+                         const void *d2, void *rho, float *pos_out, float *posraw_out = nullptr);
 // lattice-aligned fast path (M = N, exact nodes); the displacement grids must carry the folded
 // on-node TSC stencils (PassArgs::stencil in the displacement passes)
 // disp_pitch / rho_pitch: row pitches (elements) of the displacement grids and of rho, 16-byte multiples
 // batch > 1: that many realisations, every grid (d0, d1, d2, rho) bstride bytes apart; pos_out null
+// posraw_out (optional): the positions before the wrap (the velocity gather's), M^3 x 3
 int lattice_deposit(int N, double boxlen, int precision, const void *d0, const void *d1, const void *d2,
-                    int disp_pitch, void *rho, int rho_pitch, float *pos_out, int batch = 1, size_t bstride = 0);
+                    int disp_pitch, void *rho, int rho_pitch, float *pos_out, int batch = 1, size_t bstride = 0,
+                    float *posraw_out = nullptr);
 bool lattice_aligned(int N, int M, double boxlen);
+// particle velocities: TSC gather of the three velocity grids (pitch N + 2) at the unwrapped
+// positions pos (np x 3), float velocities out (np x 3)
+int velocity_gather(long np, int N, double boxlen, int precision, const float *pos, const void *v0, const void *v1,
+                    const void *v2, float *vel);
 // CIC of n given positions with per-particle value val
 int cic_positions(long n, int N, double boxlen, int precision, const float *pos, double val, void *rho);
 

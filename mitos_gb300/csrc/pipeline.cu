@@ -159,9 +159,13 @@ void mitos::seed_state(uint64_t seed, uint64_t st[4]) {
     }
 }
 
+// the reference's 2LPT factors of the velocity potential (src/mitos.c:453-455)
+static const double F1_VEL = -0.001147273637728, F2_VEL = 3.19354920304769E-05;
+
 template <typename T>
 static int run_pipeline(const struct ic_config *cfg, const double *ktab, const double *tlo, const double *thi,
-                        int k_size, double u_tau, struct ic_result *res, const PipeOpts *opt) {
+                        const double *tvlo, const double *tvhi, int k_size, double u_tau, struct ic_result *res,
+                        const PipeOpts *opt) {
     const int prec = cfg->precision;
     const int N = cfg->N, M = cfg->M;
     const double L = cfg->boxlen;
@@ -187,6 +191,11 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
         return 3;
     }
     const size_t gb = B > 1 ? B * bs : gb1, db = B > 1 ? B * bs : db1;
+    const bool want_vel = res && res->vel;
+    if (want_vel && (!tvlo || !tvhi || B > 1)) {
+        set_error(1, "velocities need a velocity transfer function (ic_config.index_vel) and an unbatched run");
+        return 1;
+    }
     const int acc_stride = 3 * cfg->pk_bins + 2;
     auto reset = [&](PassArgs &x) {
         memset(&x, 0, sizeof x);
@@ -204,7 +213,9 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     if (!phi || !S || !Sk || !rho || !A0 || !A1 || !B0 || !B1 || !B2 || !D0 || !D1 || !D2) return 5;
     const long n2max = 3L * (N / 2) * (N / 2);
     T *filt = (T *)workspace(sizeof(T) * (n2max + 1), 106);
-    double *dtab = (opt && opt->dtab) ? opt->dtab : (double *)workspace(sizeof(double) * 3 * k_size, 107);
+    // transfer rows [k, lo, hi] of the density function, then (velocities) those of the velocity one
+    const int tab_rows = want_vel ? 6 : 3;
+    double *dtab = (opt && opt->dtab) ? opt->dtab : (double *)workspace(sizeof(double) * tab_rows * k_size, 107);
     double *acc = (opt && opt->acc) ? opt->acc : (double *)workspace(sizeof(double) * acc_stride, 104);
     if (!filt || !dtab || !acc) return 5;
     double *red = acc + 3 * cfg->pk_bins;
@@ -222,33 +233,41 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
         }
     } else {
         const int tslot = (opt && opt->async_slot >= 0) ? opt->async_slot : 2;
-        double *ht = table_pinned(tslot, 3 * (size_t)k_size);
+        double *ht = table_pinned(tslot, (size_t)tab_rows * k_size);
         if (!ht) return 5;
         memcpy(ht, ktab, sizeof(double) * k_size);
         memcpy(ht + k_size, tlo, sizeof(double) * k_size);
         memcpy(ht + 2 * k_size, thi, sizeof(double) * k_size);
+        if (want_vel) {
+            memcpy(ht + 3 * k_size, ktab, sizeof(double) * k_size);
+            memcpy(ht + 4 * k_size, tvlo, sizeof(double) * k_size);
+            memcpy(ht + 5 * k_size, tvhi, sizeof(double) * k_size);
+        }
         double *hd = nullptr;
         MITOS_CUDA(cudaHostGetDevicePointer((void **)&hd, ht, 0));
         launch_begin("table_in");
-        k_copy_table<<<8, 256, 0, stream()>>>(hd, dtab, 3 * k_size);
+        k_copy_table<<<8, 256, 0, stream()>>>(hd, dtab, tab_rows * k_size);
         count_launch();
         MITOS_LAUNCH_CHECK("transfer table upload");
     }
     const bool ma = cfg->method == MITOS_METHOD_MONGE_AMPERE;
-    {
+    // filter per |n|^2 from the rows at tab, with (poisson = 1) or without the -1/k^2 kernel
+    auto filter_launch = [&](const double *tab, int poisson, T *out) {
         int blocks = (int)((n2max + 256) / 256);
         if (blocks > 4096) blocks = 4096;
         launch_begin("filter");
         if constexpr (sizeof(T) == 4)
             k_filter32<<<blocks, 256, 0, stream()>>>((int)n2max, (float)dk, (float)cfg->A_s, (float)(cfg->n_s - 1.),
-                                                     (float)(1. / cfg->k_pivot), dtab, k_size, (float)u_tau, 1.f,
-                                                     ma ? 0 : 1, (float *)filt);
+                                                     (float)(1. / cfg->k_pivot), tab, k_size, (float)u_tau, 1.f,
+                                                     poisson, (float *)out);
         else
-            k_filter<T><<<blocks, 256, 0, stream()>>>(n2max, dk, cfg->A_s, cfg->n_s, cfg->k_pivot, dtab, k_size,
-                                                      u_tau, 1.0, ma ? 0 : 1, filt);
+            k_filter<T><<<blocks, 256, 0, stream()>>>(n2max, dk, cfg->A_s, cfg->n_s, cfg->k_pivot, tab, k_size,
+                                                      u_tau, 1.0, poisson, out);
         count_launch();
-        MITOS_LAUNCH_CHECK("filter table");
-    }
+        const cudaError_t ce = cudaGetLastError();
+        return ce == cudaSuccess ? 0 : check_cuda(ce, "filter table");
+    };
+    if (int fe = filter_launch(dtab, ma ? 0 : 1, filt)) return fe;
     tim.mark();
 
     // S1: noise (src/mitos.c:148,220-224 + generatePerturbationGrid)
@@ -378,22 +397,27 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     // S5: particles + CIC.  The positions are staged in a device buffer of the run's slot and copied
     // to the caller on the copy stream as soon as the deposit ends, under the P(k) passes (and, for
     // ic_pipeline_submit, under the next IC); the buffer is reused once its last copy is done.
-    float *dpos = nullptr;
+    float *dpos = nullptr, *dposraw = nullptr;
     const int pslot = (opt && opt->async_slot >= 0) ? opt->async_slot : 0;
     const size_t pos_bytes = sizeof(float) * 3 * (size_t)M * M * M;
     if (res && res->pos) {
         dpos = (float *)workspace(pos_bytes, 108 + pslot);
         if (!dpos) return 5;
-        MITOS_CUDA(cudaStreamWaitEvent(stream(), pos_event(pslot, 1), 0));
     }
+    if (want_vel) {
+        dposraw = (float *)workspace(pos_bytes, 112);  // the velocity gather's unwrapped positions
+        if (!dposraw) return 5;
+    }
+    // the slot's staging buffers are free once their previous copies are done
+    if (dpos || want_vel) MITOS_CUDA(cudaStreamWaitEvent(stream(), pos_event(pslot, 1), 0));
     // the aligned deposit uses a row pitch of N + 4 reals (16-byte aligned rows for vector reductions)
     const int rho_pitch = aligned ? N + 4 : N + 2;
     const size_t rho_bytes = B > 1 ? db : (size_t)N * N * rho_pitch * (sizeof(T));
     void *rhoD = aligned ? workspace(rho_bytes, 15) : rho;
     if (!rhoD) return 5;
     MITOS_CUDA(cudaMemsetAsync(rhoD, 0, rho_bytes, stream()));
-    e = aligned ? lattice_deposit(N, L, prec, D0, D1, D2, disp_pitch, rhoD, rho_pitch, dpos, B, bs)
-                : displace_and_deposit(N, M, L, prec, D0, D1, D2, rhoD, dpos);
+    e = aligned ? lattice_deposit(N, L, prec, D0, D1, D2, disp_pitch, rhoD, rho_pitch, dpos, B, bs, dposraw)
+                : displace_and_deposit(N, M, L, prec, D0, D1, D2, rhoD, dpos, dposraw);
     if (e) return e;
     if (dpos) {
         MITOS_CUDA(cudaEventRecord(pos_event(pslot, 0), stream()));
@@ -402,6 +426,83 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
         MITOS_CUDA(cudaEventRecord(pos_event(pslot, 1), copy_stream()));
     }
     tim.mark();
+
+    // Velocities (src/mitos.c:425-490, :865-908): the same noise through the velocity transfer
+    // function (z_source = z_ini: rescale 1, :431-436) and the -1/k^2 kernel, the velocity potential
+    // by 2LPT with the reference's velocity factors for 2LPT configurations (:453-455) or that first
+    // order potential otherwise (:457), the TSC window undone (:461-467), three derivative grids
+    // (:470-483, pitch N + 2, no on-node stencil: the gather is at displaced positions), and the
+    // TSC gather of each at the unwrapped positions.  Every workspace of S1-S4 is free again here.
+    if (want_vel) {
+        T *filtv = (T *)workspace(sizeof(T) * (n2max + 1), 116);
+        void *V0 = workspace(gb, 19), *V1 = workspace(gb, 20), *V2 = workspace(gb, 21);
+        float *dvel = (float *)workspace(pos_bytes, 110 + pslot);
+        if (!filtv || !V0 || !V1 || !V2 || !dvel) return 5;
+        if ((e = filter_launch(dtab + 3 * k_size, 1, filtv))) return e;
+        e = noise_generate(g, prec, L, st, filtv, phi);
+        if (!e) e = hermitian_planes(g, prec, phi);
+        if (e) return e;
+        if (cfg->method == MITOS_METHOD_2LPT) {
+            e = grid_hessian(g, prec, L, phi, ZOP_HESS_2LPT, nullptr, S, nullptr, 0);
+            if (e) return e;
+            reset(a);
+            a.dk = dk;
+            a.scale = 1.0;
+            a.in[0] = S;
+            a.out[0] = Sk;
+            a.rp_in = N + 2;
+            a.rho_a = 1.0;
+            e = launch_z_r2c<T>(g, a);
+            a.in[0] = Sk;
+            if (!e) e = launch_y<T>(g, YOP_PLAIN, -1, a);
+            a.in2 = phi;
+            a.scale = V / ((double)N * N * N);
+            a.f1 = F1_VEL;
+            a.f2 = F2_VEL;
+            a.window_order = 3;
+            a.out[0] = A0;
+            a.out[1] = A1;
+            a.stencil = nullptr;
+            if (!e) e = launch_x<T>(g, XOP_COMBINE_DISP, -1, a);
+        } else {
+            reset(a);
+            a.dk = dk;
+            a.scale = 1.0;
+            a.window_order = 3;
+            a.in[0] = phi;
+            a.out[0] = A0;
+            a.out[1] = A1;
+            e = launch_x<T>(g, XOP_DISP, +1, a);
+        }
+        if (e) return e;
+        reset(a);
+        a.dk = dk;
+        a.scale = 1.0;
+        a.in[0] = A0;
+        a.out[0] = B1;
+        a.out[1] = B2;
+        e = launch_y<T>(g, YOP_DISP_A, +1, a);
+        a.in[0] = A1;
+        a.out[0] = B0;
+        if (!e) e = launch_y<T>(g, YOP_STN, +1, a);
+        if (e) return e;
+        a.in[0] = B0;
+        a.in[1] = B1;
+        a.in[2] = B2;
+        a.out[0] = V0;
+        a.out[1] = V1;
+        a.out[2] = V2;
+        a.rp_out = N + 2;
+        a.scale = 1.0 / V;
+        e = launch_z_c2r<T>(g, ZOP_DISP, a);
+        if (!e) e = velocity_gather((long)M * M * M, N, L, prec, dposraw, V0, V1, V2, dvel);
+        if (e) return e;
+        // to the caller on the copy stream, behind the positions (pos_event(pslot, 1) then covers both)
+        MITOS_CUDA(cudaEventRecord(pos_event(pslot, 0), stream()));
+        MITOS_CUDA(cudaStreamWaitEvent(copy_stream(), pos_event(pslot, 0), 0));
+        MITOS_CUDA(cudaMemcpyAsync(res->vel, dvel, pos_bytes, cudaMemcpyDeviceToHost, copy_stream()));
+        MITOS_CUDA(cudaEventRecord(pos_event(pslot, 1), copy_stream()));
+    }
 
     // S6: overdensity r2c, CIC window undo, P(k) (analyse/src/mitos_read.c:364-419)
     const int *bins = bin_table(N, cfg->pk_bins, cfg->pk_linear, L);
@@ -456,7 +557,7 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
         MITOS_CUDA(cudaMemcpyAsync(h.data(), acc + cfg->pk_bins, sizeof(double) * cfg->pk_bins,
                                    cudaMemcpyDeviceToHost, stream()));
         MITOS_CUDA(cudaStreamSynchronize(stream()));
-        if (dpos) MITOS_CUDA(cudaEventSynchronize(pos_event(pslot, 1)));
+        if (dpos || want_vel) MITOS_CUDA(cudaEventSynchronize(pos_event(pslot, 1)));
         for (int i = 0; i < cfg->pk_bins; i++) {
             const double n = (double)count[i];
             if (res->pk_obs) res->pk_obs[i] = (long)count[i];
@@ -500,8 +601,15 @@ int mitos::pipeline_table(const struct ic_config *cfg, int k_size, int tau_size,
     find_tau_h(&pd, lt, &tau_index, &u_tau);
     const double *arr = delta + (long)cfg->index_src * k_size * tau_size;
     const double *tlo = arr + (long)k_size * tau_index, *thi = arr + (long)k_size * (tau_index + 1);
-    if (cfg->precision == MITOS_FP32) return run_pipeline<float>(cfg, k, tlo, thi, k_size, u_tau, res, opt);
-    if (cfg->precision == MITOS_FP64) return run_pipeline<double>(cfg, k, tlo, thi, k_size, u_tau, res, opt);
+    // the velocity transfer function's rows at the same time (used when res->vel is set)
+    const double *tvlo = nullptr, *tvhi = nullptr;
+    if (cfg->index_vel >= 0 && cfg->index_vel < n_functions) {
+        const double *va = delta + (long)cfg->index_vel * k_size * tau_size;
+        tvlo = va + (long)k_size * tau_index;
+        tvhi = va + (long)k_size * (tau_index + 1);
+    }
+    if (cfg->precision == MITOS_FP32) return run_pipeline<float>(cfg, k, tlo, thi, tvlo, tvhi, k_size, u_tau, res, opt);
+    if (cfg->precision == MITOS_FP64) return run_pipeline<double>(cfg, k, tlo, thi, tvlo, tvhi, k_size, u_tau, res, opt);
     set_error(3, "unknown precision %d", cfg->precision);
     return 3;
 }
@@ -550,7 +658,7 @@ int finish_slot(int k) {
     if (!s.busy) return 0;
     s.busy = false;
     MITOS_CUDA(cudaEventSynchronize(acc_event(k)));
-    if (s.res && s.res->pos) MITOS_CUDA(cudaEventSynchronize(pos_event(k, 1)));
+    if (s.res && (s.res->pos || s.res->vel)) MITOS_CUDA(cudaEventSynchronize(pos_event(k, 1)));
     if (!s.res) return 0;
     const double *ksum;
     const long long *count;

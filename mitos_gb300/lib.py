@@ -82,12 +82,12 @@ class ICConfig(ctypes.Structure):
                 ("k_pivot", ctypes.c_double), ("z_ini", ctypes.c_double), ("index_src", ctypes.c_int),
                 ("method", ctypes.c_int), ("ma_cycles", ctypes.c_int), ("ma_tol", ctypes.c_double),
                 ("pk_bins", ctypes.c_int), ("pk_linear", ctypes.c_int), ("precision", ctypes.c_int),
-                ("keep_outputs", ctypes.c_int)]
+                ("keep_outputs", ctypes.c_int), ("index_vel", ctypes.c_int)]
 
 
 class ICResult(ctypes.Structure):
     _fields_ = [("pk_k", _dp), ("pk_p", _dp), ("pk_obs", _lp), ("pos", _fp),
-                ("ma_iterations", ctypes.c_int), ("ma_residual", ctypes.c_double)]
+                ("ma_iterations", ctypes.c_int), ("ma_residual", ctypes.c_double), ("vel", _fp)]
 
 
 _lib = None
@@ -323,24 +323,31 @@ def cic_deposit_dg(rho, pos: np.ndarray, mass: float) -> float:
 
 # ---- fused pipeline --------------------------------------------------------------------------
 def ic_config(N, M, boxlen, seed, table, method=METHOD_2LPT, pk_bins=32, pk_linear=True,
-              precision=FP32, z_ini=31.0, ma_cycles=0, ma_tol=0.0, index_src=0) -> ICConfig:
+              precision=FP32, z_ini=31.0, ma_cycles=0, ma_tol=0.0, index_src=0, index_vel=None) -> ICConfig:
+    """index_vel: the velocity transfer function (default: the table's ``t_cdm`` when it has one)"""
+    if index_vel is None:
+        index_vel = table.index_of("t_cdm") if "t_cdm" in getattr(table, "titles", []) else -1
     return ICConfig(N, M, boxlen, seed, table.A_s, table.n_s, table.k_pivot, z_ini, index_src,
-                    method, ma_cycles, ma_tol, pk_bins, int(pk_linear), precision, 0)
+                    method, ma_cycles, ma_tol, pk_bins, int(pk_linear), precision, 0, index_vel)
 
 
-def ic_pipeline_run(cfg: ICConfig, spline: Spline, want_pos: bool = False) -> dict:
+def ic_pipeline_run(cfg: ICConfig, spline: Spline, want_pos: bool = False, want_vel: bool = False) -> dict:
     bins = cfg.pk_bins
     k = np.zeros(bins)
     p = np.zeros(bins)
     o = np.zeros(bins, np.int64)
     pos = np.zeros((cfg.M ** 3, 3), np.float32) if want_pos else None
+    vel = np.zeros((cfg.M ** 3, 3), np.float32) if want_vel else None
     res = ICResult(k.ctypes.data_as(_dp), p.ctypes.data_as(_dp), o.ctypes.data_as(_lp),
-                   pos.ctypes.data_as(_fp) if pos is not None else None, 0, 0.0)
+                   pos.ctypes.data_as(_fp) if pos is not None else None, 0, 0.0,
+                   vel.ctypes.data_as(_fp) if vel is not None else None)
     _check(load().ic_pipeline_run(ctypes.byref(cfg), ctypes.byref(spline.sp), ctypes.byref(res)))
     out = {"pk_k": k, "pk_p": p, "pk_obs": o, "ma_iterations": res.ma_iterations,
            "ma_residual": res.ma_residual}
     if pos is not None:
         out["pos"] = pos
+    if vel is not None:
+        out["vel"] = vel
     return out
 
 

@@ -13,6 +13,10 @@ ships with the reference, so this module builds an equivalent table:
 * A_s chosen so that sigma_8 (top hat, R = 8 Mpc/h) equals ``sigma8`` at z = 0 for the power
   spectrum the reference realises, P(k) = primordialPower(k) T(k)^2
   (src/primordial.c:25-33, include/fft_kernels.h:116-155).
+* transfer function ``t_cdm`` (the velocity divergence, added at load time from the stored arrays):
+  linear continuity, theta = -delta' = -f (a H / c) d_cdm in h/Mpc, with conformal time in Mpc/h.
+  The reference builds the particle velocities from such a function (``TransferFunctionVelocity``,
+  src/mitos.c:425-490).
 
 The table is written once to ``data/perturb_bbks.npz`` and loaded from there, so every machine
 uses the same bits.
@@ -117,14 +121,25 @@ def save_table(t: PerturbTable, path: str = DATA_FILE) -> None:
                                                           t.Omega_m, t.Omega_b, t.h]))
 
 
+def velocity_transfer(t: PerturbTable) -> np.ndarray:
+    """t_cdm(tau, k) = -f(tau) a(tau) H(tau) / c * d_cdm(tau, k) (h/Mpc)"""
+    a = 1.0 / (1.0 + t.redshift)
+    rate = -(t.f_growth * a * t.H_Hubble / C_KMS)
+    return rate[:, None] * t.delta[t.index_of("d_cdm")]
+
+
 def load_table(path: str = DATA_FILE) -> PerturbTable:
     z = np.load(path)
     A_s, n_s, k_pivot, sigma8, Om, Ob, h = [float(v) for v in z["scalars"]]
-    return PerturbTable(k=z["k"], log_tau=z["log_tau"], redshift=z["redshift"],
-                        D_growth=z["D_growth"], f_growth=z["f_growth"], H_Hubble=z["H_Hubble"],
-                        delta=np.ascontiguousarray(z["delta"]), titles=[str(s) for s in z["titles"]],
-                        A_s=A_s, n_s=n_s, k_pivot=k_pivot, sigma8=sigma8, Omega_m=Om, Omega_b=Ob,
-                        h=h)
+    t = PerturbTable(k=z["k"], log_tau=z["log_tau"], redshift=z["redshift"],
+                     D_growth=z["D_growth"], f_growth=z["f_growth"], H_Hubble=z["H_Hubble"],
+                     delta=np.ascontiguousarray(z["delta"]), titles=[str(s) for s in z["titles"]],
+                     A_s=A_s, n_s=n_s, k_pivot=k_pivot, sigma8=sigma8, Omega_m=Om, Omega_b=Ob,
+                     h=h)
+    if "t_cdm" not in t.titles:
+        t.delta = np.ascontiguousarray(np.concatenate([t.delta, velocity_transfer(t)[None]], axis=0))
+        t.titles = t.titles + ["t_cdm"]
+    return t
 
 
 if __name__ == "__main__":

@@ -78,12 +78,13 @@ class OrcICParams(ctypes.Structure):
                 ("sp", ctypes.POINTER(OrcPerturb)), ("index_src", ctypes.c_int),
                 ("z_ini", ctypes.c_double), ("lpt_order", ctypes.c_int),
                 ("ma_cycles", ctypes.c_int), ("pk_bins", ctypes.c_int),
-                ("pk_linear", ctypes.c_int), ("mass", ctypes.c_double)]
+                ("pk_linear", ctypes.c_int), ("mass", ctypes.c_double), ("index_vel", ctypes.c_int)]
 
 
 class OrcICOut(ctypes.Structure):
     _fields_ = [("grf", _dp), ("delta_k", _dp), ("phi_k", _dp), ("disp", _dp * 3), ("pos", _fp),
-                ("rho", _dp), ("pk_k", _dp), ("pk_p", _dp), ("pk_obs", _lp), ("ma_eps", _dp)]
+                ("rho", _dp), ("pk_k", _dp), ("pk_p", _dp), ("pk_obs", _lp), ("ma_eps", _dp),
+                ("vel", _fp)]
 
 
 class Spline:
@@ -198,10 +199,10 @@ def powerspec(N: int, boxlen: float, f1: np.ndarray, f2: np.ndarray, bins: int, 
 
 
 def ic_params(N, M, boxlen, seed, table, lpt_order=2, ma_cycles=0, pk_bins=32, pk_linear=True,
-              z_ini=31.0, mass=1.0, index_src=0):
+              z_ini=31.0, mass=1.0, index_src=0, index_vel=-1):
     return dict(N=N, M=M, boxlen=boxlen, seed=seed, table=table, lpt_order=lpt_order,
                 ma_cycles=ma_cycles, pk_bins=pk_bins, pk_linear=pk_linear, z_ini=z_ini, mass=mass,
-                index_src=index_src)
+                index_src=index_src, index_vel=index_vel)
 
 
 def _alloc_outputs(N, M, bins, want, ma_cycles):
@@ -213,6 +214,7 @@ def _alloc_outputs(N, M, bins, want, ma_cycles):
     if "disp" in want:
         for i in range(3): o[f"disp{i}"] = np.zeros((N, N, N + 2))
     if "pos" in want: o["pos"] = np.zeros((M * M * M, 3), np.float32)
+    if "vel" in want: o["vel"] = np.zeros((M * M * M, 3), np.float32)
     if "rho" in want: o["rho"] = np.zeros((N, N, N))
     if ma_cycles: o["ma_eps"] = np.zeros(ma_cycles)
     return o
@@ -232,7 +234,7 @@ def ic_pipeline(prm: dict, want=("pk",)) -> dict:
     o = _alloc_outputs(N, M, bins, want, prm["ma_cycles"])
     p = OrcICParams(N, M, prm["boxlen"], prm["seed"], OrcCosmo(t.A_s, t.n_s, t.k_pivot),
                     ctypes.pointer(sp.s), prm["index_src"], prm["z_ini"], prm["lpt_order"],
-                    prm["ma_cycles"], bins, int(prm["pk_linear"]), prm["mass"])
+                    prm["ma_cycles"], bins, int(prm["pk_linear"]), prm["mass"], prm.get("index_vel", -1))
     out = OrcICOut()
     out.grf, out.delta_k, out.phi_k = P(o.get("grf")), P(o.get("delta_k")), P(o.get("phi_k"))
     for i in range(3):
@@ -241,6 +243,7 @@ def ic_pipeline(prm: dict, want=("pk",)) -> dict:
     out.rho = P(o.get("rho"))
     out.pk_k, out.pk_p, out.pk_obs = P(o["pk_k"]), P(o["pk_p"]), P(o["pk_obs"], _lp)
     out.ma_eps = P(o.get("ma_eps"))
+    out.vel = P(o.get("vel"), _fp)
     with np.errstate(all="ignore"):
         err = lib().orc_ic_pipeline(ctypes.byref(p), ctypes.byref(out))
     assert err == 0, err

@@ -1144,7 +1144,8 @@ int orc_ic_pipeline(const struct orc_ic_params *p, struct orc_ic_out *o) {
     }
     if (o->phi_k) memcpy(o->phi_k, pot.fbox, cbytes);
 
-    /* :395-416 TSC window undo and the three displacement grids */
+    /* :425-490 the velocity grids (flux density of the velocity transfer function, its potential,
+     * three derivatives), computed after the displacement grids below from a copy of pot */
     struct orc_hermite_params hp = {3, N, L};
     grid_kernel(&pot, &pot, ORC_K_UNDO_HERMITE, &hp);
     double *disp[3];
@@ -1158,6 +1159,32 @@ int orc_ic_pipeline(const struct orc_ic_params *p, struct orc_ic_out *o) {
     }
     /* :419 */
     orc_grid_c2r(&pot);
+
+    /* :425-490 velocity grids: generatePerturbationGrid with the velocity title (rescale 1 with
+     * z_source = z_ini, :431-436), r2c (:451), 2LPT with the reference's velocity factors (:453-455)
+     * or the inverse Poisson kernel (:457), TSC window undo (:461-467), three derivatives (:470-483) */
+    double *vgrid[3] = {NULL, NULL, NULL};
+    if (p->index_vel >= 0) {
+        struct orc_transfer_params tv;
+        tv.sp = p->sp;
+        tv.index_src = p->index_vel;
+        orc_spline_find_tau(p->sp, log_tau_src, &tv.tau_index, &tv.u_tau);
+        grid_kernel(&grid, &grf, ORC_K_TRANSFER, &tv);
+        orc_grid_c2r(&grid);
+        orc_grid_r2c(&grid);
+        if (p->lpt_order == 2 && p->ma_cycles <= 0)
+            orc_solve_2lpt(&pot, &grid, &der, -0.001147273637728, 3.19354920304769E-05);
+        else
+            grid_kernel(&pot, &grid, ORC_K_INV_POISSON, NULL);
+        struct orc_hermite_params hv = {3, N, L};
+        grid_kernel(&pot, &pot, ORC_K_UNDO_HERMITE, &hv);
+        for (int i = 0; i < 3; i++) {
+            vgrid[i] = malloc(cbytes);
+            grid_kernel(&der, &pot, kid[i], NULL);
+            orc_grid_c2r(&der);
+            memcpy(vgrid[i], der.box, cbytes);
+        }
+    }
     orc_grid_free(&grf);
     orc_grid_free(&grid);
     orc_grid_free(&pot);
@@ -1168,6 +1195,19 @@ int orc_ic_pipeline(const struct orc_ic_params *p, struct orc_ic_out *o) {
     float *pos = malloc(sizeof(float) * 3 * np);
     orc_lattice(M, L, pos);
     for (int dir = 0; dir < 3; dir++) orc_displace(M, N, L, pos, disp[dir], dir);
+    /* :865-908 velocities: the TSC gather of each velocity grid at the displaced (not yet wrapped)
+     * position, stored as float */
+    if (p->index_vel >= 0) {
+#pragma omp parallel for schedule(static)
+        for (long i = 0; i < np; i++) {
+            const double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+            for (int dir = 0; dir < 3; dir++) {
+                const double v = orc_tsc_gather(vgrid[dir], N, L, x, y, z);
+                if (o->vel) o->vel[3 * i + dir] = (float)v;
+            }
+        }
+        for (int i = 0; i < 3; i++) free(vgrid[i]);
+    }
     orc_wrap_positions(np, L, pos);
     for (int i = 0; i < 3; i++) free(disp[i]);
     if (o->pos) memcpy(o->pos, pos, sizeof(float) * 3 * np);

@@ -121,6 +121,7 @@ struct orc_ic_params {
     int pk_bins;
     int pk_linear;      /* 1 = linear shells to k_Nyquist, 0 = reference log bins */
     double mass;        /* particle mass (cancels in the overdensity) */
+    int index_vel;      /* velocity transfer function (src/mitos.c:425-490), < 0: no velocities */
 };
 struct orc_ic_out {
     double *grf;        /* complex, after hermiticity + primordial power (optional) */
@@ -131,6 +132,7 @@ struct orc_ic_out {
     double *rho;        /* N^3 CIC overdensity (optional) */
     double *pk_k, *pk_p; long *pk_obs; /* bins (required) */
     double *ma_eps;     /* per-cycle reference eps (optional, ma_cycles entries) */
+    float  *vel;        /* M^3 x 3 particle velocities (optional; index_vel >= 0) */
 };
 int orc_ic_pipeline(const struct orc_ic_params *p, struct orc_ic_out *o);
 

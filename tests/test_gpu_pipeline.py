@@ -98,3 +98,49 @@ def test_async_submissions_match_synchronous_runs(table, spline):
         assert np.array_equal(o, ref["pk_obs"])
         assert np.allclose(k, ref["pk_k"], rtol=1e-12, equal_nan=True)
         assert np.allclose(p, ref["pk_p"], rtol=1e-5, equal_nan=True)
+
+
+@pytest.mark.parametrize("N,M,method", [(32, 32, ml.METHOD_2LPT), (32, 32, ml.METHOD_ZELDOVICH),
+                                        (48, 48, ml.METHOD_2LPT), (32, 16, ml.METHOD_2LPT)])
+def test_velocities_fp64_vs_oracle(N, M, method, table, spline):
+    """particle velocities (src/mitos.c:425-490, :865-908): the velocity transfer function t_cdm,
+    2LPT with the reference's velocity factors (Zel'dovich otherwise), the TSC gather at the unwrapped
+    positions; the lattice-aligned deposit (M = N) and the general one (M != N)"""
+    L = 4.0 * N
+    iv = table.index_of("t_cdm")
+    cfg = ml.ic_config(N, M, L, 42, table, method=method, pk_bins=12, precision=ml.FP64, index_vel=iv)
+    out = ml.ic_pipeline_run(cfg, spline, want_pos=True, want_vel=True)
+    ref = oracle.ic_pipeline(oracle.ic_params(N, M, L, 42, table, lpt_order=2 if method == ml.METHOD_2LPT else 1,
+                                              pk_bins=12, index_vel=iv), want=("pos", "vel", "pk"))
+    err = rel_err(out["vel"], ref["vel"])
+    print(f"N={N} M={M} method={method}: velocity rel err {err:.3e}, max abs "
+          f"{np.abs(out['vel'] - ref['vel']).max():.3e} of rms {np.sqrt(np.mean(ref['vel'] ** 2)):.3e}")
+    assert np.abs(_wrapdiff(out["pos"], ref["pos"], L)).max() < 1e-4
+    # same arithmetic: bit-identical except where a float position rounded differently (measured
+    # 0 at 32^3, 7e-10 at 48^3)
+    assert err < 1e-8, err
+
+
+def test_velocities_leave_positions_and_pk_unchanged(table, spline):
+    N, L = 64, 256.0
+    cfg = ml.ic_config(N, N, L, 9, table, pk_bins=16, precision=ml.FP32)
+    a = ml.ic_pipeline_run(cfg, spline, want_pos=True)
+    b = ml.ic_pipeline_run(cfg, spline, want_pos=True, want_vel=True)
+    assert np.array_equal(a["pos"], b["pos"])
+    assert np.array_equal(a["pk_obs"], b["pk_obs"])
+    assert np.allclose(a["pk_p"], b["pk_p"], rtol=1e-5, equal_nan=True)
+    assert np.all(np.isfinite(b["vel"])) and np.abs(b["vel"]).max() > 0
+    bad = ml.ic_config(N, N, L, 9, table, pk_bins=16, precision=ml.FP32, index_vel=7)
+    with pytest.raises(ml.MitosError):
+        ml.ic_pipeline_run(bad, spline, want_vel=True)
+
+
+def test_velocities_fp32_vs_fp64(table, spline):
+    N, L = 128, 250.0
+    o = {}
+    for prec in (ml.FP32, ml.FP64):
+        cfg = ml.ic_config(N, N, L, 7, table, pk_bins=16, precision=prec)
+        o[prec] = ml.ic_pipeline_run(cfg, spline, want_vel=True)["vel"]
+    err = rel_err(o[ml.FP32], o[ml.FP64])
+    print(f"velocities FP32 vs FP64 at 128^3: rel err {err:.3e}")
+    assert err < 2e-5, err  # measured 3.6e-6
