@@ -267,7 +267,7 @@ def ref_ic_pipeline(prm: dict, want=("pk",)) -> dict:
         prm["ma_cycles"], bins, int(prm["pk_linear"]), ctypes.c_double(prm["mass"]),
         P(o.get("grf")), P(o.get("delta_k")), P(o.get("phi_k")), P(o.get("disp0")),
         P(o.get("disp1")), P(o.get("disp2")), P(o.get("pos"), _fp), P(o.get("rho")),
-        P(o["pk_k"]), P(o["pk_p"]), P(o["pk_obs"], _lp))
+        P(o["pk_k"]), P(o["pk_p"]), P(o["pk_obs"], _lp), prm.get("index_vel", -1), P(o.get("vel"), _fp))
     assert err == 0, err
     return _finish(o)
 

@@ -68,7 +68,8 @@ int ref_ic_pipeline(int N, int M, double L, uint64_t seed, double A_s, double n_
                     double z_ini, int lpt_order, int ma_cycles, int pk_bins, int pk_linear,
                     double mass, double *out_grf, double *out_delta_k, double *out_phi_k,
                     double *out_d0, double *out_d1, double *out_d2, float *out_pos,
-                    double *out_rho, double *pk_k, double *pk_p, long *pk_obs) {
+                    double *out_rho, double *pk_k, double *pk_p, long *pk_obs, int index_vel,
+                    float *out_vel) {
     if (n_functions > 64) return 1;
     for (int i = 0; i < n_functions; i++) {
         if (!g_titles[i]) {
@@ -168,6 +169,27 @@ int ref_ic_pipeline(int N, int M, double L, uint64_t seed, double A_s, double n_
         if (outs[i]) memcpy(outs[i], derivative.box, cb);
     }
     fft_c2r_dg(&potential);
+
+    /* :425-490 velocity grids, with z_source = z_ini (rescale 1, :431-436) */
+    double *vgrid[3] = {NULL, NULL, NULL};
+    if (index_vel >= 0) {
+        snprintf(title, sizeof title, "f%d", index_vel);
+        err = generatePerturbationGrid(&cosmo, &spline, &grf, &grid, title, "", 1.0);
+        if (err) return err;
+        fft_r2c_dg(&grid);
+        if (lpt_order == 2 && ma_cycles <= 0)
+            err = solve2LPT(&potential, &grid, &derivative, -0.001147273637728, 3.19354920304769E-05);
+        else
+            fft_apply_kernel_dg(&potential, &grid, kernel_inv_poisson, NULL);
+        if (err) return err;
+        fft_apply_kernel_dg(&potential, &potential, kernel_undo_Hermite_window, &Hkp);
+        for (int i = 0; i < 3; i++) {
+            fft_apply_kernel_dg(&derivative, &potential, derivative_kernels[i], NULL);
+            fft_c2r_dg(&derivative);
+            vgrid[i] = malloc(cb);
+            memcpy(vgrid[i], derivative.box, cb);
+        }
+    }
     free_local_grid(&grf);
     free_local_grid(&grid);
     free_local_grid(&potential);
@@ -206,6 +228,35 @@ int ref_ic_pipeline(int N, int M, double L, uint64_t seed, double A_s, double n_
             else if (dir == 1) parts[i].Y -= d;
             else parts[i].Z -= d;
         }
+    }
+    /* :865-908 velocities at the displaced positions */
+    if (index_vel >= 0) {
+        for (int dir = 0; dir < 3; dir++) {
+            struct left_right_slice lrs;
+            lrs.local_slice = vgrid[dir];
+            lrs.local_NX = N;
+            lrs.local_X0 = 0;
+            lrs.left_slice = vgrid[dir];
+            lrs.left_NX = 0;
+            lrs.left_X0 = 0;
+            lrs.right_slice = vgrid[dir];
+            lrs.right_NX = 0;
+            lrs.right_X0 = 0;
+#pragma omp parallel for
+            for (long long i = 0; i < chunk_size; i++) {
+                double vel = gridTSC_dg(&lrs, parts[i].X, parts[i].Y, parts[i].Z, L, N);
+                if (dir == 0) parts[i].v_X = vel;
+                else if (dir == 1) parts[i].v_Y = vel;
+                else parts[i].v_Z = vel;
+            }
+        }
+        for (int i = 0; i < 3; i++) free(vgrid[i]);
+        if (out_vel)
+            for (long long i = 0; i < chunk_size; i++) {
+                out_vel[3 * i] = parts[i].v_X;
+                out_vel[3 * i + 1] = parts[i].v_Y;
+                out_vel[3 * i + 2] = parts[i].v_Z;
+            }
     }
     /* :1072-1077 */
     for (long long i = 0; i < chunk_size; i++) {

@@ -50,13 +50,16 @@ def test_golden_pipeline(table):
 @pytest.mark.parametrize("N,lin,lpt,ma", [(16, True, 2, 0), (32, False, 2, 0), (16, True, 1, 0),
                                           (16, False, 2, 2)])
 def test_pin_against_reference_build(table, N, lin, lpt, ma):
+    """every intermediate and the velocities (the velocity transfer function t_cdm) of the oracle
+    equal the reference's own functions bit for bit"""
     prm = oracle.ic_params(N, N, 256.0 * N / 64, 42, table, lpt_order=lpt, ma_cycles=ma,
-                           pk_bins=8, pk_linear=lin)
-    want = ("grf", "delta_k", "phi_k", "disp", "pos", "rho", "pk")
+                           pk_bins=8, pk_linear=lin, index_vel=table.index_of("t_cdm"))
+    want = ("grf", "delta_k", "phi_k", "disp", "pos", "rho", "pk", "vel")
     a = oracle.ic_pipeline(prm, want)
     b = oracle.ref_ic_pipeline(prm, want)
+    assert np.abs(a["vel"]).max() > 0
     for key in ["grf", "delta_k", "phi_k", "disp0", "disp1", "disp2", "pos", "rho", "pk_k",
-                "pk_p", "pk_obs"]:
+                "pk_p", "pk_obs", "vel"]:
         assert np.array_equal(a[key], b[key], equal_nan=True), key
 
 
