@@ -214,6 +214,19 @@ def extras(ml, table, spline, args) -> dict:
                          "vel_rms": float(np.sqrt(np.mean(pv[1].numpy()[::4096] ** 2)))}
     del pv
 
+    # bispectrum (src/calc_powerspec.c:295-508) of a 512^3 FP32 field in 16 equilateral log bins, as
+    # analyse/src/mitos_box_bispec.c calls it (the field, then the bin volumes)
+    gb_ = ml.alloc_local_grid(N, L, ml.FP32)
+    ml.generate_complex_grf(gb_, ml.rng_init(args.seed))
+    gb_.momentum_space = b"\x01"
+    ml.calc_bispectrum(gb_, 16, 16, btype=0, theta=4 * np.pi / 3)
+    t0 = time.perf_counter()
+    bsp = ml.calc_bispectrum(gb_, 16, 16, btype=0, theta=4 * np.pi / 3)
+    ml.calc_bispectrum(gb_, 16, 16, volume_mode=True, btype=0, theta=4 * np.pi / 3)
+    out["bispectrum"] = {"N": N, "bins": 16, "ms_field_and_volumes": (time.perf_counter() - t0) * 1e3,
+                         "nonempty_bins": int(np.count_nonzero(bsp["k1"]))}
+    ml.free_local_grid(gb_)
+
     # 48 realisations (16 x 64^3 / 256, 16 x 96^3 / 384, 16 x 128^3 / 512 Mpc/h; 4 Mpc/h cells),
     # seeds 1000-1047, one captured CUDA graph over 8 streams, tiles from the autotuner
     sizes = [(64, 256.0), (96, 384.0), (128, 512.0)]

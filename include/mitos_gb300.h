@@ -204,6 +204,13 @@ void calc_cross_powerspec_float_mpi(long int N, long int X0, long int NX, double
                                     const mitos_c64 *box1, const mitos_c64 *box2, int bins,
                                     double *k_in_bins, double *power_in_bins,
                                     long int *obs_in_bins);
+/* src/calc_powerspec.c:295-508 (include/calc_powerspec.h:40-43): the bispectrum B(k1, k2, k3),
+ * k1 = k2 in each of `bins` log bins, k3 from theta (type 0) or the value k3 (type 1) in `bins3`
+ * log bins; volume_mode 1 masks ones (fbox ignored) for the bin volumes.  fbox may be a host or
+ * device pointer; outputs are host arrays; nothing is printed. */
+void calc_bispectrum(int N, double boxlen, const mitos_c128 *fbox, int bins, int bins3,
+                     double *k1_in_bins, double *k2_in_bins, double *k3_in_bins, double *bispectrum,
+                     int volume_mode, int type, double theta, double k3);
 
 /* ==== entry points with no reference counterpart ====================================== */
 
@@ -311,6 +318,11 @@ int ic_pipeline_run_table(const struct ic_config *cfg, int k_size, int tau_size,
  * library until exit); more bins return status 3.  The array is shared by all calls and cleared
  * by each: calls whose GPU work overlaps race.  The first call on a device looks up the array's
  * address (cudaGetSymbolAddress); make it before any stream capture.  Outputs are host arrays. */
+/* calc_bispectrum on a momentum-space grid of either precision (no reference counterpart);
+ * returns 0, or 1 (no grid), 2 (not in momentum space), 3, 4, 5. */
+int calc_bispectrum_dg(const struct distributed_grid *dg, int bins, int bins3, double *k1_in_bins,
+                       double *k2_in_bins, double *k3_in_bins, double *bispectrum, int volume_mode,
+                       int type, double theta, double k3);
 int calc_cross_powerspec_noalloc(int N, double boxlen, const void *dev_box1, const void *dev_box2,
                                  int precision, int bins, int linear, double *k_in_bins,
                                  double *power_in_bins, long *obs_in_bins);

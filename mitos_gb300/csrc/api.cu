@@ -603,6 +603,43 @@ extern "C" void calc_cross_powerspec_float_mpi(long int N, long int X0, long int
     for (int i = 0; i < bins; i++) obs_in_bins[i] = (long)n[i];
 }
 
+// ==== bispectrum (src/calc_powerspec.c:295-508) ===============================================
+extern "C" void calc_bispectrum(int N, double boxlen, const mitos_c128 *fbox, int bins, int bins3, double *k1_in_bins,
+                                double *k2_in_bins, double *k3_in_bins, double *bispectrum, int volume_mode, int type,
+                                double theta, double k3) {
+    const void *d = nullptr;
+    if (!volume_mode && fbox) {
+        d = fbox;
+        if (!is_device_ptr(fbox)) {
+            const size_t bytes = (size_t)N * N * (N / 2 + 1) * csize(MITOS_FP64);
+            void *t = workspace(bytes, 20);
+            if (!t) return;
+            if (cudaMemcpyAsync(t, fbox, bytes, cudaMemcpyHostToDevice, stream()) != cudaSuccess) {
+                check_cuda(cudaGetLastError(), "bispectrum input");
+                return;
+            }
+            d = t;
+        }
+    }
+    bispectrum_run(N, boxlen, MITOS_FP64, d, bins, bins3, k1_in_bins, k2_in_bins, k3_in_bins, bispectrum, volume_mode,
+                   type, theta, k3);
+}
+
+extern "C" int calc_bispectrum_dg(const struct distributed_grid *dg, int bins, int bins3, double *k1_in_bins,
+                                  double *k2_in_bins, double *k3_in_bins, double *bispectrum, int volume_mode,
+                                  int type, double theta, double k3) {
+    if (!dg || !dg->fbox) {
+        set_error(1, "grid not allocated");
+        return 1;
+    }
+    if (!volume_mode && !dg->momentum_space) {
+        set_error(2, "grid not in momentum space");
+        return 2;
+    }
+    return bispectrum_run(dg->N, dg->boxlen, dg->precision, volume_mode ? nullptr : dg->fbox, bins, bins3, k1_in_bins,
+                          k2_in_bins, k3_in_bins, bispectrum, volume_mode, type, theta, k3);
+}
+
 // ==== CIC ====================================================================================
 extern "C" int cic_deposit_dg(struct distributed_grid *rho, const float *pos, long n, double mass,
                               double *total_mass) {

@@ -1,0 +1,165 @@
+// bispectrum.cu -- calc_bispectrum (src/calc_powerspec.c:295-508) on the GPU.  For each log bin i
+// (k1 = k2 in bin i of `bins`; k3 in the bin of `bins3` picked by theta, type 0, or by the value k3,
+// type 1): one pass masks the field to both shells (ones in volume mode) and sums their wavenumbers
+// and multiplicities, the library's c2r takes both masks to real space (/ V), and a reduction sums
+// delta_1^2 delta_3 over the N^3 cells.  The bin of every |n|^2 comes from the same table as
+// calc_cross_powerspec's log bins (float u, src/calc_powerspec.c:62).  Empty bins keep zeros; the
+// reference's per-bin printf is not reproduced.
+#include <math.h>
+#include <string.h>
+
+#include <vector>
+
+#include "context.cuh"
+#include "grids.cuh"
+
+namespace mitos {
+
+// acc: [k1 sum, k3 sum, k1 multiplicity, k3 multiplicity]
+template <typename T>
+__global__ void k_bispec_mask(int N, double dk, const cplx<T> *__restrict__ f, const int *__restrict__ tab1,
+                              const int *__restrict__ tab3, int b1, int b3, int volume, cplx<T> *__restrict__ o1,
+                              cplx<T> *__restrict__ o3, double *acc) {
+    const int H = N / 2 + 1;
+    const long total = (long)N * N * H;
+    double s1 = 0, s3 = 0, c1 = 0, c3 = 0;
+    for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < total; id += (long)gridDim.x * blockDim.x) {
+        const int z = (int)(id % H);
+        const long xy = id / H;
+        const int y = (int)(xy % N), x = (int)(xy / N);
+        const int jx = kint(x, N), jy = kint(y, N);
+        const long n2 = (long)jx * jx + (long)jy * jy + (long)z * z;
+        cplx<T> v1 = mk<T>(0, 0), v3 = mk<T>(0, 0);
+        if (n2 > 0) {
+            const int bb1 = tab1[n2], bb3 = tab3[n2];
+            if (bb1 == b1 || bb3 == b3) {
+                const cplx<T> val = volume ? mk<T>(1, 0) : f[id];
+                const double mult = (z == 0 || z == N / 2) ? 1.0 : 2.0;
+                // fft_wavevector's k (src/fft.c:29-35), without contractions
+                const double kx = __dmul_rn((double)jx, dk), ky = __dmul_rn((double)jy, dk),
+                             kz = __dmul_rn((double)z, dk);
+                const double k = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(kx, kx), __dmul_rn(ky, ky)), __dmul_rn(kz, kz)));
+                if (bb1 == b1) {
+                    v1 = val;
+                    s1 += mult * k;
+                    c1 += mult;
+                }
+                if (bb3 == b3) {
+                    v3 = val;
+                    s3 += mult * k;
+                    c3 += mult;
+                }
+            }
+        }
+        o1[id] = v1;
+        o3[id] = v3;
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        s1 += __shfl_down_sync(0xffffffffu, s1, off);
+        s3 += __shfl_down_sync(0xffffffffu, s3, off);
+        c1 += __shfl_down_sync(0xffffffffu, c1, off);
+        c3 += __shfl_down_sync(0xffffffffu, c3, off);
+    }
+    if ((threadIdx.x & 31) == 0 && (c1 != 0 || c3 != 0)) {
+        atomicAdd(acc, s1);
+        atomicAdd(acc + 1, s3);
+        atomicAdd(acc + 2, c1);
+        atomicAdd(acc + 3, c3);
+    }
+}
+
+// sum of m1^2 m3 over the N^3 cells of two padded real grids (row pitch N + 2)
+template <typename T>
+__global__ void k_triple_sum(int N, const T *__restrict__ m1, const T *__restrict__ m3, double *out) {
+    const long total = (long)N * N * N;
+    T s = 0;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        const long o = (i / N) * (N + 2) + i % N;
+        const T a = m1[o];
+        s += a * a * m3[o];
+    }
+    double d = (double)s;
+    for (int off = 16; off > 0; off >>= 1) d += __shfl_down_sync(0xffffffffu, d, off);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out, d);
+}
+
+int bispectrum_run(int N, double boxlen, int prec, const void *fbox, int bins, int bins3, double *k1_in_bins,
+                   double *k2_in_bins, double *k3_in_bins, double *bispectrum, int volume_mode, int type,
+                   double theta, double k3) {
+    if (bins < 1 || bins3 < 1 || (!fbox && !volume_mode)) {
+        set_error(1, "calc_bispectrum: bins >= 1, bins3 >= 1 and a field (outside volume mode) needed");
+        return 1;
+    }
+    const GridGeom *gp = geom(N, prec);
+    if (!gp) return 3;
+    const GridGeom &g = *gp;
+    const size_t gb = (size_t)g.cells * csize(prec);
+    const int *tab1 = bin_table(N, bins, 0, boxlen), *tab3 = bin_table(N, bins3, 0, boxlen);
+    void *o1 = workspace(gb, 30), *o3 = workspace(gb, 31), *m1 = workspace(gb, 32), *m3 = workspace(gb, 33);
+    double *acc = (double *)workspace(sizeof(double) * 5, 34);
+    if (!tab1 || !tab3 || !o1 || !o3 || !m1 || !m3 || !acc) return 5;
+    const double dk = 2 * M_PI / boxlen;
+    const double max_k = sqrt(3) * dk * N / 2;
+    const double min_k = dk;
+    const double log_max_k = log(max_k);
+    const double log_min_k = log(min_k);
+    for (int i = 0; i < bins; i++) {
+        k1_in_bins[i] = 0;
+        k2_in_bins[i] = 0;
+        k3_in_bins[i] = 0;
+        bispectrum[i] = 0;
+    }
+    const long total = (long)N * N * (N / 2 + 1);
+    int blocks = (int)((total + 255) / 256);
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    for (int i = 0; i < bins; i++) {
+        // src/calc_powerspec.c:347-369, host libm as in the reference
+        int required_bin3;
+        if (type == 0) {
+            const double k1 = exp((i + 0.5) * (log_max_k - log_min_k) / (bins3 - 1) + log_min_k);
+            const double k2 = exp((i + 0.5) * (log_max_k - log_min_k) / (bins3 - 1) + log_min_k);
+            const double required_k3 = sqrt(k1 * k1 + k2 * k2 + 2 * k1 * k2 * cos(theta));
+            const float u3 = (log(required_k3) - log_min_k) / (log_max_k - log_min_k);
+            required_bin3 = (int)floor((bins3 - 1) * u3);
+        } else if (type == 1) {
+            const float u3 = (log(k3) - log_min_k) / (log_max_k - log_min_k);
+            required_bin3 = (int)floor((bins3 - 1) * u3);
+        } else {
+            required_bin3 = 0;
+        }
+        MITOS_CUDA(cudaMemsetAsync(acc, 0, sizeof(double) * 5, stream()));
+        launch_begin("bispec_mask");
+        if (prec == MITOS_FP32)
+            k_bispec_mask<float><<<blocks, 256, 0, stream()>>>(N, dk, (const float2 *)fbox, tab1, tab3, i, required_bin3,
+                                                               volume_mode, (float2 *)o1, (float2 *)o3, acc);
+        else
+            k_bispec_mask<double><<<blocks, 256, 0, stream()>>>(N, dk, (const double2 *)fbox, tab1, tab3, i,
+                                                                required_bin3, volume_mode, (double2 *)o1,
+                                                                (double2 *)o3, acc);
+        count_launch();
+        MITOS_LAUNCH_CHECK("bispectrum mask");
+        double h[5];
+        MITOS_CUDA(cudaMemcpyAsync(h, acc, sizeof(double) * 4, cudaMemcpyDeviceToHost, stream()));
+        MITOS_CUDA(cudaStreamSynchronize(stream()));
+        if (h[2] == 0 || h[3] == 0) continue;  // src/calc_powerspec.c:436
+        int e = grid_c2r(g, prec, boxlen, o1, m1);
+        if (!e) e = grid_c2r(g, prec, boxlen, o3, m3);
+        if (e) return e;
+        launch_begin("bispec_sum");
+        if (prec == MITOS_FP32)
+            k_triple_sum<float><<<152 * 8, 256, 0, stream()>>>(N, (const float *)m1, (const float *)m3, acc + 4);
+        else
+            k_triple_sum<double><<<152 * 8, 256, 0, stream()>>>(N, (const double *)m1, (const double *)m3, acc + 4);
+        count_launch();
+        MITOS_LAUNCH_CHECK("bispectrum sum");
+        MITOS_CUDA(cudaMemcpyAsync(h + 4, acc + 4, sizeof(double), cudaMemcpyDeviceToHost, stream()));
+        MITOS_CUDA(cudaStreamSynchronize(stream()));
+        bispectrum[i] = h[4];
+        k1_in_bins[i] = h[0] / h[2];
+        k2_in_bins[i] = h[0] / h[2];
+        k3_in_bins[i] = h[1] / h[3];
+    }
+    return 0;
+}
+
+}  // namespace mitos

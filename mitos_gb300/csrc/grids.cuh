@@ -35,6 +35,10 @@ struct PipeOpts {
     int *iters = nullptr;        // async: Monge-Ampere cycles and residual, filled on the host
     double *last_rel = nullptr;
 };
+// calc_bispectrum on a device field of the precision (fbox may be null in volume mode)
+int bispectrum_run(int N, double boxlen, int prec, const void *fbox, int bins, int bins3, double *k1_in_bins,
+                   double *k2_in_bins, double *k3_in_bins, double *bispectrum, int volume_mode, int type,
+                   double theta, double k3);
 // the xoshiro256** start state of a seed (splitmix64, as the reference seeds Seed + rank 0)
 void seed_state(uint64_t seed, uint64_t st[4]);
 int pipeline_table(const struct ic_config *cfg, int k_size, int tau_size, int n_functions, const double *k,

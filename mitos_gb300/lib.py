@@ -331,6 +331,15 @@ def ic_config(N, M, boxlen, seed, table, method=METHOD_2LPT, pk_bins=32, pk_line
                     method, ma_cycles, ma_tol, pk_bins, int(pk_linear), precision, 0, index_vel)
 
 
+def calc_bispectrum(g, bins, bins3, volume_mode=False, btype=0, theta=0.0, k3=0.0) -> dict:
+    """calc_bispectrum_dg on a momentum-space grid (either precision)"""
+    k1, k2, k3o, b = (np.zeros(bins) for _ in range(4))
+    _check(load().calc_bispectrum_dg(ctypes.byref(g), bins, bins3, k1.ctypes.data_as(_dp), k2.ctypes.data_as(_dp),
+                                     k3o.ctypes.data_as(_dp), b.ctypes.data_as(_dp), int(volume_mode), int(btype),
+                                     ctypes.c_double(theta), ctypes.c_double(k3)))
+    return {"k1": k1, "k2": k2, "k3": k3o, "B": b}
+
+
 def ic_pipeline_run(cfg: ICConfig, spline: Spline, want_pos: bool = False, want_vel: bool = False) -> dict:
     bins = cfg.pk_bins
     k = np.zeros(bins)

@@ -272,6 +272,32 @@ def ref_ic_pipeline(prm: dict, want=("pk",)) -> dict:
     return _finish(o)
 
 
+def _bispec_args(N, bins):
+    return [np.zeros(bins) for _ in range(4)]
+
+
+def bispectrum(N, boxlen, fbox, bins, bins3, volume_mode=False, btype=0, theta=0.0, k3=0.0) -> dict:
+    """orc_bispectrum (src/calc_powerspec.c:295-508 restated); fbox complex (N, N, N/2+1)"""
+    buf = None if fbox is None else np.ascontiguousarray(np.stack([fbox.real, fbox.imag], -1), np.float64)
+    k1, k2, k3o, b = _bispec_args(N, bins)
+    if buf is None:
+        buf = np.zeros((N, N, N // 2 + 1, 2))
+    lib().orc_bispectrum(N, ctypes.c_double(boxlen), P(buf), bins, bins3, P(k1), P(k2), P(k3o), P(b),
+                         int(volume_mode), int(btype), ctypes.c_double(theta), ctypes.c_double(k3))
+    return {"k1": k1, "k2": k2, "k3": k3o, "B": b}
+
+
+def ref_bispectrum(N, boxlen, fbox, bins, bins3, volume_mode=False, btype=0, theta=0.0, k3=0.0) -> dict:
+    """the reference's own calc_bispectrum (needs the _ref build)"""
+    buf = np.zeros((N, N, N // 2 + 1, 2)) if fbox is None else \
+        np.ascontiguousarray(np.stack([fbox.real, fbox.imag], -1), np.float64)
+    k1, k2, k3o, b = _bispec_args(N, bins)
+    ref_lib().calc_bispectrum(N, ctypes.c_double(boxlen), None if fbox is None else P(buf), bins, bins3,
+                              P(k1), P(k2), P(k3o), P(b), int(volume_mode), int(btype), ctypes.c_double(theta),
+                              ctypes.c_double(k3))
+    return {"k1": k1, "k2": k2, "k3": k3o, "B": b}
+
+
 def ref_grf(N: int, boxlen: float, seed: int, hermitian: bool = True) -> np.ndarray:
     buf = np.zeros((N, N, N // 2 + 1, 2))
     ref_lib().ref_grf(N, ctypes.c_double(boxlen), ctypes.c_uint64(seed), int(hermitian), P(buf))

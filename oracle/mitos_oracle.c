@@ -1016,6 +1016,94 @@ static inline int log_bin_k(double k, int bins, double log_min_k, double log_max
     return floor((bins - 1) * u);
 }
 
+/* calc_bispectrum: src/calc_powerspec.c:295-508.  For each log bin i (k1 = k2 in bin i; k3 in the
+ * bin of bins3 log bins picked by theta (type 0) or by the value k3 (type 1)), the field masked to
+ * each shell (or ones in volume mode) to real space (c2r / V), and sum delta_1^2 delta_3 over the
+ * N^3 cells.  Empty bins keep zeros.  (The reference also prints a line per bin.) */
+void orc_bispectrum(int N, double boxlen, const double *fbox, int bins, int bins3, double *k1_in_bins,
+                    double *k2_in_bins, double *k3_in_bins, double *bispectrum, int volume_mode, int type,
+                    double theta, double k3) {
+    const double dk = 2 * M_PI / boxlen;
+    const double max_k = sqrt(3) * dk * N / 2;
+    const double min_k = dk;
+    const double log_max_k = log(max_k);
+    const double log_min_k = log(min_k);
+    for (int i = 0; i < bins; i++) { k1_in_bins[i] = 0; k2_in_bins[i] = 0; k3_in_bins[i] = 0; bispectrum[i] = 0; }
+    const long H = N / 2 + 1, cn = (long)N * N * H;
+    double *fbox1 = malloc(sizeof(double) * 2 * cn), *fbox3 = malloc(sizeof(double) * 2 * cn);
+    double *m1 = malloc(sizeof(double) * N * N * (N + 2)), *m3 = malloc(sizeof(double) * N * N * (N + 2));
+    for (int i = 0; i < bins; i++) {
+        double k1_mean = 0., k3_mean = 0.;
+        long long k1_obs = 0, k3_obs = 0;
+        const int required_bin1 = i;
+        int required_bin3;
+        if (type == 0) {
+            double k1 = exp((i + 0.5) * (log_max_k - log_min_k) / (bins3 - 1) + log_min_k);
+            double k2 = exp((i + 0.5) * (log_max_k - log_min_k) / (bins3 - 1) + log_min_k);
+            double required_k3 = sqrt(k1 * k1 + k2 * k2 + 2 * k1 * k2 * cos(theta));
+            float u3 = (log(required_k3) - log_min_k) / (log_max_k - log_min_k);
+            required_bin3 = floor((bins3 - 1) * u3);
+        } else if (type == 1) {
+            float u3 = (log(k3) - log_min_k) / (log_max_k - log_min_k);
+            required_bin3 = floor((bins3 - 1) * u3);
+        } else {
+            required_bin3 = 0;
+        }
+        double kx, ky, kz, k;
+        for (int x = 0; x < N; x++)
+            for (int y = 0; y < N; y++)
+                for (int z = 0; z <= N / 2; z++) {
+                    orc_wavevector(x, y, z, N, dk, &kx, &ky, &kz, &k);
+                    const long id = idx_half(N, x, y, z);
+                    if (k == 0) {
+                        fbox1[2 * id] = fbox1[2 * id + 1] = 0;
+                        fbox3[2 * id] = fbox3[2 * id + 1] = 0;
+                        continue;
+                    }
+                    const float u = (log(k) - log_min_k) / (log_max_k - log_min_k);
+                    const int bin = floor((bins - 1) * u);
+                    const int bin3 = floor((bins3 - 1) * u);
+                    const int multiplicity = (z == 0 || z == N / 2) ? 1 : 2;
+                    if (bin == required_bin1) {
+                        fbox1[2 * id] = volume_mode ? 1.0 : fbox[2 * id];
+                        fbox1[2 * id + 1] = volume_mode ? 0.0 : fbox[2 * id + 1];
+                        k1_mean += multiplicity * k;
+                        k1_obs += multiplicity;
+                    } else {
+                        fbox1[2 * id] = fbox1[2 * id + 1] = 0;
+                    }
+                    if (bin3 == required_bin3) {
+                        fbox3[2 * id] = volume_mode ? 1.0 : fbox[2 * id];
+                        fbox3[2 * id + 1] = volume_mode ? 0.0 : fbox[2 * id + 1];
+                        k3_mean += multiplicity * k;
+                        k3_obs += multiplicity;
+                    } else {
+                        fbox3[2 * id] = fbox3[2 * id + 1] = 0;
+                    }
+                }
+        if (k1_obs == 0 || k3_obs == 0) continue;
+        k1_mean /= k1_obs;
+        k3_mean /= k3_obs;
+        orc_fft_c2r(N, boxlen, fbox1, m1, N + 2);
+        orc_fft_c2r(N, boxlen, fbox3, m3, N + 2);
+        double sum = 0.;
+        for (int x = 0; x < N; x++)
+            for (int y = 0; y < N; y++)
+                for (int z = 0; z < N; z++) {
+                    const long id = ((long)x * N + y) * (N + 2) + z;
+                    sum += m1[id] * m1[id] * m3[id];
+                }
+        bispectrum[i] = sum;
+        k1_in_bins[i] = k1_mean;
+        k2_in_bins[i] = k1_mean;
+        k3_in_bins[i] = k3_mean;
+    }
+    free(fbox1);
+    free(fbox3);
+    free(m1);
+    free(m3);
+}
+
 /* calc_cross_powerspec: src/calc_powerspec.c:32-90 */
 void orc_powerspec_log(int N, double boxlen, const double *f1, const double *f2, int bins,
                        double *k_in_bins, double *power_in_bins, long *obs_in_bins) {

@@ -104,6 +104,9 @@ void orc_powerspec_log(int N, double boxlen, const double *f1, const double *f2,
 void orc_powerspec_lin(int N, double boxlen, const double *f1, const double *f2, int bins,
                        double *k_in_bins, double *power_in_bins, long *obs_in_bins);
 int  orc_lin_bin(int N, int bins, long n2);
+void orc_bispectrum(int N, double boxlen, const double *fbox, int bins, int bins3, double *k1_in_bins,
+                    double *k2_in_bins, double *k3_in_bins, double *bispectrum, int volume_mode, int type,
+                    double theta, double k3);
 int  orc_log_bin(int N, double boxlen, int bins, long n2);
 
 /* ---- the whole initial-condition pipeline (src/mitos.c:205-422,794-863 followed by

@@ -155,3 +155,18 @@ def test_linear_bins_integer_exact():
             # shell b holds modes with b * (N/2)/bins <= |n| < (b+1) * (N/2)/bins
             w = (N / 2) / bins
             assert b * w <= np.sqrt(n2) + 1e-12 and np.sqrt(n2) < (b + 1) * w + 1e-12
+
+
+@pytest.mark.skipif(oracle.ref_lib() is None, reason="reference build not present here")
+@pytest.mark.parametrize("btype,vol", [(0, False), (1, False), (0, True)])
+def test_pin_bispectrum_against_reference_build(btype, vol):
+    """orc_bispectrum equals the reference's calc_bispectrum (src/calc_powerspec.c:295-508) bit for
+    bit: equilateral (type 0, theta = 4 pi / 3), fixed k3 (type 1) and the bin volumes"""
+    N, L = 16, 64.0
+    f = _smooth_grf(N, L, 5)
+    args = dict(bins=8, bins3=8, volume_mode=vol, btype=btype, theta=4 * np.pi / 3, k3=0.3)
+    a = oracle.bispectrum(N, L, None if vol else f, **args)
+    b = oracle.ref_bispectrum(N, L, None if vol else f, **args)
+    assert np.any(a["B"] != 0)
+    for key in ("k1", "k2", "k3", "B"):
+        assert np.array_equal(a[key], b[key]), key
