@@ -212,6 +212,40 @@ def extras(ml, table, spline, args) -> dict:
     out["velocities"] = {"ms_per_ic": msv, "ic_per_s": 1e3 / msv,
                          "vel_gather_ms": sum(vg) / max(len(vg), 1),
                          "vel_rms": float(np.sqrt(np.mean(pv[1].numpy()[::4096] ** 2)))}
+
+    # thermal motion (src/mitos.c:910-1064 without Firebolt) of a 512^3 species: Fermi-Dirac at the
+    # relic neutrino temperature, 0.06 eV, km/s.  The kernel alone on device velocities (7 draws, one
+    # sampler lookup and three Box-Muller normals a particle; 24 bytes read and written), FP32 and FP64,
+    # then the IC with positions, velocities and thermal motion
+    t_nu = 1.9517578 * 8.617333262e-5
+    smp = ml.thermal_sampler(ml.FERMION, t_nu)
+    dv = torch.zeros((N ** 3, 3), dtype=torch.float32, device="cuda")
+    st0 = np.array(list(ml.rng_init(args.seed).s), np.uint64)
+    th = {}
+    for name, prec in (("fp32", ml.FP32), ("fp64", ml.FP64)):
+        ml.set_precision(prec)
+        ml.thermal_velocities(smp, st0, dv, 0.06, 1 / 32.0, 299792.458)
+        ml.kernel_timing(True)
+        for i in range(3):
+            ml.thermal_velocities(smp, st0, dv, 0.06, 1 / 32.0, 299792.458)
+        kt = ml.kernel_times()
+        ml.kernel_timing(False)
+        tk = [t for n_, t in kt if n_ == "thermal"]
+        ms = sum(tk) / max(len(tk), 1)
+        th[name] = {"kernel_ms": ms, "particles_per_s": N ** 3 / (ms * 1e-3),
+                    "GB_per_s": 24.0 * N ** 3 / (ms * 1e-3) / 1e9}
+    ml.set_precision(ml.FP64)
+    ml.thermal_sampler_free(smp)
+    del dv
+    ct = ml.ic_config(N, N, L, args.seed, table, method=ml.METHOD_2LPT, pk_bins=args.bins, pk_linear=True,
+                      precision=ml.FP32, thermal=ml.FERMION, thermal_M_eV=0.06, thermal_T_eV=t_nu,
+                      speed_of_light=299792.458)
+    ml._check(ml.load().ic_pipeline_run(ctypes.byref(ct), ctypes.byref(spline.sp), ctypes.byref(rv)))
+    ml.timer_start()
+    for i in range(3):
+        ml._check(ml.load().ic_pipeline_run(ctypes.byref(ct), ctypes.byref(spline.sp), ctypes.byref(rv)))
+    th["ic_ms_with_thermal"] = ml.timer_stop() / 3
+    out["thermal"] = th
     del pv
 
     # bispectrum (src/calc_powerspec.c:295-508) of a 512^3 FP32 field in 16 equilateral log bins, as

@@ -15,7 +15,8 @@
  *   - One rank: NX = N, X0 = 0.  MPI_Comm is kept as an opaque pointer-sized type.
  *   - Functions return an int status instead of exiting: 0 ok, 1 shape mismatch, 2 not in
  *     momentum space, 3 unsupported kernel callback or size, 4 CUDA error, 5 out of memory,
- *     6 bounded wait timed out, 7 no convergence.  mitos_last_error() describes the last one.
+ *     6 bounded wait timed out, 7 no convergence, 8 invalid value drawn.  mitos_last_error()
+ *     describes the last one.
  *   - Every entry point is synchronous on return (its work on the library stream is done).
  */
 #ifndef MITOS_GB300_H
@@ -278,6 +279,13 @@ struct ic_config {
     int keep_outputs;   /* 1: keep the displacement grids, positions and density on the device */
     int index_vel;      /* velocity transfer function (TransferFunctionVelocity, src/mitos.c:425-490);
                            used when res->vel is set */
+    /* thermal motion on top of the velocities (ThermalMotionType, src/mitos.c:910-1064, the branch
+     * without Firebolt); used when res->vel is set */
+    int thermal;                /* 0 none, 1 "fermion" (fd_pdf), 2 "boson" (be_pdf) */
+    double thermal_M_eV;        /* MicroscopicMass_eV */
+    double thermal_T_eV;        /* MicroscopyTemperature * kBoltzmann / ElectronVolt */
+    double speed_of_light;      /* us.SpeedOfLight in internal units */
+    uint64_t thermal_draw_offset; /* draws taken after the white noise by earlier thermal species */
 };
 struct ic_result {
     double *pk_k;       /* host [pk_bins] */
@@ -289,7 +297,8 @@ struct ic_result {
     float *vel;         /* optional host [M^3 * 3]: particle velocities (src/mitos.c:865-908): the TSC
                            gather of the velocity grids at the displaced positions; the velocity
                            potential from 2LPT with the reference's velocity factors (:453-455) for
-                           2LPT configurations, else the inverse Poisson kernel (:457) */
+                           2LPT configurations, else the inverse Poisson kernel (:457); plus the
+                           thermal motion when cfg->thermal is set */
 };
 int ic_pipeline_run(const struct ic_config *cfg, const struct perturb_spline *spline,
                     struct ic_result *res);
@@ -309,6 +318,53 @@ int ic_pipeline_run_table(const struct ic_config *cfg, int k_size, int tau_size,
                           const double *redshift, const double *D_growth, const double *delta,
                           struct ic_result *res);
 
+/* calc_bispectrum on a momentum-space grid of either precision (no reference counterpart);
+ * returns 0, or 1 (no grid), 2 (not in momentum space), 3, 4, 5. */
+int calc_bispectrum_dg(const struct distributed_grid *dg, int bins, int bins3, double *k1_in_bins,
+                       double *k2_in_bins, double *k3_in_bins, double *bispectrum, int volume_mode,
+                       int type, double theta, double k3);
+
+/* ---- thermal motion: src/random.c:87-289 and the loop of src/mitos.c:928-1064 ---------------- */
+#ifndef RANDOM_H
+/* include/random.h:43-81 */
+typedef double (*pdf)(double x, void *params);
+struct interval {
+    int id;
+    double l, r;
+    double Fl, Fr;
+    double a0, a1, a2, a3;
+    double error;
+    int nid;
+};
+struct sampler {
+    double norm;
+    double xl, xr;
+    pdf f;
+    void *params;
+    struct interval *intervals;
+    int intervalNum;
+    int I_max;
+    double *index;
+};
+#endif
+/* The thermal-motion loop of src/mitos.c:928-965,1054-1062 (without Firebolt) on the GPU, for n
+ * particles of one species in id order: seven draws a particle from *state (samplerCustom of s,
+ * then three sampleNorm), vel[i*stride + c] += n_c p / (a_ini M_eV) speed_of_light.  s is a sampler
+ * made by the reference's initSampler (its pieces in order, as initSampler leaves them) or by
+ * thermal_sampler_init.  vel is host or device memory (n particles, `stride` floats apart: 3 for
+ * packed velocities, 10 for the v_X of struct particle).  *state advances by 7 n draws, as the
+ * reference loop leaves it.  Every draw is the reference's; FP64 (mitos_set_precision) evaluates
+ * it with the reference's operations.  Returns 0, 1, 3 (a sampler not in order), 5, or 8 (an
+ * invalid momentum, where the reference exits). */
+int thermal_velocities(const struct sampler *s, rng_state *state, long n, double M_eV, double a_ini,
+                       double speed_of_light, float *vel, long stride);
+/* initSampler (src/random.c:87-209) for fd_pdf (kind 1) or be_pdf (kind 2) on the domain
+ * src/mitos.c:645-668 sets up ([1e-10, 15] T_eV, mu = 0), built on the host; no reference
+ * counterpart under this name.  f and params are left NULL; free with thermal_sampler_free (or the
+ * reference's cleanSampler). */
+int thermal_sampler_init(struct sampler *s, int kind, double T_eV);
+int thermal_sampler_free(struct sampler *s);
+
 /* P(k) binning that allocates no device memory.  No counterpart in the reference: for callers
  * that must not allocate device memory in their loop, because another allocator already holds
  * the device's memory or because cudaMalloc / cudaFree would synchronise a streaming pipeline.
@@ -318,11 +374,6 @@ int ic_pipeline_run_table(const struct ic_config *cfg, int k_size, int tau_size,
  * library until exit); more bins return status 3.  The array is shared by all calls and cleared
  * by each: calls whose GPU work overlaps race.  The first call on a device looks up the array's
  * address (cudaGetSymbolAddress); make it before any stream capture.  Outputs are host arrays. */
-/* calc_bispectrum on a momentum-space grid of either precision (no reference counterpart);
- * returns 0, or 1 (no grid), 2 (not in momentum space), 3, 4, 5. */
-int calc_bispectrum_dg(const struct distributed_grid *dg, int bins, int bins3, double *k1_in_bins,
-                       double *k2_in_bins, double *k3_in_bins, double *bispectrum, int volume_mode,
-                       int type, double theta, double k3);
 int calc_cross_powerspec_noalloc(int N, double boxlen, const void *dev_box1, const void *dev_box2,
                                  int precision, int bins, int linear, double *k_in_bins,
                                  double *power_in_bins, long *obs_in_bins);

@@ -41,6 +41,11 @@ int bispectrum_run(int N, double boxlen, int prec, const void *fbox, int bins, i
                    double theta, double k3);
 // the xoshiro256** start state of a seed (splitmix64, as the reference seeds Seed + rank 0)
 void seed_state(uint64_t seed, uint64_t st[4]);
+// thermal motion of one species (thermal.cu): n particles from the stream of seed_state advanced by
+// `skip` draws, added to the device velocities (n x stride floats); *derr (device) gets bit 0 for an
+// invalid momentum
+int thermal_add(int prec, long n, const uint64_t seed_state[4], unsigned long long skip, int kind, double T_eV,
+                double M_eV, double a_ini, double c, float *dvel, long stride, int *derr);
 int pipeline_table(const struct ic_config *cfg, int k_size, int tau_size, int n_functions, const double *k,
                    const double *log_tau, const double *redshift, const double *D_growth, const double *delta,
                    struct ic_result *res, const PipeOpts *opt);

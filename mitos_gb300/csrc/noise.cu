@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "context.cuh"
+#include "rng.cuh"
 
 namespace mitos {
 
@@ -150,22 +151,11 @@ void rng_jump(uint64_t st[4], unsigned long long n) {
     memcpy(st, out, sizeof out);
 }
 
-// per-N table of column polynomials (device), 4 x uint64 per column
-static std::map<int, uint64_t *> g_ptabs;
-static const uint64_t *column_polys(int N) {
-    std::lock_guard<std::mutex> lk(g_nmu);
-    auto it = g_ptabs.find(N);
-    if (it != g_ptabs.end()) return it->second;
-    if (!charpoly_init()) {
-        set_error(4, "xoshiro256** characteristic polynomial check failed");
-        return nullptr;
-    }
-    const long ncol = (long)N * N;
-    const unsigned long long T = 4ULL * (N / 2 + 1);
-    std::vector<uint64_t> tab(4 * ncol);
-    // columns of multiplication by x^T: MT[i] = x^(T + i) mod p
+// x^(first + stride c) mod p for c < count into tab (four words each), on the host's threads:
+// each step multiplies by x^stride through the table MT[i] = x^(stride + i) mod p
+static void fill_affine(uint64_t *tab, unsigned long long first, unsigned long long stride, long count) {
     std::vector<Poly> MT(256);
-    MT[0] = ppow_x(T);
+    MT[0] = ppow_x(stride);
     for (int i = 1; i < 256; i++) {
         MT[i] = MT[i - 1];
         pmulx(MT[i]);
@@ -173,17 +163,15 @@ static const uint64_t *column_polys(int N) {
     unsigned nth = std::thread::hardware_concurrency();
     if (nth < 1) nth = 1;
     if (nth > 32) nth = 32;
-    if (ncol < 4096) nth = 1;
+    if (count < 4096) nth = 1;
     std::vector<std::thread> th;
     for (unsigned w = 0; w < nth; w++) {
         th.emplace_back([&, w]() {
-            long c0 = ncol * w / nth, c1 = ncol * (w + 1) / nth;
+            const long c0 = count * w / nth, c1 = count * (w + 1) / nth;
             Poly q;
             for (long c = c0; c < c1; c++) {
-                if (c == 0) {
-                    q = Poly{{1, 0, 0, 0}};
-                } else if (c == c0 || c == 1) {
-                    q = ppow_x(T * (unsigned long long)c - 4);
+                if (c == c0) {
+                    q = ppow_x(first + stride * (unsigned long long)c);
                 } else {
                     Poly r = {{0, 0, 0, 0}};
                     for (int i = 0; i < 256; i++)
@@ -196,97 +184,68 @@ static const uint64_t *column_polys(int N) {
         });
     }
     for (auto &t : th) t.join();
+}
+
+static uint64_t *upload_polys(const std::vector<uint64_t> &tab, const char *what) {
     uint64_t *d = nullptr;
-    if (cudaMalloc(&d, sizeof(uint64_t) * 4 * ncol) != cudaSuccess) {
+    if (cudaMalloc(&d, sizeof(uint64_t) * tab.size()) != cudaSuccess) {
         cudaGetLastError();
-        set_error(5, "out of device memory for the noise column table");
+        set_error(5, what);
         return nullptr;
     }
-    cudaMemcpy(d, tab.data(), sizeof(uint64_t) * 4 * ncol, cudaMemcpyHostToDevice);
-    g_ptabs[N] = d;
+    cudaMemcpy(d, tab.data(), sizeof(uint64_t) * tab.size(), cudaMemcpyHostToDevice);
     return d;
 }
 
-// ---- device -----------------------------------------------------------------------------
-struct RngState {
-    uint64_t s[4];
+// per-N table of column polynomials (device), 4 x uint64 per column: column 0 starts at draw 0,
+// column c > 0 at T c - 4 (T = 4 (N/2 + 1) draws a column, none for the DC mode)
+static std::map<int, uint64_t *> g_ptabs;
+static const uint64_t *column_polys(int N) {
+    std::lock_guard<std::mutex> lk(g_nmu);
+    auto it = g_ptabs.find(N);
+    if (it != g_ptabs.end()) return it->second;
+    if (!charpoly_init()) {
+        set_error(4, "xoshiro256** characteristic polynomial check failed");
+        return nullptr;
+    }
+    const long ncol = (long)N * N;
+    const unsigned long long T = 4ULL * (N / 2 + 1);
+    std::vector<uint64_t> tab(4 * ncol, 0);
+    tab[0] = 1;
+    if (ncol > 1) fill_affine(tab.data() + 4, T - 4, T, ncol - 1);
+    uint64_t *d = upload_polys(tab, "out of device memory for the noise column table");
+    if (d) g_ptabs[N] = d;
+    return d;
+}
+
+struct AffineKey {
+    unsigned long long first, stride;
+    long count;
+    bool operator<(const AffineKey &o) const {
+        if (first != o.first) return first < o.first;
+        if (stride != o.stride) return stride < o.stride;
+        return count < o.count;
+    }
 };
-
-__device__ __forceinline__ uint64_t drotl(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
-
-__device__ __forceinline__ uint64_t dnext(uint64_t &s0, uint64_t &s1, uint64_t &s2, uint64_t &s3) {
-    const uint64_t result = drotl(s1 * 5, 7) * 9;  // include/random_xorshift.h:17
-    const uint64_t t = s1 << 17;
-    s2 ^= s0;
-    s3 ^= s1;
-    s1 ^= s2;
-    s0 ^= s3;
-    s2 ^= t;
-    s3 = drotl(s3, 45);
-    return result;
+static std::map<AffineKey, uint64_t *> g_atabs;
+const uint64_t *affine_jump_polys(unsigned long long first, unsigned long long stride, long count) {
+    std::lock_guard<std::mutex> lk(g_nmu);
+    const AffineKey key{first, stride, count};
+    auto it = g_atabs.find(key);
+    if (it != g_atabs.end()) return it->second;
+    if (!charpoly_init()) {
+        set_error(4, "xoshiro256** characteristic polynomial check failed");
+        return nullptr;
+    }
+    std::vector<uint64_t> tab(4 * (size_t)count);
+    fill_affine(tab.data(), first, stride, count);
+    uint64_t *d = upload_polys(tab, "out of device memory for a jump table");
+    if (d) g_atabs[key] = d;
+    return d;
 }
-
-// sampleNorm in FP64: src/random.c:34-49 (2^64 = (double)UINT64_MAX + 1)
-__device__ __forceinline__ double gauss64(uint64_t A, uint64_t B) {
-    const double RMax = 18446744073709551616.0;
-    const double u = (__ull2double_rn(A) + 0.5) / RMax;
-    const double v = (__ull2double_rn(B) + 0.5) / RMax;
-    return sqrt(-2 * log(u)) * cos(2 * 3.14159265358979323846 * v);
-}
-
-// the same Box-Muller transform in FP32, without divergence: t = u or 1 - u (the exact complement
-// ~A), t in (0, 1/2]; ln u = ln t for u < 1/2 (|ln t| >= ln 2, so the hardware log2 keeps full
-// relative precision) and ln u = ln(1 - t) = -2 atanh(s), s = t / (2 - t) <= 1/3, for u >= 1/2
-// (the atanh series through s^15; the next term is below 4e-9 relative)
-//
-// No 64-bit integer -> float conversions (they run on the FP64 pipe, a small fraction of the FP32
-// rate on this part): the uniform is hi 2^32 + lo from the two 32-bit halves (one FMA: within an
-// ulp of the rounded 64-bit value, 2^-24 relative at every magnitude), the cosine argument the
-// top 32 bits (absolute error below 2^-32).
-__device__ __forceinline__ float gauss32(uint64_t A, uint64_t B) {
-    const float inv64 = 5.42101086242752217e-20f;  // 2^-64
-    const bool hi = (A >> 63) != 0;
-    const uint64_t a = hi ? ~A : A;
-    const float af = fmaf((float)(unsigned)(a >> 32), 4294967296.f, (float)(unsigned)a);
-    const float t = (af + 0.5f) * inv64;
-    const float s = __fdividef(t, 2.f - t), s2 = s * s;
-    float p = 1.f / 15.f;
-    p = fmaf(p, s2, 1.f / 13.f);
-    p = fmaf(p, s2, 1.f / 11.f);
-    p = fmaf(p, s2, 1.f / 9.f);
-    p = fmaf(p, s2, 1.f / 7.f);
-    p = fmaf(p, s2, 1.f / 5.f);
-    p = fmaf(p, s2, 1.f / 3.f);
-    p = fmaf(p, s2, 1.f);
-    const float lnu = hi ? -2.f * s * p : __logf(t);
-    const float x = -2.f * lnu;  // > 0
-    // cos(2 pi v) = -cos(2 pi (v - 1/2)), argument in (-pi, pi) for the hardware cosine
-    const float w = ((float)(int)((unsigned)(B >> 32) ^ 0x80000000u) + 0.5f) * 2.3283064365386963e-10f;  // 2^-32
-    return -(x * rsqrtf(x)) * __cosf(6.28318530717958647692f * w);
-}
-
-template <typename T> __device__ __forceinline__ T gauss(uint64_t A, uint64_t B);
-template <> __device__ __forceinline__ float gauss<float>(uint64_t A, uint64_t B) { return gauss32(A, B); }
-template <> __device__ __forceinline__ double gauss<double>(uint64_t A, uint64_t B) { return gauss64(A, B); }
 
 #define NOISE_THREADS 128
 #define NOISE_CHUNK 16
-
-// Column start states.  A column's state is sum_i q_i A^i s0 over the bits q_i of its jump
-// polynomial (A: one xoshiro256** step, sums in GF(2)).  Each block tabulates A^i s0 for
-// i = 0..255 in shared memory once; a column's state is then the XOR of the entries its bits select
-// (a broadcast load and an and-xor per word and bit, against a full state step per bit for
-// Horner's rule).
-__device__ __forceinline__ void noise_state_table(const RngState &s0, ulonglong4 *tab) {
-    if (threadIdx.x == 0) {
-        uint64_t a0 = s0.s[0], a1 = s0.s[1], a2 = s0.s[2], a3 = s0.s[3];
-        for (int i = 0; i < 256; i++) {
-            tab[i] = make_ulonglong4(a0, a1, a2, a3);
-            dnext(a0, a1, a2, a3);
-        }
-    }
-    __syncthreads();
-}
 
 // One thread generates one column (x, y) of the half-complex grid, z fastest, from its jumped
 // state.  (Two consecutive columns a thread, the second continuing the first's stream without a
@@ -310,23 +269,7 @@ k_noise(int N, const uint64_t *__restrict__ polys, RngState s0, T factor, const 
     const long c0 = cblock + threadIdx.x;
     const bool valid = c0 < ncol;
     uint64_t r0 = 0, r1 = 0, r2 = 0, r3 = 0;
-    if (valid) {
-#pragma unroll 1
-        for (int wq = 0; wq < 4; wq++) {
-            const unsigned long long w = polys[4 * c0 + wq];
-            const unsigned lo = (unsigned)w, hi = (unsigned)(w >> 32);
-#pragma unroll 8
-            for (int bit = 0; bit < 64; bit++) {
-                const unsigned m = 0u - (((bit < 32 ? lo : hi) >> (bit & 31)) & 1u);
-                const uint64_t mm = ((uint64_t)m << 32) | m;
-                const ulonglong4 e = tab[wq * 64 + bit];
-                r0 ^= e.x & mm;
-                r1 ^= e.y & mm;
-                r2 ^= e.z & mm;
-                r3 ^= e.w & mm;
-            }
-        }
-    }
+    if (valid) jump_state(tab, polys + 4 * c0, r0, r1, r2, r3);
     {
         const long c = c0;
         const int kx = valid ? kint((int)(c / N), N) : 0;

@@ -128,6 +128,7 @@ static double *table_pinned(int slot, size_t n) {
 __global__ void k_copy_table(const double *__restrict__ src, double *__restrict__ dst, int n) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = src[i];
 }
+__global__ void k_flag_out(const int *__restrict__ flag, double *__restrict__ dst) { *dst = (double)*flag; }
 
 // the copy stream of the position transfers and the events of the two staging slots:
 // pos_event(s, 0) = positions ready on the device, pos_event(s, 1) = their copy done (buffer free)
@@ -194,6 +195,11 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     const bool want_vel = res && res->vel;
     if (want_vel && (!tvlo || !tvhi || B > 1)) {
         set_error(1, "velocities need a velocity transfer function (ic_config.index_vel) and an unbatched run");
+        return 1;
+    }
+    if (cfg->thermal && (!want_vel || (cfg->thermal != 1 && cfg->thermal != 2) || !(cfg->thermal_M_eV > 0) ||
+                         !(cfg->thermal_T_eV > 0))) {
+        set_error(1, "thermal motion needs velocities (ic_result.vel), kind 1 or 2, and positive mass and temperature");
         return 1;
     }
     const int acc_stride = 3 * cfg->pk_bins + 2;
@@ -410,6 +416,7 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     }
     // the slot's staging buffers are free once their previous copies are done
     if (dpos || want_vel) MITOS_CUDA(cudaStreamWaitEvent(stream(), pos_event(pslot, 1), 0));
+    int *therr = nullptr;  // thermal motion: bit 0 set for an invalid momentum
     // the aligned deposit uses a row pitch of N + 4 reals (16-byte aligned rows for vector reductions)
     const int rho_pitch = aligned ? N + 4 : N + 2;
     const size_t rho_bytes = B > 1 ? db : (size_t)N * N * rho_pitch * (sizeof(T));
@@ -497,6 +504,17 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
         e = launch_z_c2r<T>(g, ZOP_DISP, a);
         if (!e) e = velocity_gather((long)M * M * M, N, L, prec, dposraw, V0, V1, V2, dvel);
         if (e) return e;
+        // thermal motion (src/mitos.c:910-1064) from the stream the white noise left: four draws a
+        // mode with k > 0 (src/grf.c:47-63), then those of earlier thermal species
+        if (cfg->thermal) {
+            therr = (int *)workspace(sizeof(int), 153 + pslot);
+            if (!therr) return 5;
+            MITOS_CUDA(cudaMemsetAsync(therr, 0, sizeof(int), stream()));
+            const unsigned long long skip = 4ULL * ((unsigned long long)N * N * (N / 2 + 1) - 1) + cfg->thermal_draw_offset;
+            e = thermal_add(prec, (long)M * M * M, st, skip, cfg->thermal, cfg->thermal_T_eV, cfg->thermal_M_eV,
+                            1.0 / (1.0 + cfg->z_ini), cfg->speed_of_light, dvel, 3, therr);
+            if (e) return e;
+        }
         // to the caller on the copy stream, behind the positions (pos_event(pslot, 1) then covers both)
         MITOS_CUDA(cudaEventRecord(pos_event(pslot, 0), stream()));
         MITOS_CUDA(cudaStreamWaitEvent(copy_stream(), pos_event(pslot, 0), 0));
@@ -542,6 +560,13 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
         k_copy_table<<<1, 256, 0, stream()>>>(acc + cfg->pk_bins, hd, cfg->pk_bins);
         count_launch();
         MITOS_LAUNCH_CHECK("P(k) sums to the host");
+        opt->acc_host[cfg->pk_bins] = 0;
+        if (therr) {
+            launch_begin("flag_out");
+            k_flag_out<<<1, 1, 0, stream()>>>(therr, hd + cfg->pk_bins);
+            count_launch();
+            MITOS_LAUNCH_CHECK("thermal flag to the host");
+        }
         MITOS_CUDA(cudaEventRecord(acc_event(opt->async_slot), stream()));
         if (opt->iters) *opt->iters = iters;
         if (opt->last_rel) *opt->last_rel = last_rel;
@@ -558,6 +583,14 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
                                    cudaMemcpyDeviceToHost, stream()));
         MITOS_CUDA(cudaStreamSynchronize(stream()));
         if (dpos || want_vel) MITOS_CUDA(cudaEventSynchronize(pos_event(pslot, 1)));
+        if (therr) {
+            int h = 0;
+            MITOS_CUDA(cudaMemcpy(&h, therr, sizeof(int), cudaMemcpyDeviceToHost));
+            if (h) {
+                set_error(8, "thermal motion: invalid thermal momentum drawn");
+                return 8;
+            }
+        }
         for (int i = 0; i < cfg->pk_bins; i++) {
             const double n = (double)count[i];
             if (res->pk_obs) res->pk_obs[i] = (long)count[i];
@@ -673,6 +706,10 @@ int finish_slot(int k) {
     }
     s.res->ma_iterations = s.iters;
     s.res->ma_residual = s.last_rel;
+    if (s.acc_host[s.cfg.pk_bins] != 0) {
+        set_error(8, "thermal motion: invalid thermal momentum drawn");
+        return 8;
+    }
     return 0;
 }
 }  // namespace
@@ -691,7 +728,8 @@ extern "C" int ic_pipeline_submit(const struct ic_config *cfg, const struct pert
         if (s.acc_host) cudaFreeHost(s.acc_host);
         s.acc_host = nullptr;
         s.acc_cap = 0;
-        if (cudaMallocHost(&s.acc_host, sizeof(double) * cfg->pk_bins) != cudaSuccess) {
+        // P(k) sums, then the thermal-motion flag
+        if (cudaMallocHost(&s.acc_host, sizeof(double) * (cfg->pk_bins + 1)) != cudaSuccess) {
             cudaGetLastError();
             set_error(5, "out of pinned host memory for the P(k) sums");
             return 5;

@@ -1,0 +1,477 @@
+// thermal.cu -- thermal motion of a particle species on the GPU: the loop of src/mitos.c:928-965 and
+// :1054-1062 (the branch without Firebolt, where every draw is accepted).  Particle i of the species
+// (in id order) takes seven draws of the run's one xoshiro256** stream: a momentum from the
+// inverse-CDF sampler of src/random.c:261-289, then three sampleNorm for a direction; its velocity
+// gains n^ p / (a_ini M) c.
+//
+// Parallel form.  The draw count per particle is fixed, so particle i starts at draw 7 i of the
+// species: a thread takes a run of R consecutive particles from its jumped start state (rng.cuh),
+// stages its velocity increments in shared memory, and the block adds them to the velocities with
+// consecutive threads on consecutive addresses.
+//
+// The sampler's piece choice compares u = (double)w / 2^64 (w the 64-bit draw; (double)UINT64_MAX
+// is 2^64) with the pieces' CDF values.  Each comparison is exact in integers: the host finds, per
+// piece, the largest w with u <= Fr, and per search-table entry i the smallest w with
+// floor(u I_max) >= i.  Both precisions therefore pick the reference's piece for every draw.  The
+// FP64 build then evaluates the cubic, the momentum, the directions (GPU libm) and the float update
+// with the reference's operations and rounding; the FP32 build evaluates them in float from the same
+// piece (u - Fl taken exactly in integers first, so the cancellation costs no precision), with
+// normals whose cosine is accurate near its zeros (a normalised triple of small normals would
+// magnify an absolute error).
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <map>
+#include <mutex>
+#include <vector>
+
+#include "../../include/mitos_gb300.h"
+#include "context.cuh"
+#include "rng.cuh"
+
+namespace mitos {
+
+// ---- host: the sampler of src/random.c:87-209 for fd_pdf / be_pdf --------------------------------
+// (the constants of include/random.h:35-39: 1000 midpoint cells, a 1000-entry search table, the
+// momentum range [1e-10, 15] kT)
+namespace {
+constexpr int kCdfCells = 1000;
+constexpr int kTableLen = 1000;
+
+struct ThermalPdf {
+    int kind;  // 1 Fermi-Dirac, 2 Bose-Einstein (src/random.c:52-71)
+    double T, mu;
+    double operator()(double x) const {
+        if (x <= 0) return 0;
+        return x * x / (exp((x - mu) / T) + (kind == 2 ? -1. : 1.));
+    }
+};
+
+// Pieces of the inverse CDF, built by recursive halving.  A piece is halved while it holds more
+// than 5% of the probability; then while its cubic Hermite interpolant of x(F) is not monotone or
+// misses the CDF by more than 1e-6 at its middle.  Whether a piece is halved depends only on its
+// own ends, so the recursion gives the reference's pieces, already in order.
+struct PieceBuilder {
+    ThermalPdf f;
+    double xl, norm;
+    std::vector<struct interval> out;
+    bool overflow = false;
+
+    double integral(double b) const {  // midpoint rule on [xl, b]
+        const double h = (b - xl) / kCdfCells;
+        double s = 0;
+        for (int i = 0; i < kCdfCells; i++) s += h * f(xl + (i + 0.5) * h);
+        return s;
+    }
+    double cdf(double x) const { return norm * integral(x); }
+
+    void by_mass(double l, double r, double Fl, double Fr, int depth) {
+        if (Fr - Fl > 0.05 && depth < 200) {
+            const double m = l + 0.5 * (r - l), Fm = cdf(m);
+            by_mass(l, m, Fl, Fm, depth + 1);
+            by_mass(m, r, Fm, Fr, depth + 1);
+        } else {
+            overflow |= depth >= 200;
+            by_fit(l, r, Fl, Fr, depth);
+        }
+    }
+    void by_fit(double l, double r, double Fl, double Fr, int depth) {
+        const double pl = norm * f(l), pr = norm * f(r), dF = Fr - Fl;
+        struct interval iv;
+        memset(&iv, 0, sizeof iv);
+        iv.l = l;
+        iv.r = r;
+        iv.Fl = Fl;
+        iv.Fr = Fr;
+        iv.a0 = l;
+        iv.a1 = dF / pl;
+        iv.a2 = 3 * (r - l) - dF * (2. / pl + 1. / pr);
+        iv.a3 = 2 * (l - r) + dF * (1. / pl + 1. / pr);
+        const double xmid = iv.a0 + iv.a1 * 0.5 + iv.a2 * 0.25 + iv.a3 * 0.125;
+        iv.error = fabs(cdf(xmid) - 0.5 * (Fr + Fl));
+        const double slope = dF / (r - l);
+        const bool monotone = slope <= 3 * pl && slope <= 3 * pr;
+        if ((iv.error > 1e-6 || !monotone) && depth < 200) {
+            const double m = l + 0.5 * (r - l), Fm = cdf(m);
+            by_fit(l, m, Fl, Fm, depth + 1);
+            by_fit(m, r, Fm, Fr, depth + 1);
+        } else {
+            overflow |= depth >= 200;
+            out.push_back(iv);
+        }
+    }
+};
+}  // namespace
+
+// ---- device table ------------------------------------------------------------------------------
+struct ThermPiece {
+    unsigned long long le;     // largest draw w with (double)w 2^-64 <= Fr: "Fr < u" is w > le
+    unsigned long long flfix;  // floor(Fl 2^64)
+    double Fl, Fr, a0, a1, a2, a3;
+    float invw;                // FP32: 2^-64 / (Fr - Fl)
+    float b0, b1, b2, b3;      // FP32 copies of a0..a3
+    float pad;
+};
+static_assert(sizeof(ThermPiece) == 88, "piece layout");
+
+struct ThermTable {
+    int n, imax;
+    const ThermPiece *piece;
+    const unsigned long long *first;  // [imax + 1]: smallest w with floor(u imax) >= i
+    const int *start;                 // [imax]: the search table
+};
+
+static unsigned long long largest_not_above(double Fr) {
+    auto below = [&](unsigned long long w) { return (double)w * 0x1p-64 <= Fr; };
+    if (below(~0ULL)) return ~0ULL;
+    unsigned long long lo = 0, hi = ~0ULL;  // below(lo), !below(hi)
+    while (hi - lo > 1) {
+        const unsigned long long mid = lo + (hi - lo) / 2;
+        if (below(mid)) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+static unsigned long long smallest_reaching(int i, int imax) {
+    auto reach = [&](unsigned long long w) { return (int)floor(((double)w * 0x1p-64) * imax) >= i; };
+    if (reach(0)) return 0;
+    unsigned long long lo = 0, hi = ~0ULL;  // !reach(lo), reach(hi)
+    while (hi - lo > 1) {
+        const unsigned long long mid = lo + (hi - lo) / 2;
+        if (reach(mid)) hi = mid;
+        else lo = mid;
+    }
+    return hi;
+}
+
+// host image of the device table of a sampler; 0 or status 3 for a sampler this kernel cannot take
+static int table_image(const struct sampler *s, std::vector<unsigned char> &img, int &n, int &imax) {
+    n = s ? s->intervalNum : 0;
+    imax = s ? s->I_max : 0;
+    if (!s || n < 1 || imax < 1 || !s->intervals || !s->index) {
+        set_error(3, "thermal sampler: no pieces or no search table");
+        return 3;
+    }
+    for (int j = 0; j < n; j++) {
+        const struct interval &iv = s->intervals[j];
+        // the reference scan also requires r > (the previous piece's r); with pieces in order and
+        // increasing right ends that holds for every consecutive piece, so the kernel omits it
+        if (!(iv.r > 0) || !(iv.Fr >= 0) || !(iv.Fr - iv.Fl > 0) || (j > 0 && !(iv.r > s->intervals[j - 1].r))) {
+            set_error(3, "thermal sampler: pieces not in order of increasing right end");
+            return 3;
+        }
+    }
+    for (int i = 0; i < imax; i++)
+        if (!(s->index[i] >= 0 && s->index[i] < n)) {
+            set_error(3, "thermal sampler: search table entry out of range");
+            return 3;
+        }
+    const size_t pb = sizeof(ThermPiece) * n, fb = sizeof(unsigned long long) * (imax + 1);
+    img.assign(pb + fb + sizeof(int) * imax, 0);
+    ThermPiece *pc = (ThermPiece *)img.data();
+    for (int j = 0; j < n; j++) {
+        const struct interval &iv = s->intervals[j];
+        ThermPiece &p = pc[j];
+        p.le = largest_not_above(iv.Fr);
+        const double fl = iv.Fl * 0x1p64;
+        p.flfix = fl <= 0 ? 0ULL : (fl >= 0x1p64 ? ~0ULL : (unsigned long long)fl);
+        p.Fl = iv.Fl;
+        p.Fr = iv.Fr;
+        p.a0 = iv.a0;
+        p.a1 = iv.a1;
+        p.a2 = iv.a2;
+        p.a3 = iv.a3;
+        p.invw = (float)(0x1p-64 / (iv.Fr - iv.Fl));
+        p.b0 = (float)iv.a0;
+        p.b1 = (float)iv.a1;
+        p.b2 = (float)iv.a2;
+        p.b3 = (float)iv.a3;
+    }
+    unsigned long long *first = (unsigned long long *)(img.data() + pb);
+    for (int i = 0; i <= imax; i++) first[i] = smallest_reaching(i, imax);
+    int *start = (int *)(img.data() + pb + fb);
+    for (int i = 0; i < imax; i++) start[i] = (int)s->index[i];
+    return 0;
+}
+
+static ThermTable table_view(const void *dev, int n, int imax) {
+    ThermTable t;
+    t.n = n;
+    t.imax = imax;
+    t.piece = (const ThermPiece *)dev;
+    t.first = (const unsigned long long *)((const char *)dev + sizeof(ThermPiece) * n);
+    t.start = (const int *)((const char *)t.first + sizeof(unsigned long long) * (imax + 1));
+    return t;
+}
+
+// ---- kernel ------------------------------------------------------------------------------------
+#define THERMAL_THREADS 128
+#define THERMAL_CHUNK 8
+
+// piece for draw w (src/random.c:265-281 in integers)
+__device__ __forceinline__ int thermal_piece(const ThermTable &t, uint64_t w) {
+    unsigned long long q = __umul64hi(w, (unsigned long long)t.imax);  // floor(w imax / 2^64)
+    while (q < (unsigned long long)t.imax && w >= t.first[q + 1]) q++;
+    while (q > 0 && w < t.first[q]) q--;
+    int j = t.start[q < (unsigned long long)t.imax ? q : t.imax - 1];
+    int pick = j;
+    while (j < t.n && w > t.piece[j].le) pick = j++;
+    return pick;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(THERMAL_THREADS)
+k_thermal(long n, int R, RngState s0, const uint64_t *__restrict__ polys, ThermTable tt, double a_ini, double M_eV,
+          double c, float vfac, float *__restrict__ vel, long stride, int *err) {
+    __shared__ ulonglong4 tab[256];
+    __shared__ T stage[THERMAL_THREADS][3 * THERMAL_CHUNK + 1];
+    noise_state_table(s0, tab);
+    const long g = (long)blockIdx.x * THERMAL_THREADS + threadIdx.x;
+    const long first = g * R;
+    uint64_t r0 = 0, r1 = 0, r2 = 0, r3 = 0;
+    if (first < n) jump_state(tab, polys + 4 * g, r0, r1, r2, r3);
+    const long block_first = (long)blockIdx.x * THERMAL_THREADS * R;
+    bool bad = false;
+    for (int k0 = 0; k0 < R; k0 += THERMAL_CHUNK) {
+        for (int j = 0; j < THERMAL_CHUNK; j++) {
+            T d[3] = {0, 0, 0};
+            if (k0 + j < R && first + k0 + j < n) {
+                const uint64_t w = dnext(r0, r1, r2, r3);
+                const ThermPiece &P = tt.piece[thermal_piece(tt, w)];
+                if constexpr (sizeof(T) == 8) {
+                    // src/random.c:284-286, src/mitos.c:935-965 with the reference's rounding
+                    const double u = __dmul_rn(__ull2double_rn(w), 0x1p-64);
+                    const double v = __ddiv_rn(__dsub_rn(u, P.Fl), __dsub_rn(P.Fr, P.Fl));
+                    const double H = __dadd_rn(__dadd_rn(__dadd_rn(P.a0, __dmul_rn(P.a1, v)), __dmul_rn(__dmul_rn(P.a2, v), v)),
+                                               __dmul_rn(__dmul_rn(__dmul_rn(P.a3, v), v), v));
+                    const double p = __ddiv_rn(H, a_ini);
+                    bad |= isnan(p) || p <= 0;
+                    const double V = __dmul_rn(__ddiv_rn(p, M_eV), c);
+                    double e[3];
+                    for (int m = 0; m < 3; m++) {
+                        const uint64_t A = dnext(r0, r1, r2, r3), B = dnext(r0, r1, r2, r3);
+                        e[m] = gauss64(A, B);
+                    }
+                    const double len = hypot(e[0], hypot(e[1], e[2]));
+                    if (len > 0)
+                        for (int m = 0; m < 3; m++) e[m] = __ddiv_rn(e[m], len);
+                    for (int m = 0; m < 3; m++) d[m] = __dmul_rn(e[m], V);
+                } else {
+                    const long long diff = (long long)(w - P.flfix);  // (u - Fl) 2^64, exact
+                    const float dv = fmaf((float)(int)(diff >> 32), 4294967296.f, (float)(unsigned)diff);
+                    const float v = dv * P.invw;
+                    const float H = fmaf(fmaf(fmaf(P.b3, v, P.b2), v, P.b1), v, P.b0);
+                    bad |= !(H > 0.f);
+                    const float V = H * vfac;
+                    float e[3];
+                    for (int m = 0; m < 3; m++) {
+                        const uint64_t A = dnext(r0, r1, r2, r3), B = dnext(r0, r1, r2, r3);
+                        e[m] = gauss32_cospi(A, B);
+                    }
+                    const float l2 = e[0] * e[0] + e[1] * e[1] + e[2] * e[2];
+                    const float s = l2 > 0.f ? rsqrtf(l2) * V : V;
+                    for (int m = 0; m < 3; m++) d[m] = e[m] * s;
+                }
+            }
+            for (int m = 0; m < 3; m++) stage[threadIdx.x][3 * j + m] = d[m];
+        }
+        __syncthreads();
+        // add the block's increments: thread t's run starts at particle block_first + t R
+        for (int idx = threadIdx.x; idx < THERMAL_THREADS * 3 * THERMAL_CHUNK; idx += THERMAL_THREADS) {
+            const int t = idx / (3 * THERMAL_CHUNK), f = idx - t * (3 * THERMAL_CHUNK);
+            const int j = f / 3, m = f - 3 * j;
+            const long tf = block_first + (long)t * R;
+            const long p = tf + k0 + j;
+            if (k0 + j < R && p < n) {
+                float *a = vel + p * stride + m;
+                if constexpr (sizeof(T) == 8) *a = __double2float_rn(__dadd_rn((double)*a, stage[t][f]));
+                else *a += stage[t][f];
+            }
+        }
+        __syncthreads();
+    }
+    if (bad) atomicOr(err, 1);
+}
+
+// one species: n particles from state s0 advanced by `skip` draws; vel (device) n x stride floats
+static int thermal_launch(int prec, long n, const uint64_t s0[4], unsigned long long skip, const ThermTable &tt,
+                          double a_ini, double M_eV, double c, float *vel, long stride, int *err) {
+    if (n <= 0) return 0;
+    const long wave = 152L * 2048;
+    const int R = (int)((n + wave - 1) / wave);
+    const long G = (n + R - 1) / R;
+    const uint64_t *polys = affine_jump_polys(skip, 7ULL * (unsigned long long)R, G);
+    if (!polys) return 5;
+    RngState st;
+    memcpy(st.s, s0, sizeof st.s);
+    const unsigned blocks = (unsigned)((G + THERMAL_THREADS - 1) / THERMAL_THREADS);
+    const float vfac = (float)(c / (a_ini * M_eV));
+    launch_begin("thermal");
+    if (prec == MITOS_FP32)
+        k_thermal<float><<<blocks, THERMAL_THREADS, 0, stream()>>>(n, R, st, polys, tt, a_ini, M_eV, c, vfac, vel,
+                                                                    stride, err);
+    else
+        k_thermal<double><<<blocks, THERMAL_THREADS, 0, stream()>>>(n, R, st, polys, tt, a_ini, M_eV, c, vfac, vel,
+                                                                     stride, err);
+    count_launch();
+    MITOS_LAUNCH_CHECK("thermal velocities");
+    return 0;
+}
+
+// sampler tables of the pipeline's species, per (kind, T): device copies kept until exit
+struct CachedTable {
+    void *dev;
+    int n, imax;
+};
+static std::mutex g_tmu;
+static std::map<std::pair<int, double>, CachedTable> g_tables;
+
+static int sampler_build(struct sampler *s, int kind, double T_eV);
+
+int thermal_add(int prec, long n, const uint64_t seed_state[4], unsigned long long skip, int kind, double T_eV,
+                double M_eV, double a_ini, double c, float *dvel, long stride, int *derr) {
+    CachedTable ct;
+    {
+        std::lock_guard<std::mutex> lk(g_tmu);
+        auto it = g_tables.find({kind, T_eV});
+        if (it == g_tables.end()) {
+            struct sampler s;
+            int e = sampler_build(&s, kind, T_eV);
+            std::vector<unsigned char> img;
+            int nn = 0, im = 0;
+            if (!e) e = table_image(&s, img, nn, im);
+            free(s.intervals);
+            free(s.index);
+            if (e) return e;
+            void *d = nullptr;
+            if (cudaMalloc(&d, img.size()) != cudaSuccess) {
+                cudaGetLastError();
+                set_error(5, "out of device memory for a thermal sampler table");
+                return 5;
+            }
+            MITOS_CUDA(cudaMemcpy(d, img.data(), img.size(), cudaMemcpyHostToDevice));
+            it = g_tables.emplace(std::make_pair(kind, T_eV), CachedTable{d, nn, im}).first;
+        }
+        ct = it->second;
+    }
+    return thermal_launch(prec, n, seed_state, skip, table_view(ct.dev, ct.n, ct.imax), a_ini, M_eV, c, dvel, stride,
+                          derr);
+}
+
+static int sampler_build(struct sampler *s, int kind, double T_eV) {
+    memset(s, 0, sizeof *s);
+    if ((kind != 1 && kind != 2) || !(T_eV > 0)) {
+        set_error(1, "thermal sampler: kind 1 (fermion) or 2 (boson) and T_eV > 0");
+        return 1;
+    }
+    // src/mitos.c:645-668: the domain [1e-10, 15] kT in eV, mu = 0
+    PieceBuilder b;
+    b.f = ThermalPdf{kind, T_eV, 0.0};
+    b.xl = 1e-10 * T_eV;
+    const double xr = 15.0 * T_eV;
+    b.norm = 1.0;
+    b.norm = 1.0 / b.integral(xr);
+    b.by_mass(b.xl, xr, 0.0, 1.0, 0);
+    if (b.overflow) {
+        set_error(7, "thermal sampler: pieces did not converge");
+        return 7;
+    }
+    const int n = (int)b.out.size();
+    s->intervals = (struct interval *)malloc(sizeof(struct interval) * n);
+    s->index = (double *)malloc(sizeof(double) * kTableLen);
+    if (!s->intervals || !s->index) {
+        free(s->intervals);
+        free(s->index);
+        memset(s, 0, sizeof *s);
+        set_error(5, "thermal sampler: out of host memory");
+        return 5;
+    }
+    for (int j = 0; j < n; j++) {
+        s->intervals[j] = b.out[j];
+        s->intervals[j].id = j;
+        s->intervals[j].nid = j + 1 < n ? j + 1 : -1;
+    }
+    // search table: per u = i / 1000 the piece with the largest right end among those with Fr < u;
+    // pieces are in order, so that is the last one with Fr < u (piece 0 when there is none)
+    int last = 0;
+    for (int i = 0; i < kTableLen; i++) {
+        const double u = (double)i / kTableLen;
+        while (last + 1 < n && s->intervals[last + 1].Fr < u) last++;
+        s->index[i] = (s->intervals[last].Fr < u) ? last : 0;
+    }
+    s->norm = b.norm;
+    s->xl = b.xl;
+    s->xr = xr;
+    s->f = nullptr;
+    s->params = nullptr;
+    s->intervalNum = n;
+    s->I_max = kTableLen;
+    return 0;
+}
+
+}  // namespace mitos
+
+// ==== C ABI ===================================================================================
+extern "C" int thermal_sampler_init(struct sampler *s, int kind, double T_eV) {
+    if (!s) {
+        mitos::set_error(1, "thermal_sampler_init: no sampler");
+        return 1;
+    }
+    return mitos::sampler_build(s, kind, T_eV);
+}
+
+extern "C" int thermal_sampler_free(struct sampler *s) {
+    if (!s) return 0;
+    free(s->intervals);
+    free(s->index);
+    s->intervals = nullptr;
+    s->index = nullptr;
+    s->intervalNum = 0;
+    return 0;
+}
+
+extern "C" int thermal_velocities(const struct sampler *s, rng_state *state, long n, double M_eV, double a_ini,
+                                  double speed_of_light, float *vel, long stride) {
+    using namespace mitos;
+    if (!state || !vel || n < 0 || stride < 3 || !(M_eV > 0) || !(a_ini > 0)) {
+        set_error(1, "thermal_velocities: state, vel, n >= 0, stride >= 3, M_eV > 0 and a_ini > 0 needed");
+        return 1;
+    }
+    if (n == 0) return 0;
+    std::vector<unsigned char> img;
+    int nn = 0, im = 0;
+    int e = table_image(s, img, nn, im);
+    if (e) return e;
+    void *dtab = workspace(img.size(), 150);
+    int *derr = (int *)workspace(sizeof(int), 151);
+    if (!dtab || !derr) return 5;
+    MITOS_CUDA(cudaMemcpyAsync(dtab, img.data(), img.size(), cudaMemcpyHostToDevice, stream()));
+    MITOS_CUDA(cudaMemsetAsync(derr, 0, sizeof(int), stream()));
+    const size_t vbytes = sizeof(float) * (size_t)((n - 1) * stride + 3);
+    float *dvel = vel;
+    cudaPointerAttributes at;
+    const bool dev = cudaPointerGetAttributes(&at, vel) == cudaSuccess &&
+                     (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged);
+    if (!dev) {
+        cudaGetLastError();
+        dvel = (float *)workspace(vbytes, 152);
+        if (!dvel) return 5;
+        MITOS_CUDA(cudaMemcpyAsync(dvel, vel, vbytes, cudaMemcpyHostToDevice, stream()));
+    }
+    e = thermal_launch(mitos_get_precision(), n, state->s, 0, table_view(dtab, nn, im), a_ini, M_eV,
+                       speed_of_light, dvel, stride, derr);
+    if (e) return e;
+    if (!dev) MITOS_CUDA(cudaMemcpyAsync(vel, dvel, vbytes, cudaMemcpyDeviceToHost, stream()));
+    int herr = 0;
+    MITOS_CUDA(cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, stream()));
+    MITOS_CUDA(cudaStreamSynchronize(stream()));
+    // the caller's stream continues after the species' 7 n draws, as the reference loop leaves it
+    rng_jump(state->s, 7ULL * (unsigned long long)n);
+    if (herr) {
+        set_error(8, "thermal_velocities: invalid thermal momentum drawn");
+        return 8;
+    }
+    return 0;
+}

@@ -82,7 +82,29 @@ class ICConfig(ctypes.Structure):
                 ("k_pivot", ctypes.c_double), ("z_ini", ctypes.c_double), ("index_src", ctypes.c_int),
                 ("method", ctypes.c_int), ("ma_cycles", ctypes.c_int), ("ma_tol", ctypes.c_double),
                 ("pk_bins", ctypes.c_int), ("pk_linear", ctypes.c_int), ("precision", ctypes.c_int),
-                ("keep_outputs", ctypes.c_int), ("index_vel", ctypes.c_int)]
+                ("keep_outputs", ctypes.c_int), ("index_vel", ctypes.c_int),
+                ("thermal", ctypes.c_int), ("thermal_M_eV", ctypes.c_double),
+                ("thermal_T_eV", ctypes.c_double), ("speed_of_light", ctypes.c_double),
+                ("thermal_draw_offset", ctypes.c_uint64)]
+
+
+class Interval(ctypes.Structure):
+    """struct interval (include/random.h:43-51)"""
+    _fields_ = [("id", ctypes.c_int), ("l", ctypes.c_double), ("r", ctypes.c_double),
+                ("Fl", ctypes.c_double), ("Fr", ctypes.c_double), ("a0", ctypes.c_double),
+                ("a1", ctypes.c_double), ("a2", ctypes.c_double), ("a3", ctypes.c_double),
+                ("error", ctypes.c_double), ("nid", ctypes.c_int)]
+
+
+class Sampler(ctypes.Structure):
+    """struct sampler (include/random.h:54-81)"""
+    _fields_ = [("norm", ctypes.c_double), ("xl", ctypes.c_double), ("xr", ctypes.c_double),
+                ("f", ctypes.c_void_p), ("params", ctypes.c_void_p),
+                ("intervals", ctypes.POINTER(Interval)), ("intervalNum", ctypes.c_int),
+                ("I_max", ctypes.c_int), ("index", _dp)]
+
+
+FERMION, BOSON = 1, 2
 
 
 class ICResult(ctypes.Structure):
@@ -323,12 +345,60 @@ def cic_deposit_dg(rho, pos: np.ndarray, mass: float) -> float:
 
 # ---- fused pipeline --------------------------------------------------------------------------
 def ic_config(N, M, boxlen, seed, table, method=METHOD_2LPT, pk_bins=32, pk_linear=True,
-              precision=FP32, z_ini=31.0, ma_cycles=0, ma_tol=0.0, index_src=0, index_vel=None) -> ICConfig:
-    """index_vel: the velocity transfer function (default: the table's ``t_cdm`` when it has one)"""
+              precision=FP32, z_ini=31.0, ma_cycles=0, ma_tol=0.0, index_src=0, index_vel=None,
+              thermal=0, thermal_M_eV=0.0, thermal_T_eV=0.0, speed_of_light=0.0,
+              thermal_draw_offset=0) -> ICConfig:
+    """index_vel: the velocity transfer function (default: the table's ``t_cdm`` when it has one);
+    thermal: FERMION or BOSON adds thermal motion to the velocities (0: none)"""
     if index_vel is None:
         index_vel = table.index_of("t_cdm") if "t_cdm" in getattr(table, "titles", []) else -1
     return ICConfig(N, M, boxlen, seed, table.A_s, table.n_s, table.k_pivot, z_ini, index_src,
-                    method, ma_cycles, ma_tol, pk_bins, int(pk_linear), precision, 0, index_vel)
+                    method, ma_cycles, ma_tol, pk_bins, int(pk_linear), precision, 0, index_vel,
+                    int(thermal), thermal_M_eV, thermal_T_eV, speed_of_light, thermal_draw_offset)
+
+
+def thermal_sampler(kind: int, T_eV: float) -> Sampler:
+    """thermal_sampler_init: the inverse-CDF sampler of fd_pdf (FERMION) or be_pdf (BOSON)"""
+    s = Sampler()
+    _check(load().thermal_sampler_init(ctypes.byref(s), int(kind), ctypes.c_double(T_eV)))
+    return s
+
+
+def thermal_sampler_free(s: Sampler) -> None:
+    load().thermal_sampler_free(ctypes.byref(s))
+
+
+def sampler_rows(s: Sampler) -> np.ndarray:
+    """the sampler's pieces as rows [l r Fl Fr a0 a1 a2 a3]"""
+    rows = np.zeros((s.intervalNum, 8))
+    for j in range(s.intervalNum):
+        iv = s.intervals[j]
+        rows[j] = (iv.l, iv.r, iv.Fl, iv.Fr, iv.a0, iv.a1, iv.a2, iv.a3)
+    return rows
+
+
+def sampler_index(s: Sampler) -> np.ndarray:
+    return np.array([s.index[i] for i in range(s.I_max)], dtype=np.int64)
+
+
+def thermal_velocities(s: Sampler, state: np.ndarray, vel, M_eV: float, a_ini: float, c: float,
+                       stride: int = 3, n: int | None = None, offset: int = 0) -> np.ndarray:
+    """thermal_velocities on vel (host float32 array or a device tensor, updated in place): n particles
+    (default: size // stride) whose components start at float `offset` and lie `stride` floats apart;
+    state (four uint64) is advanced by 7 n draws.  Returns the new state."""
+    st = RngState()
+    for i in range(4):
+        st.s[i] = int(state[i])
+    if hasattr(vel, "data_ptr"):
+        n = vel.numel() // stride if n is None else n
+        ptr = ctypes.cast(vel.data_ptr() + 4 * offset, _fp)
+    else:
+        assert vel.dtype == np.float32 and vel.flags.c_contiguous
+        n = vel.size // stride if n is None else n
+        ptr = ctypes.cast(vel.ctypes.data + 4 * offset, _fp)
+    _check(load().thermal_velocities(ctypes.byref(s), ctypes.byref(st), ctypes.c_long(n), ctypes.c_double(M_eV),
+                                     ctypes.c_double(a_ini), ctypes.c_double(c), ptr, ctypes.c_long(stride)))
+    return np.array([st.s[i] for i in range(4)], dtype=np.uint64)
 
 
 def calc_bispectrum(g, bins, bins3, volume_mode=False, btype=0, theta=0.0, k3=0.0) -> dict:

@@ -78,7 +78,10 @@ class OrcICParams(ctypes.Structure):
                 ("sp", ctypes.POINTER(OrcPerturb)), ("index_src", ctypes.c_int),
                 ("z_ini", ctypes.c_double), ("lpt_order", ctypes.c_int),
                 ("ma_cycles", ctypes.c_int), ("pk_bins", ctypes.c_int),
-                ("pk_linear", ctypes.c_int), ("mass", ctypes.c_double), ("index_vel", ctypes.c_int)]
+                ("pk_linear", ctypes.c_int), ("mass", ctypes.c_double), ("index_vel", ctypes.c_int),
+                ("thermal", ctypes.c_int), ("thermal_T_eV", ctypes.c_double),
+                ("thermal_M_eV", ctypes.c_double), ("speed_of_light", ctypes.c_double),
+                ("thermal_draw_offset", ctypes.c_uint64)]
 
 
 class OrcICOut(ctypes.Structure):
@@ -199,10 +202,19 @@ def powerspec(N: int, boxlen: float, f1: np.ndarray, f2: np.ndarray, bins: int, 
 
 
 def ic_params(N, M, boxlen, seed, table, lpt_order=2, ma_cycles=0, pk_bins=32, pk_linear=True,
-              z_ini=31.0, mass=1.0, index_src=0, index_vel=-1):
+              z_ini=31.0, mass=1.0, index_src=0, index_vel=-1, thermal=0, thermal_T_eV=0.0,
+              thermal_M_eV=0.0, speed_of_light=0.0, thermal_draw_offset=0):
     return dict(N=N, M=M, boxlen=boxlen, seed=seed, table=table, lpt_order=lpt_order,
                 ma_cycles=ma_cycles, pk_bins=pk_bins, pk_linear=pk_linear, z_ini=z_ini, mass=mass,
-                index_src=index_src, index_vel=index_vel)
+                index_src=index_src, index_vel=index_vel, thermal=thermal, thermal_T_eV=thermal_T_eV,
+                thermal_M_eV=thermal_M_eV, speed_of_light=speed_of_light,
+                thermal_draw_offset=thermal_draw_offset)
+
+
+def _thermal_args(prm):
+    return (int(prm.get("thermal", 0)), ctypes.c_double(prm.get("thermal_T_eV", 0.0)),
+            ctypes.c_double(prm.get("thermal_M_eV", 0.0)), ctypes.c_double(prm.get("speed_of_light", 0.0)),
+            ctypes.c_uint64(prm.get("thermal_draw_offset", 0)))
 
 
 def _alloc_outputs(N, M, bins, want, ma_cycles):
@@ -234,7 +246,8 @@ def ic_pipeline(prm: dict, want=("pk",)) -> dict:
     o = _alloc_outputs(N, M, bins, want, prm["ma_cycles"])
     p = OrcICParams(N, M, prm["boxlen"], prm["seed"], OrcCosmo(t.A_s, t.n_s, t.k_pivot),
                     ctypes.pointer(sp.s), prm["index_src"], prm["z_ini"], prm["lpt_order"],
-                    prm["ma_cycles"], bins, int(prm["pk_linear"]), prm["mass"], prm.get("index_vel", -1))
+                    prm["ma_cycles"], bins, int(prm["pk_linear"]), prm["mass"], prm.get("index_vel", -1),
+                    *_thermal_args(prm))
     out = OrcICOut()
     out.grf, out.delta_k, out.phi_k = P(o.get("grf")), P(o.get("delta_k")), P(o.get("phi_k"))
     for i in range(3):
@@ -267,9 +280,88 @@ def ref_ic_pipeline(prm: dict, want=("pk",)) -> dict:
         prm["ma_cycles"], bins, int(prm["pk_linear"]), ctypes.c_double(prm["mass"]),
         P(o.get("grf")), P(o.get("delta_k")), P(o.get("phi_k")), P(o.get("disp0")),
         P(o.get("disp1")), P(o.get("disp2")), P(o.get("pos"), _fp), P(o.get("rho")),
-        P(o["pk_k"]), P(o["pk_p"]), P(o["pk_obs"], _lp), prm.get("index_vel", -1), P(o.get("vel"), _fp))
+        P(o["pk_k"]), P(o["pk_p"]), P(o["pk_obs"], _lp), prm.get("index_vel", -1), P(o.get("vel"), _fp),
+        *_thermal_args(prm))
     assert err == 0, err
     return _finish(o)
+
+
+# ---- thermal-motion sampler (thermal_oracle.c) ----------------------------------------------
+FERMION, BOSON = 1, 2
+
+
+def _state(st):
+    a = np.ascontiguousarray(np.asarray(st, dtype=np.uint64).reshape(4))
+    return a
+
+
+def _table_call(fn, kind, T_eV):
+    rows = np.zeros((4096, 8))
+    table = np.zeros(1000, np.int32)
+    norm = ctypes.c_double(0)
+    fn.restype = ctypes.c_int
+    with np.errstate(all="ignore"):
+        n = fn(int(kind), ctypes.c_double(T_eV), 4096, P(rows), table.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+               ctypes.byref(norm))
+    assert 0 < n <= 4096, n
+    return {"pieces": rows[:n].copy(), "table": table, "norm": norm.value}
+
+
+def sampler_table(kind: int, T_eV: float) -> dict:
+    """The sampler's pieces (rows l r Fl Fr a0 a1 a2 a3, sorted by Fl), start table and norm."""
+    return _table_call(lib().orc_sampler_table, kind, T_eV)
+
+
+def ref_sampler_table(kind: int, T_eV: float) -> dict:
+    return _table_call(ref_lib().ref_sampler_table, kind, T_eV)
+
+
+def _draws_call(fn, kind, T_eV, st0, n):
+    out = np.zeros(n)
+    st = _state(st0)
+    assert fn(int(kind), ctypes.c_double(T_eV), P(st, _up), ctypes.c_long(n), P(out)) == 0
+    return out
+
+
+def sampler_draws(kind: int, T_eV: float, st0, n: int) -> np.ndarray:
+    """n momenta (eV) drawn from start state st0 (four uint64)."""
+    return _draws_call(lib().orc_sampler_draws, kind, T_eV, st0, n)
+
+
+def ref_sampler_draws(kind: int, T_eV: float, st0, n: int) -> np.ndarray:
+    return _draws_call(ref_lib().ref_sampler_draws, kind, T_eV, st0, n)
+
+
+def thermal(kind, T_eV, M_eV, a_ini, c, st0, vel, stride=3) -> np.ndarray:
+    """vel (float32, particles x stride, updated copy returned) plus the thermal motion of
+    src/mitos.c:928-1062 from start state st0."""
+    v = np.array(vel, dtype=np.float32, copy=True, order="C")
+    n = v.shape[0]
+    st = _state(st0)
+    with np.errstate(all="ignore"):
+        e = lib().orc_thermal(int(kind), ctypes.c_double(T_eV), ctypes.c_double(M_eV), ctypes.c_double(a_ini),
+                              ctypes.c_double(c), P(st, _up), ctypes.c_long(n), P(v, _fp), ctypes.c_long(stride))
+    assert e == 0, e
+    return v
+
+
+def ref_thermal(kind, T_eV, M_eV, a_ini, c, st0, vel) -> np.ndarray:
+    v = np.array(vel, dtype=np.float32, copy=True, order="C")
+    st = _state(st0)
+    with np.errstate(all="ignore"):
+        e = ref_lib().ref_thermal(int(kind), ctypes.c_double(T_eV), ctypes.c_double(M_eV), ctypes.c_double(a_ini),
+                                  ctypes.c_double(c), P(st, _up), ctypes.c_long(v.shape[0]), P(v, _fp))
+    assert e == 0, e
+    return v
+
+
+def rng_state(seed: int, advance: int = 0) -> np.ndarray:
+    """xoshiro256** state of Seed after `advance` draws (sequential stepping)."""
+    st = np.zeros(4, np.uint64)
+    lib().orc_rng_init(ctypes.c_uint64(seed), P(st, _up))
+    if advance:
+        lib().orc_rng_advance(P(st, _up), ctypes.c_uint64(advance))
+    return st
 
 
 def _bispec_args(N, bins):

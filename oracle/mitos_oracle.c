@@ -13,6 +13,7 @@
  * twiddles from the host libm.
  */
 #include "mitos_oracle.h"
+#include "thermal_oracle.h"
 
 #include <math.h>
 #include <stdlib.h>
@@ -1280,6 +1281,7 @@ int orc_ic_pipeline(const struct orc_ic_params *p, struct orc_ic_out *o) {
 
     /* particle stage: :794 lattice, :827-863 displacements, :1072-1077 wrap */
     const long np = (long)M * M * M;
+    int thermal_err = 0;
     float *pos = malloc(sizeof(float) * 3 * np);
     orc_lattice(M, L, pos);
     for (int dir = 0; dir < 3; dir++) orc_displace(M, N, L, pos, disp[dir], dir);
@@ -1295,6 +1297,19 @@ int orc_ic_pipeline(const struct orc_ic_params *p, struct orc_ic_out *o) {
             }
         }
         for (int i = 0; i < 3; i++) free(vgrid[i]);
+        /* :910-1064 thermal motion (no Firebolt) on top, from the stream the white noise left:
+         * four draws a mode with k > 0 (src/grf.c:47-63), then those of earlier thermal species */
+        if (p->thermal > 0 && o->vel) {
+            uint64_t st[4];
+            orc_rng_init(p->seed, st);
+            orc_rng_advance(st, 4 * ((uint64_t)N * N * (N / 2 + 1) - 1) + p->thermal_draw_offset);
+            struct orc_sampler ts;
+            thermal_err = orc_sampler_init(&ts, p->thermal, p->thermal_T_eV, 0.0);
+            if (!thermal_err)
+                thermal_err = orc_thermal_velocities(&ts, st, np, p->thermal_M_eV, 1.0 / (1.0 + p->z_ini),
+                                                     p->speed_of_light, o->vel, 3);
+            orc_sampler_free(&ts);
+        }
     }
     orc_wrap_positions(np, L, pos);
     for (int i = 0; i < 3; i++) free(disp[i]);
@@ -1317,5 +1332,5 @@ int orc_ic_pipeline(const struct orc_ic_params *p, struct orc_ic_out *o) {
     else
         orc_powerspec_log(N, L, fbox, fbox, p->pk_bins, o->pk_k, o->pk_p, o->pk_obs);
     free(fbox);
-    return 0;
+    return thermal_err;
 }

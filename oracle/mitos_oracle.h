@@ -125,6 +125,9 @@ struct orc_ic_params {
     int pk_linear;      /* 1 = linear shells to k_Nyquist, 0 = reference log bins */
     double mass;        /* particle mass (cancels in the overdensity) */
     int index_vel;      /* velocity transfer function (src/mitos.c:425-490), < 0: no velocities */
+    int thermal;        /* thermal motion (src/mitos.c:910-1064): 0 none, 1 fermion, 2 boson */
+    double thermal_T_eV, thermal_M_eV, speed_of_light;
+    uint64_t thermal_draw_offset; /* draws of earlier thermal species after the white noise */
 };
 struct orc_ic_out {
     double *grf;        /* complex, after hermiticity + primordial power (optional) */

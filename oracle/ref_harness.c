@@ -8,6 +8,7 @@
  * (analyse/src/mitos_read.c:278-376); for those two steps this harness calls the oracle's
  * line-by-line restatement.  Linear P(k) shells are an extension with no reference code.
  */
+#include <math.h>
 #include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -61,6 +62,90 @@ int ref_fft_dg(int N, double boxlen, int to_momentum, double *real_padded, doubl
 
 static char *g_titles[64];
 
+/* the thermal-motion loop of src/mitos.c:928-965,1054-1062 (the branch without Firebolt, every draw
+ * accepted), calling the reference's samplerCustom and sampleNorm; the loop itself is inline in the
+ * reference's main() */
+static int thermal_loop(struct sampler *ts, rng_state *seed, struct particle *parts, long long n,
+                        double M_eV, double a_ini, double speed_of_light) {
+    for (long long i = 0; i < n; i++) {
+        double p0_eV = samplerCustom(ts, seed);
+        double p_eV = p0_eV / a_ini;
+        if (isnan(p_eV) || p_eV <= 0) return 1;
+        double V = p_eV / M_eV * speed_of_light;
+        double nx = sampleNorm(seed);
+        double ny = sampleNorm(seed);
+        double nz = sampleNorm(seed);
+        double length = hypot(nx, hypot(ny, nz));
+        if (length > 0) {
+            nx /= length;
+            ny /= length;
+            nz /= length;
+        }
+        parts[i].v_X += nx * V;
+        parts[i].v_Y += ny * V;
+        parts[i].v_Z += nz * V;
+    }
+    return 0;
+}
+
+/* the reference sampler (src/random.c:87-289) for kind 1 (fd_pdf) or 2 (be_pdf) on
+ * [THERMAL_MIN_MOMENTUM, THERMAL_MAX_MOMENTUM] kT, as src/mitos.c:641-668 sets it up: the pieces as
+ * rows [l r Fl Fr a0 a1 a2 a3], the search table, the normalisation */
+int ref_sampler_table(int kind, double T_eV, int max, double *rows, int *table, double *norm) {
+    double tp[2] = {T_eV, 0};
+    struct sampler s;
+    if (initSampler(&s, kind == 2 ? be_pdf : fd_pdf, THERMAL_MIN_MOMENTUM * T_eV, THERMAL_MAX_MOMENTUM * T_eV, tp))
+        return -1;
+    for (int j = 0; j < s.intervalNum && j < max; j++) {
+        const struct interval *iv = &s.intervals[j];
+        const double r[8] = {iv->l, iv->r, iv->Fl, iv->Fr, iv->a0, iv->a1, iv->a2, iv->a3};
+        memcpy(rows + 8 * j, r, sizeof r);
+    }
+    for (int i = 0; i < s.I_max && table; i++) table[i] = (int)s.index[i];
+    if (norm) *norm = s.norm;
+    const int n = s.intervalNum;
+    cleanSampler(&s);
+    return n;
+}
+
+int ref_sampler_draws(int kind, double T_eV, const uint64_t st0[4], long n, double *out) {
+    double tp[2] = {T_eV, 0};
+    struct sampler s;
+    if (initSampler(&s, kind == 2 ? be_pdf : fd_pdf, THERMAL_MIN_MOMENTUM * T_eV, THERMAL_MAX_MOMENTUM * T_eV, tp))
+        return 1;
+    rng_state st;
+    memcpy(st.s, st0, sizeof st.s);
+    for (long i = 0; i < n; i++) out[i] = samplerCustom(&s, &st);
+    cleanSampler(&s);
+    return 0;
+}
+
+/* n particles (velocities n x 3 in/out) through the thermal loop from state st0 */
+int ref_thermal(int kind, double T_eV, double M_eV, double a_ini, double speed_of_light,
+                const uint64_t st0[4], long n, float *vel) {
+    double tp[2] = {T_eV, 0};
+    struct sampler s;
+    if (initSampler(&s, kind == 2 ? be_pdf : fd_pdf, THERMAL_MIN_MOMENTUM * T_eV, THERMAL_MAX_MOMENTUM * T_eV, tp))
+        return 1;
+    struct particle *parts = calloc((size_t)n, sizeof(struct particle));
+    for (long i = 0; i < n; i++) {
+        parts[i].v_X = vel[3 * i];
+        parts[i].v_Y = vel[3 * i + 1];
+        parts[i].v_Z = vel[3 * i + 2];
+    }
+    rng_state st;
+    memcpy(st.s, st0, sizeof st.s);
+    const int e = thermal_loop(&s, &st, parts, n, M_eV, a_ini, speed_of_light);
+    for (long i = 0; i < n; i++) {
+        vel[3 * i] = parts[i].v_X;
+        vel[3 * i + 1] = parts[i].v_Y;
+        vel[3 * i + 2] = parts[i].v_Z;
+    }
+    free(parts);
+    cleanSampler(&s);
+    return e;
+}
+
 int ref_ic_pipeline(int N, int M, double L, uint64_t seed, double A_s, double n_s, double k_pivot,
                     int k_size, int tau_size, int n_functions, const double *kv,
                     const double *log_tau, const double *redshift, const double *Dg,
@@ -69,7 +154,8 @@ int ref_ic_pipeline(int N, int M, double L, uint64_t seed, double A_s, double n_
                     double mass, double *out_grf, double *out_delta_k, double *out_phi_k,
                     double *out_d0, double *out_d1, double *out_d2, float *out_pos,
                     double *out_rho, double *pk_k, double *pk_p, long *pk_obs, int index_vel,
-                    float *out_vel) {
+                    float *out_vel, int thermal_kind, double T_eV, double M_eV,
+                    double speed_of_light, uint64_t thermal_draw_offset) {
     if (n_functions > 64) return 1;
     for (int i = 0; i < n_functions; i++) {
         if (!g_titles[i]) {
@@ -251,6 +337,19 @@ int ref_ic_pipeline(int N, int M, double L, uint64_t seed, double A_s, double n_
             }
         }
         for (int i = 0; i < 3; i++) free(vgrid[i]);
+        /* :910-1064 thermal motion (no Firebolt), from the stream the white noise left (:148, :220) */
+        if (thermal_kind > 0) {
+            for (uint64_t d = 0; d < thermal_draw_offset; d++) (void)rand_uint64(&seed_state);
+            double tp[2] = {T_eV, 0};
+            struct sampler ts;
+            if (initSampler(&ts, thermal_kind == 2 ? be_pdf : fd_pdf, THERMAL_MIN_MOMENTUM * T_eV,
+                            THERMAL_MAX_MOMENTUM * T_eV, tp))
+                return 1;
+            const double a_ini = 1.0 / (1.0 + cosmo.z_ini);
+            err = thermal_loop(&ts, &seed_state, parts, chunk_size, M_eV, a_ini, speed_of_light);
+            cleanSampler(&ts);
+            if (err) return err;
+        }
         if (out_vel)
             for (long long i = 0; i < chunk_size; i++) {
                 out_vel[3 * i] = parts[i].v_X;

@@ -6,6 +6,8 @@ needs the reference tree) through oracle.ref_* and stores small fixtures:
   sample_norm.npz    sampleNorm streams (src/random.c:34-49)
   grf.npz            generate_complex_grf + enforce_hermiticity at 16^3 and 32^3
   pipeline.npz       positions and P(k) of src/mitos.c + analyse/src/mitos_read.c at 16^3 / 32^3
+  thermal.npz        initSampler pieces and search tables (src/random.c:87-209), samplerCustom
+                     draws (:261-289) and the thermal-motion loop of src/mitos.c:928-1062
 Usage: python tests/golden/make_golden.py
 """
 import os
@@ -43,7 +45,30 @@ def main():
         fx[name + "_obs"] = out["pk_obs"]
         fx[name + "_pk"] = out["pk_p"]
     np.savez_compressed(os.path.join(HERE, "pipeline.npz"), **fx)
+    thermal_fixture()
     print("golden vectors written to", HERE)
+
+
+# neutrino temperature today (1.9517578 K) in eV, and a heavier relic
+THERMAL_CASES = ((1, 1.9517578 * 8.617333262e-5), (2, 1.9517578 * 8.617333262e-5), (1, 0.25))
+
+
+def thermal_fixture():
+    oracle.build(ref=True)
+    fx = {}
+    rng = np.random.default_rng(5)
+    for kind, T in THERMAL_CASES:
+        name = f"k{kind}_T{T:.6e}"
+        tab = oracle.ref_sampler_table(kind, T)
+        fx[name + "_pieces"] = tab["pieces"]
+        fx[name + "_table"] = tab["table"]
+        st = oracle.rng_state(42, 123)
+        fx[name + "_state"] = st
+        fx[name + "_draws"] = oracle.ref_sampler_draws(kind, T, st, 2048)
+        vel = rng.standard_normal((512, 3)).astype(np.float32)
+        fx[name + "_vel_in"] = vel
+        fx[name + "_vel_out"] = oracle.ref_thermal(kind, T, 0.06, 1 / 32.0, 299792.458, st, vel)
+    np.savez_compressed(os.path.join(HERE, "thermal.npz"), **fx)
 
 
 if __name__ == "__main__":

@@ -1,0 +1,218 @@
+"""Thermal motion of a particle species (src/random.c:52-289, src/mitos.c:910-1064 without Firebolt).
+
+CPU: the oracle's sampler and thermal loop against the reference build and the golden vectors, and the
+library's host-side sampler (thermal_sampler_init) against the oracle.  GPU (marked): the kernel through
+the C ABI against the oracle, the FP32 build against FP64, the stream position it leaves, the struct
+particle stride, device buffers, and the pipeline's thermal stage against the oracle pipeline."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+import mitos_gb300.lib as ml
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+T_NU = 1.9517578 * 8.617333262e-5  # relic neutrino temperature today, eV
+CASES = ((ml.FERMION, T_NU), (ml.BOSON, T_NU), (ml.FERMION, 0.25))
+C_KMS = 299792.458
+
+
+def _needs_ref():
+    if oracle.ref_lib() is None:
+        pytest.skip("reference build absent (no reference tree on this machine)")
+
+
+# ---- CPU ------------------------------------------------------------------------------------------
+@pytest.mark.parametrize("kind,T", CASES)
+def test_oracle_sampler_pinned_to_reference(kind, T):
+    _needs_ref()
+    a, b = oracle.sampler_table(kind, T), oracle.ref_sampler_table(kind, T)
+    assert np.array_equal(a["pieces"], b["pieces"])
+    assert np.array_equal(a["table"], b["table"])
+    assert a["norm"] == b["norm"]
+    for seed, skip in ((42, 0), (7, 1000), (1001, 12345)):
+        st = oracle.rng_state(seed, skip)
+        assert np.array_equal(oracle.sampler_draws(kind, T, st, 20000), oracle.ref_sampler_draws(kind, T, st, 20000))
+    vel = np.random.default_rng(kind).standard_normal((3000, 3)).astype(np.float32)
+    st = oracle.rng_state(3, 77)
+    assert np.array_equal(oracle.thermal(kind, T, 0.06, 1 / 32.0, C_KMS, st, vel),
+                          oracle.ref_thermal(kind, T, 0.06, 1 / 32.0, C_KMS, st, vel))
+
+
+def test_oracle_thermal_golden():
+    g = np.load(os.path.join(GOLDEN, "thermal.npz"))
+    for kind, T in CASES:
+        name = f"k{kind}_T{T:.6e}"
+        tab = oracle.sampler_table(kind, T)
+        assert np.array_equal(tab["pieces"], g[name + "_pieces"])
+        assert np.array_equal(tab["table"], g[name + "_table"])
+        st = g[name + "_state"]
+        assert np.array_equal(oracle.sampler_draws(kind, T, st, 2048), g[name + "_draws"])
+        assert np.array_equal(oracle.thermal(kind, T, 0.06, 1 / 32.0, C_KMS, st, g[name + "_vel_in"]),
+                              g[name + "_vel_out"])
+
+
+def test_sampler_moments():
+    """Fermi-Dirac <p> = 3.1514 kT, Bose-Einstein 2.7012 kT; the reference draw (which evaluates the
+    cubic of the piece left of u, beyond its end) stays within 1% of them"""
+    st = oracle.rng_state(11, 0)
+    for kind, mean in ((ml.FERMION, 3.15137), (ml.BOSON, 2.70118)):
+        d = oracle.sampler_draws(kind, 1.0, st, 400000)
+        assert d.min() > 0 and d.max() <= 15.0 * 1.01
+        assert abs(d.mean() / mean - 1) < 0.01, d.mean()
+
+
+@pytest.mark.parametrize("kind,T", CASES)
+def test_library_sampler_matches_oracle(kind, T):
+    """thermal_sampler_init is host code (no GPU): its pieces, search table and norm equal the oracle's"""
+    s = ml.thermal_sampler(kind, T)
+    try:
+        o = oracle.sampler_table(kind, T)
+        assert np.array_equal(ml.sampler_rows(s), o["pieces"])
+        assert np.array_equal(ml.sampler_index(s), o["table"])
+        assert s.norm == o["norm"] and s.I_max == 1000
+    finally:
+        ml.thermal_sampler_free(s)
+    with pytest.raises(ml.MitosError):
+        ml.thermal_sampler(3, T)
+
+
+def test_oracle_pipeline_thermal_pinned_to_reference(table):
+    """the thermal stage of the oracle pipeline, from the stream the white noise leaves (src/mitos.c:148,
+    :220, :935), equals the reference functions driven in the reference order"""
+    _needs_ref()
+    iv = table.index_of("t_cdm")
+    for kind, off in ((ml.FERMION, 0), (ml.BOSON, 5000)):
+        prm = oracle.ic_params(16, 16, 64.0, 42, table, pk_bins=8, index_vel=iv, thermal=kind,
+                               thermal_T_eV=T_NU, thermal_M_eV=0.06, speed_of_light=C_KMS,
+                               thermal_draw_offset=off)
+        a = oracle.ic_pipeline(prm, want=("vel", "pk"))
+        b = oracle.ref_ic_pipeline(prm, want=("vel", "pk"))
+        assert np.array_equal(a["vel"], b["vel"])
+        plain = oracle.ic_pipeline(dict(prm, thermal=0), want=("vel", "pk"))
+        assert not np.array_equal(a["vel"], plain["vel"])
+
+
+# ---- GPU ------------------------------------------------------------------------------------------
+def _ulps(a, b):
+    a = np.asarray(a, np.float32).view(np.int32).astype(np.int64)
+    b = np.asarray(b, np.float32).view(np.int32).astype(np.int64)
+    return np.abs(a - b)
+
+
+def _gpu_thermal(kind, T, st, vel, prec, M_eV=0.06, a_ini=1 / 32.0, stride=3, n=None, offset=0):
+    s = ml.thermal_sampler(kind, T)
+    ml.set_precision(prec)
+    try:
+        return ml.thermal_velocities(s, st, vel, M_eV, a_ini, C_KMS, stride=stride, n=n, offset=offset)
+    finally:
+        ml.set_precision(ml.FP64)
+        ml.thermal_sampler_free(s)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind,T", CASES)
+def test_thermal_fp64_vs_oracle(kind, T):
+    """FP64: the reference's draws, pieces and operations; only GPU log/cos/hypot may move a float
+    result by one unit in the last place"""
+    n = 200003
+    vel = np.random.default_rng(1).standard_normal((n, 3)).astype(np.float32) * 100
+    st = oracle.rng_state(42, 999)
+    ref = oracle.thermal(kind, T, 0.06, 1 / 32.0, C_KMS, st, vel)
+    out = vel.copy()
+    st2 = _gpu_thermal(kind, T, st, out, ml.FP64)
+    u = _ulps(out, ref)
+    print(f"kind {kind} T {T:.3e}: {np.count_nonzero(u)} of {u.size} floats differ, max {u.max()} ulp")
+    assert u.max() <= 1 and np.count_nonzero(u) <= u.size * 1e-4
+    # the stream continues after 7 n draws, as the reference loop leaves it
+    assert np.array_equal(st2, oracle.rng_state(42, 999 + 7 * n))
+
+
+@pytest.mark.gpu
+def test_thermal_fp32_vs_fp64():
+    n = 1 << 20
+    vel = np.zeros((n, 3), np.float32)
+    st = oracle.rng_state(8, 0)
+    a, b = vel.copy(), vel.copy()
+    _gpu_thermal(ml.FERMION, T_NU, st, a, ml.FP32)
+    _gpu_thermal(ml.FERMION, T_NU, st, b, ml.FP64)
+    speed = np.linalg.norm(b, axis=1)
+    err = np.abs(a - b).max(axis=1) / speed
+    print(f"FP32 vs FP64 thermal velocities: max rel {err.max():.3e}, mean {err.mean():.3e}")
+    # measured 6.6e-6 (mean 7.5e-8) on 2^20 particles
+    assert err.max() < 1e-5
+
+
+@pytest.mark.gpu
+def test_thermal_struct_particle_stride_and_device_buffer():
+    """stride 10 floats (struct particle: X Y Z v_X v_Y v_Z mass pad id) leaves the other fields alone;
+    a device buffer gives the same result as a host one"""
+    import torch
+    n = 50000
+    parts = np.random.default_rng(2).standard_normal((n, 10)).astype(np.float32)
+    packed = np.ascontiguousarray(parts[:, 3:6])
+    st = oracle.rng_state(5, 17)
+    want = parts.copy()
+    want[:, 3:6] = oracle.thermal(ml.FERMION, T_NU, 0.06, 1 / 32.0, C_KMS, st, packed)
+    got = parts.copy()
+    _gpu_thermal(ml.FERMION, T_NU, st, got, ml.FP64, stride=10, n=n, offset=3)
+    assert np.array_equal(np.delete(got, [3, 4, 5], axis=1), np.delete(parts, [3, 4, 5], axis=1))
+    assert _ulps(got[:, 3:6], want[:, 3:6]).max() <= 1
+    dev = torch.from_numpy(packed.copy()).cuda()
+    _gpu_thermal(ml.FERMION, T_NU, st, dev, ml.FP64)
+    host = packed.copy()
+    _gpu_thermal(ml.FERMION, T_NU, st, host, ml.FP64)
+    assert np.array_equal(dev.cpu().numpy(), host)
+
+
+@pytest.mark.gpu
+def test_thermal_full_size_thread_boundaries():
+    """512^3 particles (R = 432 a thread): particles at and around thread-run boundaries, and a spread
+    of others, equal the oracle started from the jumped stream; isotropy of the increments"""
+    n = 1 << 27
+    vel = np.zeros((n, 3), np.float32)
+    st = oracle.rng_state(1000, 0)
+    _gpu_thermal(ml.FERMION, T_NU, st, vel, ml.FP64)
+    R = -(-n // (152 * 2048))
+    picks = sorted({0, 1, R - 1, R, R + 1, 2 * R, 5000 * R - 1, 5000 * R, n - R, n - 2, n - 1,
+                    *np.random.default_rng(0).integers(0, n, 40).tolist()})
+    for i in picks:
+        s = st.copy()
+        ml.load().mitos_rng_jump(s.ctypes.data_as(ml.ctypes.POINTER(ml.ctypes.c_uint64)),
+                                 ml.ctypes.c_ulonglong(7 * i))
+        ref = oracle.thermal(ml.FERMION, T_NU, 0.06, 1 / 32.0, C_KMS, s, np.zeros((1, 3), np.float32))
+        assert _ulps(vel[i], ref[0]).max() <= 1, i
+    v64 = vel.astype(np.float64)
+    mean = v64.mean(axis=0)
+    speed = np.sqrt((v64 ** 2).sum(axis=1))
+    sigma = np.sqrt((speed ** 2).mean() / 3)  # per component
+    assert np.abs(mean).max() < 6 * sigma / np.sqrt(n)
+    # <p> = 3.1514 kT for the Fermi-Dirac momentum, speed = p / (a M) c
+    assert abs(speed.mean() / (3.15137 * T_NU * 32 / 0.06 * C_KMS) - 1) < 0.01
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [ml.FP64, ml.FP32])
+def test_pipeline_thermal_vs_oracle(prec, table, spline):
+    """the pipeline's thermal stage: the species' draws start after the white noise's (and after
+    thermal_draw_offset more), on top of the gathered velocities"""
+    N, L = 32, 128.0
+    iv = table.index_of("t_cdm")
+    for kind, off in ((ml.FERMION, 0), (ml.BOSON, 4242)):
+        cfg = ml.ic_config(N, N, L, 42, table, pk_bins=12, precision=prec, index_vel=iv, thermal=kind,
+                           thermal_M_eV=0.06, thermal_T_eV=T_NU, speed_of_light=C_KMS, thermal_draw_offset=off)
+        out = ml.ic_pipeline_run(cfg, spline, want_vel=True)
+        ref = oracle.ic_pipeline(oracle.ic_params(N, N, L, 42, table, pk_bins=12, index_vel=iv, thermal=kind,
+                                                  thermal_T_eV=T_NU, thermal_M_eV=0.06, speed_of_light=C_KMS,
+                                                  thermal_draw_offset=off), want=("vel", "pk"))
+        if prec == ml.FP64:
+            u = _ulps(out["vel"], ref["vel"])
+            assert u.max() <= 1 and np.count_nonzero(u) <= u.size * 1e-3, (u.max(), np.count_nonzero(u))
+        else:
+            err = np.abs(out["vel"] - ref["vel"]).max() / np.abs(ref["vel"]).max()
+            assert err < 2e-5, err
+    bad = ml.ic_config(N, N, L, 42, table, pk_bins=12, precision=prec, index_vel=iv, thermal=ml.FERMION,
+                       thermal_M_eV=0.0, thermal_T_eV=T_NU, speed_of_light=C_KMS)
+    with pytest.raises(ml.MitosError):
+        ml.ic_pipeline_run(bad, spline, want_vel=True)
