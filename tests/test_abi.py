@@ -18,7 +18,8 @@ def declared_functions():
     for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
         src = open(h).read()
         src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-        for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b([A-Za-z_]\w*)\s*\(", src, re.M):
+        # function declarations (typedefs of function pointers are types, not exports)
+        for m in re.finditer(r"^\s*(?!typedef\b)(?:const\s+)?[A-Za-z_][\w\s\*]*?\b([A-Za-z_]\w*)\s*\(", src, re.M):
             name = m.group(1)
             if name not in ("if", "while", "for", "return", "sizeof", "defined"):
                 names.add(name)
