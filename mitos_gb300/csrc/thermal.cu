@@ -11,8 +11,8 @@
 //
 // The sampler's piece choice compares u = (double)w / 2^64 (w the 64-bit draw; (double)UINT64_MAX
 // is 2^64) with the pieces' CDF values.  Each comparison is exact in integers: the host finds, per
-// piece, the largest w with u <= Fr, and per search-table entry i the smallest w with
-// floor(u I_max) >= i.  Both precisions therefore pick the reference's piece for every draw.  The
+// piece, the largest w with u <= Fr.  Both precisions therefore pick the reference's piece for
+// every draw.  The
 // FP64 build then evaluates the cubic, the momentum, the directions (GPU libm) and the float update
 // with the reference's operations and rounding; the FP32 build evaluates them in float from the same
 // piece (u - Fl taken exactly in integers first, so the cancellation costs no precision), with
@@ -105,6 +105,16 @@ struct PieceBuilder {
 }  // namespace
 
 // ---- device table ------------------------------------------------------------------------------
+// The reference's scan (src/random.c:270-280) starts at a search-table piece whose Fr is below
+// u (or at piece 0) and steps on while Fr < u, so the piece it ends on is the last one with Fr < u,
+// or piece 0 when there is none: the search table only makes the scan short.  With "Fr_j < u"
+// exact as "w > le_j" (le_j below), the kernel starts from the last piece whose le lies below the
+// start of w's bucket (top 10 bits of w) and steps on while w > le of the next piece: one table
+// load, then usually one threshold compare.  The host checks that the sampler's search table is
+// the one initSampler builds, which that argument assumes.
+constexpr int kBucketBits = 10;
+constexpr int kBuckets = 1 << kBucketBits;
+
 struct ThermPiece {
     unsigned long long le;     // largest draw w with (double)w 2^-64 <= Fr: "Fr < u" is w > le
     unsigned long long flfix;  // floor(Fl 2^64)
@@ -115,11 +125,17 @@ struct ThermPiece {
 };
 static_assert(sizeof(ThermPiece) == 88, "piece layout");
 
+// FP32 part of a piece, as kept in shared memory
+struct PieceF {
+    unsigned long long flfix;
+    float invw, b0, b1, b2, b3, pad;
+};
+static_assert(sizeof(PieceF) == 32, "shared piece layout");
+
 struct ThermTable {
-    int n, imax;
+    int n;
     const ThermPiece *piece;
-    const unsigned long long *first;  // [imax + 1]: smallest w with floor(u imax) >= i
-    const int *start;                 // [imax]: the search table
+    const unsigned short *bucket;  // [kBuckets]: piece to start from for the draws of each bucket
 };
 
 static unsigned long long largest_not_above(double Fr) {
@@ -134,42 +150,40 @@ static unsigned long long largest_not_above(double Fr) {
     return lo;
 }
 
-static unsigned long long smallest_reaching(int i, int imax) {
-    auto reach = [&](unsigned long long w) { return (int)floor(((double)w * 0x1p-64) * imax) >= i; };
-    if (reach(0)) return 0;
-    unsigned long long lo = 0, hi = ~0ULL;  // !reach(lo), reach(hi)
-    while (hi - lo > 1) {
-        const unsigned long long mid = lo + (hi - lo) / 2;
-        if (reach(mid)) hi = mid;
-        else lo = mid;
-    }
-    return hi;
-}
-
 // host image of the device table of a sampler; 0 or status 3 for a sampler this kernel cannot take
-static int table_image(const struct sampler *s, std::vector<unsigned char> &img, int &n, int &imax) {
+static int table_image(const struct sampler *s, std::vector<unsigned char> &img, int &n) {
     n = s ? s->intervalNum : 0;
-    imax = s ? s->I_max : 0;
-    if (!s || n < 1 || imax < 1 || !s->intervals || !s->index) {
+    if (!s || n < 1 || n > 65535 || s->I_max < 1 || !s->intervals || !s->index) {
         set_error(3, "thermal sampler: no pieces or no search table");
         return 3;
     }
     for (int j = 0; j < n; j++) {
         const struct interval &iv = s->intervals[j];
         // the reference scan also requires r > (the previous piece's r); with pieces in order and
-        // increasing right ends that holds for every consecutive piece, so the kernel omits it
-        if (!(iv.r > 0) || !(iv.Fr >= 0) || !(iv.Fr - iv.Fl > 0) || (j > 0 && !(iv.r > s->intervals[j - 1].r))) {
+        // increasing right ends that holds for every consecutive piece
+        if (!(iv.r > 0) || !(iv.Fr >= 0) || !(iv.Fr - iv.Fl > 0) ||
+            (j > 0 && (!(iv.r > s->intervals[j - 1].r) || !(iv.Fr > s->intervals[j - 1].Fr)))) {
             set_error(3, "thermal sampler: pieces not in order of increasing right end");
             return 3;
         }
     }
-    for (int i = 0; i < imax; i++)
-        if (!(s->index[i] >= 0 && s->index[i] < n)) {
-            set_error(3, "thermal sampler: search table entry out of range");
+    // the search table must be initSampler's (src/random.c:191-206)
+    for (int i = 0; i < s->I_max; i++) {
+        const double u = (double)i / s->I_max;
+        double rmax = 0;
+        int want = 0;
+        for (int j = 0; j < n; j++)
+            if (s->intervals[j].Fr < u && s->intervals[j].r > rmax) {
+                rmax = s->intervals[j].r;
+                want = j;
+            }
+        if (s->index[i] != (double)want) {
+            set_error(3, "thermal sampler: search table is not the one initSampler builds");
             return 3;
         }
-    const size_t pb = sizeof(ThermPiece) * n, fb = sizeof(unsigned long long) * (imax + 1);
-    img.assign(pb + fb + sizeof(int) * imax, 0);
+    }
+    const size_t pb = sizeof(ThermPiece) * n;
+    img.assign(pb + sizeof(unsigned short) * kBuckets, 0);
     ThermPiece *pc = (ThermPiece *)img.data();
     for (int j = 0; j < n; j++) {
         const struct interval &iv = s->intervals[j];
@@ -189,59 +203,81 @@ static int table_image(const struct sampler *s, std::vector<unsigned char> &img,
         p.b2 = (float)iv.a2;
         p.b3 = (float)iv.a3;
     }
-    unsigned long long *first = (unsigned long long *)(img.data() + pb);
-    for (int i = 0; i <= imax; i++) first[i] = smallest_reaching(i, imax);
-    int *start = (int *)(img.data() + pb + fb);
-    for (int i = 0; i < imax; i++) start[i] = (int)s->index[i];
+    // bucket b holds the draws w >> (64 - kBucketBits) == b; its start piece is the pick of its
+    // smallest draw: (number of pieces with le < w) - 1, at least 0
+    unsigned short *bucket = (unsigned short *)(img.data() + pb);
+    int c = 0;
+    for (int b = 0; b < kBuckets; b++) {
+        const unsigned long long w0 = (unsigned long long)b << (64 - kBucketBits);
+        while (c < n && pc[c].le < w0) c++;
+        bucket[b] = (unsigned short)(c > 0 ? c - 1 : 0);
+    }
     return 0;
 }
 
-static ThermTable table_view(const void *dev, int n, int imax) {
+static ThermTable table_view(const void *dev, int n) {
     ThermTable t;
     t.n = n;
-    t.imax = imax;
     t.piece = (const ThermPiece *)dev;
-    t.first = (const unsigned long long *)((const char *)dev + sizeof(ThermPiece) * n);
-    t.start = (const int *)((const char *)t.first + sizeof(unsigned long long) * (imax + 1));
+    t.bucket = (const unsigned short *)((const char *)dev + sizeof(ThermPiece) * n);
     return t;
 }
 
 // ---- kernel ------------------------------------------------------------------------------------
 #define THERMAL_THREADS 128
 #define THERMAL_CHUNK 8
+static_assert(THERMAL_CHUNK == 8, "the packed add loop divides f < 24 by 3 as (11 f) >> 5");
 
-// piece for draw w (src/random.c:265-281 in integers)
-__device__ __forceinline__ int thermal_piece(const ThermTable &t, uint64_t w) {
-    unsigned long long q = __umul64hi(w, (unsigned long long)t.imax);  // floor(w imax / 2^64)
-    while (q < (unsigned long long)t.imax && w >= t.first[q + 1]) q++;
-    while (q > 0 && w < t.first[q]) q--;
-    int j = t.start[q < (unsigned long long)t.imax ? q : t.imax - 1];
-    int pick = j;
-    while (j < t.n && w > t.piece[j].le) pick = j++;
-    return pick;
+// Shared memory: the block's table of A^i s0 (8 KB) while the threads jump to their start states,
+// then, in the same bytes, the bucket table, the thresholds and (FP32) the pieces.
+__host__ __device__ constexpr size_t thermal_smem(int n) {
+    const size_t tables = sizeof(unsigned short) * kBuckets + (sizeof(unsigned long long) + sizeof(PieceF)) * (size_t)n;
+    return tables > 256 * sizeof(ulonglong4) ? tables : 256 * sizeof(ulonglong4);
 }
 
 template <typename T>
-__global__ void __launch_bounds__(THERMAL_THREADS)
+__global__ void __launch_bounds__(THERMAL_THREADS, sizeof(T) == 4 ? 10 : 6)
 k_thermal(long n, int R, RngState s0, const uint64_t *__restrict__ polys, ThermTable tt, double a_ini, double M_eV,
           double c, float vfac, float *__restrict__ vel, long stride, int *err) {
-    __shared__ ulonglong4 tab[256];
+    extern __shared__ __align__(16) unsigned char smem[];
     __shared__ T stage[THERMAL_THREADS][3 * THERMAL_CHUNK + 1];
+    ulonglong4 *tab = (ulonglong4 *)smem;
     noise_state_table(s0, tab);
     const long g = (long)blockIdx.x * THERMAL_THREADS + threadIdx.x;
     const long first = g * R;
     uint64_t r0 = 0, r1 = 0, r2 = 0, r3 = 0;
     if (first < n) jump_state(tab, polys + 4 * g, r0, r1, r2, r3);
+    __syncthreads();
+    // the sampler tables over the jump table
+    PieceF *spf = (PieceF *)smem;
+    unsigned long long *sle = (unsigned long long *)(spf + tt.n);
+    unsigned short *sbk = (unsigned short *)(sle + tt.n);
+    for (int i = threadIdx.x; i < tt.n; i += THERMAL_THREADS) {
+        const ThermPiece &P = tt.piece[i];
+        sle[i] = P.le;
+        spf[i] = PieceF{P.flfix, P.invw, P.b0, P.b1, P.b2, P.b3, 0.f};
+    }
+    for (int i = threadIdx.x; i < kBuckets; i += THERMAL_THREADS) sbk[i] = tt.bucket[i];
+    __syncthreads();
     const long block_first = (long)blockIdx.x * THERMAL_THREADS * R;
     bool bad = false;
+    const long rem = n - block_first;  // particles from the block's first on
     for (int k0 = 0; k0 < R; k0 += THERMAL_CHUNK) {
+        // the velocities this chunk adds to, on their way to L2 while the chunk computes
+        if (first + k0 < n) {
+            const long last = min(first + k0 + THERMAL_CHUNK, min(first + R, n)) - 1;
+            prefetch_l2(vel + (first + k0) * stride);
+            prefetch_l2(vel + last * stride + 2);
+        }
         for (int j = 0; j < THERMAL_CHUNK; j++) {
             T d[3] = {0, 0, 0};
             if (k0 + j < R && first + k0 + j < n) {
                 const uint64_t w = dnext(r0, r1, r2, r3);
-                const ThermPiece &P = tt.piece[thermal_piece(tt, w)];
+                int pk = sbk[w >> (64 - kBucketBits)];
+                while (pk + 1 < tt.n && w > sle[pk + 1]) pk++;
                 if constexpr (sizeof(T) == 8) {
                     // src/random.c:284-286, src/mitos.c:935-965 with the reference's rounding
+                    const ThermPiece &P = tt.piece[pk];
                     const double u = __dmul_rn(__ull2double_rn(w), 0x1p-64);
                     const double v = __ddiv_rn(__dsub_rn(u, P.Fl), __dsub_rn(P.Fr, P.Fl));
                     const double H = __dadd_rn(__dadd_rn(__dadd_rn(P.a0, __dmul_rn(P.a1, v)), __dmul_rn(__dmul_rn(P.a2, v), v)),
@@ -259,6 +295,7 @@ k_thermal(long n, int R, RngState s0, const uint64_t *__restrict__ polys, ThermT
                         for (int m = 0; m < 3; m++) e[m] = __ddiv_rn(e[m], len);
                     for (int m = 0; m < 3; m++) d[m] = __dmul_rn(e[m], V);
                 } else {
+                    const PieceF P = spf[pk];
                     const long long diff = (long long)(w - P.flfix);  // (u - Fl) 2^64, exact
                     const float dv = fmaf((float)(int)(diff >> 32), 4294967296.f, (float)(unsigned)diff);
                     const float v = dv * P.invw;
@@ -271,23 +308,36 @@ k_thermal(long n, int R, RngState s0, const uint64_t *__restrict__ polys, ThermT
                         e[m] = gauss32_cospi(A, B);
                     }
                     const float l2 = e[0] * e[0] + e[1] * e[1] + e[2] * e[2];
-                    const float s = l2 > 0.f ? rsqrtf(l2) * V : V;
-                    for (int m = 0; m < 3; m++) d[m] = e[m] * s;
+                    const float sc = l2 > 0.f ? rsqrtf(l2) * V : V;
+                    for (int m = 0; m < 3; m++) d[m] = e[m] * sc;
                 }
             }
             for (int m = 0; m < 3; m++) stage[threadIdx.x][3 * j + m] = d[m];
         }
         __syncthreads();
         // add the block's increments: thread t's run starts at particle block_first + t R
-        for (int idx = threadIdx.x; idx < THERMAL_THREADS * 3 * THERMAL_CHUNK; idx += THERMAL_THREADS) {
-            const int t = idx / (3 * THERMAL_CHUNK), f = idx - t * (3 * THERMAL_CHUNK);
-            const int j = f / 3, m = f - 3 * j;
-            const long tf = block_first + (long)t * R;
-            const long p = tf + k0 + j;
-            if (k0 + j < R && p < n) {
-                float *a = vel + p * stride + m;
-                if constexpr (sizeof(T) == 8) *a = __double2float_rn(__dadd_rn((double)*a, stage[t][f]));
-                else *a += stage[t][f];
+        if (stride == 3) {
+            // packed velocities: thread t's chunk is 24 consecutive floats; 32-bit offsets in the block
+            float *base = vel + 3 * (block_first + k0);
+            for (int idx = threadIdx.x; idx < THERMAL_THREADS * 3 * THERMAL_CHUNK; idx += THERMAL_THREADS) {
+                const int t = idx / (3 * THERMAL_CHUNK), f = idx - t * (3 * THERMAL_CHUNK);
+                const int j = (f * 11) >> 5;  // f / 3 for f < 24
+                if (k0 + j < R && (long)(t * R + k0 + j) < rem) {
+                    float *a = base + (3 * t * R + f);
+                    if constexpr (sizeof(T) == 8) *a = __double2float_rn(__dadd_rn((double)*a, stage[t][f]));
+                    else *a += stage[t][f];
+                }
+            }
+        } else {
+            for (int idx = threadIdx.x; idx < THERMAL_THREADS * 3 * THERMAL_CHUNK; idx += THERMAL_THREADS) {
+                const int t = idx / (3 * THERMAL_CHUNK), f = idx - t * (3 * THERMAL_CHUNK);
+                const int j = f / 3, m = f - 3 * j;
+                const long p = block_first + (long)t * R + k0 + j;
+                if (k0 + j < R && p < n) {
+                    float *a = vel + p * stride + m;
+                    if constexpr (sizeof(T) == 8) *a = __double2float_rn(__dadd_rn((double)*a, stage[t][f]));
+                    else *a += stage[t][f];
+                }
             }
         }
         __syncthreads();
@@ -295,11 +345,28 @@ k_thermal(long n, int R, RngState s0, const uint64_t *__restrict__ polys, ThermT
     if (bad) atomicOr(err, 1);
 }
 
-// one species: n particles from state s0 advanced by `skip` draws; vel (device) n x stride floats
+// one species: n particles from state s0 advanced by `skip` draws; vel (device) n x stride floats.
+// The grid is one wave of resident blocks (every thread a run of R particles, the same work), so no
+// partial second wave idles most SMs.
 static int thermal_launch(int prec, long n, const uint64_t s0[4], unsigned long long skip, const ThermTable &tt,
                           double a_ini, double M_eV, double c, float *vel, long stride, int *err) {
     if (n <= 0) return 0;
-    const long wave = 152L * 2048;
+    const size_t smem = thermal_smem(tt.n);
+    int dev = 0, sms = 0, per_sm = 0;
+    MITOS_CUDA(cudaGetDevice(&dev));
+    MITOS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    if (prec == MITOS_FP32) {
+        if (smem > 48 * 1024) MITOS_CUDA(cudaFuncSetAttribute(k_thermal<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        MITOS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_thermal<float>, THERMAL_THREADS, smem));
+    } else {
+        if (smem > 48 * 1024) MITOS_CUDA(cudaFuncSetAttribute(k_thermal<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        MITOS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_thermal<double>, THERMAL_THREADS, smem));
+    }
+    if (per_sm < 1) {
+        set_error(3, "thermal sampler of %d pieces does not fit the kernel's shared memory", tt.n);
+        return 3;
+    }
+    const long wave = (long)sms * per_sm * THERMAL_THREADS;
     const int R = (int)((n + wave - 1) / wave);
     const long G = (n + R - 1) / R;
     const uint64_t *polys = affine_jump_polys(skip, 7ULL * (unsigned long long)R, G);
@@ -310,11 +377,11 @@ static int thermal_launch(int prec, long n, const uint64_t s0[4], unsigned long 
     const float vfac = (float)(c / (a_ini * M_eV));
     launch_begin("thermal");
     if (prec == MITOS_FP32)
-        k_thermal<float><<<blocks, THERMAL_THREADS, 0, stream()>>>(n, R, st, polys, tt, a_ini, M_eV, c, vfac, vel,
-                                                                    stride, err);
+        k_thermal<float><<<blocks, THERMAL_THREADS, smem, stream()>>>(n, R, st, polys, tt, a_ini, M_eV, c, vfac, vel,
+                                                                       stride, err);
     else
-        k_thermal<double><<<blocks, THERMAL_THREADS, 0, stream()>>>(n, R, st, polys, tt, a_ini, M_eV, c, vfac, vel,
-                                                                     stride, err);
+        k_thermal<double><<<blocks, THERMAL_THREADS, smem, stream()>>>(n, R, st, polys, tt, a_ini, M_eV, c, vfac, vel,
+                                                                        stride, err);
     count_launch();
     MITOS_LAUNCH_CHECK("thermal velocities");
     return 0;
@@ -323,7 +390,7 @@ static int thermal_launch(int prec, long n, const uint64_t s0[4], unsigned long 
 // sampler tables of the pipeline's species, per (kind, T): device copies kept until exit
 struct CachedTable {
     void *dev;
-    int n, imax;
+    int n;
 };
 static std::mutex g_tmu;
 static std::map<std::pair<int, double>, CachedTable> g_tables;
@@ -340,8 +407,8 @@ int thermal_add(int prec, long n, const uint64_t seed_state[4], unsigned long lo
             struct sampler s;
             int e = sampler_build(&s, kind, T_eV);
             std::vector<unsigned char> img;
-            int nn = 0, im = 0;
-            if (!e) e = table_image(&s, img, nn, im);
+            int nn = 0;
+            if (!e) e = table_image(&s, img, nn);
             free(s.intervals);
             free(s.index);
             if (e) return e;
@@ -352,11 +419,11 @@ int thermal_add(int prec, long n, const uint64_t seed_state[4], unsigned long lo
                 return 5;
             }
             MITOS_CUDA(cudaMemcpy(d, img.data(), img.size(), cudaMemcpyHostToDevice));
-            it = g_tables.emplace(std::make_pair(kind, T_eV), CachedTable{d, nn, im}).first;
+            it = g_tables.emplace(std::make_pair(kind, T_eV), CachedTable{d, nn}).first;
         }
         ct = it->second;
     }
-    return thermal_launch(prec, n, seed_state, skip, table_view(ct.dev, ct.n, ct.imax), a_ini, M_eV, c, dvel, stride,
+    return thermal_launch(prec, n, seed_state, skip, table_view(ct.dev, ct.n), a_ini, M_eV, c, dvel, stride,
                           derr);
 }
 
@@ -441,8 +508,8 @@ extern "C" int thermal_velocities(const struct sampler *s, rng_state *state, lon
     }
     if (n == 0) return 0;
     std::vector<unsigned char> img;
-    int nn = 0, im = 0;
-    int e = table_image(s, img, nn, im);
+    int nn = 0;
+    int e = table_image(s, img, nn);
     if (e) return e;
     void *dtab = workspace(img.size(), 150);
     int *derr = (int *)workspace(sizeof(int), 151);
@@ -460,7 +527,7 @@ extern "C" int thermal_velocities(const struct sampler *s, rng_state *state, lon
         if (!dvel) return 5;
         MITOS_CUDA(cudaMemcpyAsync(dvel, vel, vbytes, cudaMemcpyHostToDevice, stream()));
     }
-    e = thermal_launch(mitos_get_precision(), n, state->s, 0, table_view(dtab, nn, im), a_ini, M_eV,
+    e = thermal_launch(mitos_get_precision(), n, state->s, 0, table_view(dtab, nn), a_ini, M_eV,
                        speed_of_light, dvel, stride, derr);
     if (e) return e;
     if (!dev) MITOS_CUDA(cudaMemcpyAsync(vel, dvel, vbytes, cudaMemcpyDeviceToHost, stream()));
