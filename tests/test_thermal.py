@@ -193,6 +193,26 @@ def test_thermal_full_size_thread_boundaries():
 
 
 @pytest.mark.gpu
+def test_thermal_fp32_large_ragged():
+    """FP32 on 2^25 + 12345 particles (400 MB of velocities, above L2; the last thread's run is
+    short): sampled particles against the oracle started from the jumped stream"""
+    import torch
+    n = (1 << 25) + 12345
+    dev = torch.zeros((n, 3), dtype=torch.float32, device="cuda")
+    st = oracle.rng_state(77, 0)
+    _gpu_thermal(ml.FERMION, T_NU, st, dev, ml.FP32)
+    vel = dev.cpu().numpy()
+    R = -(-n // (152 * 2048))
+    picks = sorted({0, R - 1, R, n - 1, n - R, *np.random.default_rng(3).integers(0, n, 30).tolist()})
+    for i in picks:
+        s = st.copy()
+        ml.load().mitos_rng_jump(s.ctypes.data_as(ml.ctypes.POINTER(ml.ctypes.c_uint64)),
+                                 ml.ctypes.c_ulonglong(7 * i))
+        ref = oracle.thermal(ml.FERMION, T_NU, 0.06, 1 / 32.0, C_KMS, s, np.zeros((1, 3), np.float32))[0]
+        assert np.abs(vel[i] - ref).max() <= 1e-5 * np.linalg.norm(ref), i
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("prec", [ml.FP64, ml.FP32])
 def test_pipeline_thermal_vs_oracle(prec, table, spline):
     """the pipeline's thermal stage: the species' draws start after the white noise's (and after
@@ -216,3 +236,65 @@ def test_pipeline_thermal_vs_oracle(prec, table, spline):
                        thermal_M_eV=0.0, thermal_T_eV=T_NU, speed_of_light=C_KMS)
     with pytest.raises(ml.MitosError):
         ml.ic_pipeline_run(bad, spline, want_vel=True)
+
+
+@pytest.mark.gpu
+def test_async_submissions_with_thermal(table, spline):
+    """ic_pipeline_submit with velocities and thermal motion (three ICs in flight, one without thermal
+    motion): the velocities of ic_pipeline_run bit for bit"""
+    import ctypes
+    N, L, bins = 32, 128.0, 12
+    iv = table.index_of("t_cdm")
+    kinds = [ml.FERMION, 0, ml.BOSON]
+
+    def cfg(kind, seed):
+        return ml.ic_config(N, N, L, seed, table, pk_bins=bins, index_vel=iv, thermal=kind, thermal_M_eV=0.06,
+                            thermal_T_eV=T_NU, speed_of_light=C_KMS)
+
+    refs = [ml.ic_pipeline_run(cfg(k, 20 + i), spline, want_vel=True) for i, k in enumerate(kinds)]
+    keep = []
+    for i, k in enumerate(kinds):
+        kk, p, o = np.zeros(bins), np.zeros(bins), np.zeros(bins, np.int64)
+        vel = np.zeros((N ** 3, 3), np.float32)
+        res = ml.ICResult(kk.ctypes.data_as(ml._dp), p.ctypes.data_as(ml._dp), o.ctypes.data_as(ml._lp), None, 0, 0.0,
+                          vel.ctypes.data_as(ml._fp))
+        c = cfg(k, 20 + i)
+        ml.ic_pipeline_submit(c, spline, res)
+        keep.append((vel, p, res, c))
+    ml.ic_pipeline_wait()
+    for (vel, p, res, c), ref in zip(keep, refs):
+        assert np.array_equal(vel, ref["vel"])
+        assert np.allclose(p, ref["pk_p"], rtol=1e-5, equal_nan=True)
+    assert not np.array_equal(refs[0]["vel"], refs[1]["vel"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [ml.FP64, ml.FP32])
+def test_thermal_invalid_momentum_reports_status_8(prec):
+    """a sampler whose cubic is negative everywhere: the reference exits (src/mitos.c:939-942), the
+    library returns status 8 and leaves the context usable"""
+    import ctypes
+    iv = (ml.Interval * 1)()
+    iv[0].l, iv[0].r, iv[0].Fl, iv[0].Fr, iv[0].a0 = 1.0, 2.0, 0.0, 1.0, -1.0
+    index = (ctypes.c_double * 1)(0.0)
+    s = ml.Sampler(1.0, 1.0, 2.0, None, None, iv, 1, 1, index)
+    vel = np.zeros((1000, 3), np.float32)
+    ml.set_precision(prec)
+    try:
+        with pytest.raises(ml.MitosError) as e:
+            ml.thermal_velocities(s, oracle.rng_state(1, 0), vel, 0.06, 1 / 32.0, C_KMS)
+        assert e.value.code == 8
+    finally:
+        ml.set_precision(ml.FP64)
+    # a sampler whose search table is not initSampler's is refused before any launch (status 3)
+    index[0] = 5.0
+    with pytest.raises(ml.MitosError) as e:
+        ml.thermal_velocities(s, oracle.rng_state(1, 0), vel, 0.06, 1 / 32.0, C_KMS)
+    assert e.value.code == 3
+    out = vel.copy()
+    st = ml.thermal_sampler(ml.FERMION, T_NU)
+    try:
+        ml.thermal_velocities(st, oracle.rng_state(1, 0), out, 0.06, 1 / 32.0, C_KMS)
+    finally:
+        ml.thermal_sampler_free(st)
+    assert np.all(np.isfinite(out)) and np.abs(out).max() > 0
