@@ -45,6 +45,27 @@ def algorithmic_bytes(name: str, G: float) -> float:
     return table.get(name, 0) * G
 
 
+def replica_seed(base: int, rank: int) -> int:
+    """first seed of a rank's replicas: ranks 1000 seeds apart, so up to 1000 steps never share one"""
+    return base + 1000 * rank
+
+
+def max_over_ranks(x: float, dist) -> float:
+    """the largest value of x over the ranks (the slowest replica sets the job's time)"""
+    if dist is None:
+        return x
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(ws: int, steps: int, seconds: float) -> float:
+    """units all ranks processed (steps each) per second of the slowest rank"""
+    return ws * steps / seconds
+
+
 def dist_setup():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -388,7 +409,7 @@ def main():
     spline = ml.Spline(table)
     prec = ml.FP32 if args.precision == "fp32" else ml.FP64
     N = args.N
-    seed0 = args.seed + 1000 * rank
+    seed0 = replica_seed(args.seed, rank)
 
     def cfg(step):
         return ml.ic_config(N, N, args.boxlen, seed0 + step, table, method=ml.METHOD_2LPT,
@@ -423,13 +444,9 @@ def main():
     barrier()
     clk = clocks.stop()
     launches = (ml.launch_count() - launches0) // args.steps
-    if dist:
-        import torch
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, dist)
     ms_per_step = ms / args.steps
-    value = ws * args.steps / (ms / 1e3)
+    value = job_throughput(ws, args.steps, ms / 1e3)
     if args.quick:
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "ms_per_step": ms_per_step,
@@ -462,8 +479,8 @@ def main():
         ml.ic_pipeline_submit(cfg(args.warmup + i), spline, outs[i][3])
     ml.ic_pipeline_wait()
     barrier()
-    e2e_s = time.perf_counter() - t0
-    e2e_val = ws * args.steps / e2e_s
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dist)
+    e2e_val = job_throughput(ws, args.steps, e2e_s)
     assert all(np.isfinite(o[1][1:]).all() for o in outs[:args.steps])
 
     # per-kernel durations of one IC (roofline of the dominant kernel)
