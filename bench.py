@@ -74,54 +74,74 @@ def dist_setup():
 
 
 class Clocks:
-    """nvidia-smi samples during the timed region"""
+    """nvidia-smi samples (every 20 ms, timestamped) kept for the timed region only: start() returns
+    once the sampler has written its first line, mark() brackets the region"""
 
     def __init__(self, gpu: int):
         self.gpu = gpu
         self.proc = None
         self.path = None
+        self.t0 = self.t1 = None
 
     def start(self):
         fd, self.path = tempfile.mkstemp(suffix=".csv")
         os.close(fd)
-        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+        q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={q}",
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except (FileNotFoundError, OSError):
             self.proc = None
+            return
+        deadline = time.time() + 5.0
+        while time.time() < deadline and os.path.getsize(self.path) == 0 and self.proc.poll() is None:
+            time.sleep(0.01)
+
+    def mark(self, begin: bool):
+        if begin:
+            self.t0 = time.time()
+        else:
+            self.t1 = time.time()
 
     def stop(self):
         if not self.proc:
             return None
+        time.sleep(0.05)
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
-        sm, mx, reasons = [], [], set()
+        import datetime
+        rows = []
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in open(self.path):
             f = [x.strip() for x in line.split(",")]
-            if len(f) < 9:
+            if len(f) < 10:
                 continue
             try:
-                sm.append(float(f[1]))
-                mx.append(float(f[2]))
+                ts = datetime.datetime.strptime(f[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                rows.append((ts, float(f[2]), float(f[3]), [n for n, v in zip(names, f[6:10]) if v.lower() == "active"]))
             except ValueError:
                 continue
-            for n, v in zip(names, f[5:9]):
-                if v.lower() == "active":
-                    reasons.add(n)
         os.unlink(self.path)
-        if not sm:
+        if not rows:
             return None
-        load = [s for s in sm if s > 0.5 * max(sm)] or sm
-        return {"sm_mhz": statistics.median(load), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+        t0 = self.t0 if self.t0 is not None else rows[0][0]
+        t1 = self.t1 if self.t1 is not None else rows[-1][0]
+        inside = [r for r in rows if t0 <= r[0] <= t1]
+        if not inside:  # a region shorter than the sampling interval: the samples on either side
+            before = [r for r in rows if r[0] < t0][-1:]
+            after = [r for r in rows if r[0] > t1][:1]
+            inside = before + after
+        sm = [r[1] for r in inside]
+        load = [x for x in sm if x > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(load), "sm_max_mhz": max(r[2] for r in inside),
+                "reasons": sorted({n for r in inside for n in r[3]}), "samples": len(inside),
+                "region_s": round(t1 - t0, 3)}
 
 
 def peak_hbm():
@@ -435,13 +455,15 @@ def main():
         step(i)
     launches0 = ml.launch_count()
     clocks = Clocks(local)
-    barrier()
     clocks.start()
+    barrier()
+    clocks.mark(True)
     ml.timer_start()
     for i in range(args.steps):
         step(args.warmup + i)
     ms = ml.timer_stop()
     barrier()
+    clocks.mark(False)
     clk = clocks.stop()
     launches = (ml.launch_count() - launches0) // args.steps
     ms = max_over_ranks(ms, dist)
@@ -505,7 +527,7 @@ def main():
     kernels = {k: {"ms": round(v[0] / v[1], 4), "launches": v[1] // KT_ICS,
                    "GBps": round(algorithmic_bytes(k, G) / (v[0] / v[1] / 1e3) / 1e9, 1) if algorithmic_bytes(k, G) else None}
                for k, v in sorted(agg.items(), key=lambda kv: -kv[1][0])}
-    alg_ic = 37 * G  # survey byte model per IC with two-pass FFTs, (15 + 22 (P - 1)) G
+    alg_ic = 37 * G  # byte model per IC with two-pass FFTs, (15 + 22 (P - 1)) G
     if rank != 0:
         return 0
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
