@@ -34,6 +34,26 @@ def test_pipeline_fp64_vs_oracle(N, method, lin, table, spline):
     assert np.abs(_wrapdiff(out["pos"], ref["pos"], L)).max() < 1e-4
 
 
+@pytest.mark.parametrize("method", [ml.METHOD_2LPT, ml.METHOD_ZELDOVICH])
+def test_large_displacements_take_the_global_gather(method, table, spline):
+    """z = 0 in a 64 Mpc/h box of 1 Mpc/h cells: displacements of several cells, so most particles
+    leave the lattice deposit's staged tiles and gather from global memory; positions and P(k)
+    still equal the oracle's"""
+    N, L = 64, 64.0
+    cfg = ml.ic_config(N, N, L, 5, table, method=method, pk_bins=16, pk_linear=True, precision=ml.FP64, z_ini=0.0)
+    out = ml.ic_pipeline_run(cfg, spline, want_pos=True)
+    ref = oracle.ic_pipeline(oracle.ic_params(N, N, L, 5, table, lpt_order=2 if method == ml.METHOD_2LPT else 1,
+                                              pk_bins=16, pk_linear=True, z_ini=0.0), want=("pos", "pk"))
+    lattice = (np.indices((N, N, N)).reshape(3, -1).T + 0.0) * (L / N)
+    disp = np.abs(_wrapdiff(ref["pos"], lattice, L)) / (L / N)
+    print(f"displacements: rms {np.sqrt(np.mean(disp ** 2)):.2f} cells, beyond half a cell: {np.mean(disp.max(axis=1) > 0.5):.2f}")
+    assert np.mean(disp.max(axis=1) > 0.5) > 0.3
+    assert np.abs(_wrapdiff(out["pos"], ref["pos"], L)).max() < 1e-4
+    assert np.array_equal(out["pk_obs"], ref["pk_obs"])
+    ok = ref["pk_obs"] > 0
+    assert np.abs(out["pk_p"][ok] / ref["pk_p"][ok] - 1).max() < 1e-8
+
+
 def test_pipeline_ma_fp64_vs_oracle(table, spline):
     N, L = 32, 128.0
     cfg = ml.ic_config(N, N, L, 42, table, method=ml.METHOD_MONGE_AMPERE, pk_bins=12, pk_linear=True,
