@@ -298,3 +298,16 @@ def test_thermal_invalid_momentum_reports_status_8(prec):
     finally:
         ml.thermal_sampler_free(st)
     assert np.all(np.isfinite(out)) and np.abs(out).max() > 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [1, 7, 129])
+def test_thermal_few_particles(n):
+    """fewer particles than one block's threads (one particle a thread)"""
+    vel = np.random.default_rng(n).standard_normal((n, 3)).astype(np.float32)
+    st = oracle.rng_state(99, 5)
+    ref = oracle.thermal(ml.BOSON, T_NU, 0.06, 1 / 32.0, C_KMS, st, vel)
+    out = vel.copy()
+    st2 = _gpu_thermal(ml.BOSON, T_NU, st, out, ml.FP64)
+    assert _ulps(out, ref).max() <= 1
+    assert np.array_equal(st2, oracle.rng_state(99, 5 + 7 * n))
