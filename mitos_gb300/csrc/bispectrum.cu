@@ -5,6 +5,11 @@
 // delta_1^2 delta_3 over the N^3 cells.  The bin of every |n|^2 comes from the same table as
 // calc_cross_powerspec's log bins (float u, src/calc_powerspec.c:62).  Empty bins keep zeros; the
 // reference's per-bin printf is not reproduced.
+//
+// The reference skips a bin whose shell 1 or shell 3 holds no mode (:436); the host knows those
+// counts from the bin tables, so every bin is enqueued without a wait and the sums come back in one
+// copy at the end.  When shell 3 is shell 1 (bins3 = bins and k3 in bin i: the equilateral case),
+// the two masks are the same array, so one c2r serves both (the second would be bit-identical).
 #include <math.h>
 #include <string.h>
 
@@ -52,7 +57,7 @@ __global__ void k_bispec_mask(int N, double dk, const cplx<T> *__restrict__ f, c
             }
         }
         o1[id] = v1;
-        o3[id] = v3;
+        if (o3) o3[id] = v3;
     }
     for (int off = 16; off > 0; off >>= 1) {
         s1 += __shfl_down_sync(0xffffffffu, s1, off);
@@ -95,8 +100,12 @@ int bispectrum_run(int N, double boxlen, int prec, const void *fbox, int bins, i
     const GridGeom &g = *gp;
     const size_t gb = (size_t)g.cells * csize(prec);
     const int *tab1 = bin_table(N, bins, 0, boxlen), *tab3 = bin_table(N, bins3, 0, boxlen);
+    const double *ks1, *ks3;
+    const long long *cn1, *cn3;
+    if (bin_geometry(N, bins, 0, boxlen, &ks1, &cn1) || bin_geometry(N, bins3, 0, boxlen, &ks3, &cn3)) return 5;
     void *o1 = workspace(gb, 30), *o3 = workspace(gb, 31), *m1 = workspace(gb, 32), *m3 = workspace(gb, 33);
-    double *acc = (double *)workspace(sizeof(double) * 5, 34);
+    // per bin: [k1 sum, k3 sum, k1 multiplicity, k3 multiplicity, sum delta_1^2 delta_3]
+    double *acc = (double *)workspace(sizeof(double) * 5 * bins, 34);
     if (!tab1 || !tab3 || !o1 || !o3 || !m1 || !m3 || !acc) return 5;
     const double dk = 2 * M_PI / boxlen;
     const double max_k = sqrt(3) * dk * N / 2;
@@ -109,9 +118,11 @@ int bispectrum_run(int N, double boxlen, int prec, const void *fbox, int bins, i
         k3_in_bins[i] = 0;
         bispectrum[i] = 0;
     }
+    MITOS_CUDA(cudaMemsetAsync(acc, 0, sizeof(double) * 5 * bins, stream()));
     const long total = (long)N * N * (N / 2 + 1);
     int blocks = (int)((total + 255) / 256);
     if (blocks > 152 * 8) blocks = 152 * 8;
+    std::vector<char> done(bins, 0);
     for (int i = 0; i < bins; i++) {
         // src/calc_powerspec.c:347-369, host libm as in the reference
         int required_bin3;
@@ -127,37 +138,45 @@ int bispectrum_run(int N, double boxlen, int prec, const void *fbox, int bins, i
         } else {
             required_bin3 = 0;
         }
-        MITOS_CUDA(cudaMemsetAsync(acc, 0, sizeof(double) * 5, stream()));
+        // src/calc_powerspec.c:436: a shell without modes skips the bin
+        const long long c1 = cn1[i];
+        const long long c3 = (required_bin3 >= 0 && required_bin3 < bins3) ? cn3[required_bin3] : 0;
+        if (c1 == 0 || c3 == 0) continue;
+        done[i] = 1;
+        const bool same = bins == bins3 && required_bin3 == i;
+        double *ab = acc + 5 * (size_t)i;
         launch_begin("bispec_mask");
         if (prec == MITOS_FP32)
             k_bispec_mask<float><<<blocks, 256, 0, stream()>>>(N, dk, (const float2 *)fbox, tab1, tab3, i, required_bin3,
-                                                               volume_mode, (float2 *)o1, (float2 *)o3, acc);
+                                                               volume_mode, (float2 *)o1, same ? nullptr : (float2 *)o3, ab);
         else
             k_bispec_mask<double><<<blocks, 256, 0, stream()>>>(N, dk, (const double2 *)fbox, tab1, tab3, i,
                                                                 required_bin3, volume_mode, (double2 *)o1,
-                                                                (double2 *)o3, acc);
+                                                                same ? nullptr : (double2 *)o3, ab);
         count_launch();
         MITOS_LAUNCH_CHECK("bispectrum mask");
-        double h[5];
-        MITOS_CUDA(cudaMemcpyAsync(h, acc, sizeof(double) * 4, cudaMemcpyDeviceToHost, stream()));
-        MITOS_CUDA(cudaStreamSynchronize(stream()));
-        if (h[2] == 0 || h[3] == 0) continue;  // src/calc_powerspec.c:436
         int e = grid_c2r(g, prec, boxlen, o1, m1);
-        if (!e) e = grid_c2r(g, prec, boxlen, o3, m3);
+        if (!e && !same) e = grid_c2r(g, prec, boxlen, o3, m3);
         if (e) return e;
+        const void *m3s = same ? m1 : m3;
         launch_begin("bispec_sum");
         if (prec == MITOS_FP32)
-            k_triple_sum<float><<<152 * 8, 256, 0, stream()>>>(N, (const float *)m1, (const float *)m3, acc + 4);
+            k_triple_sum<float><<<152 * 8, 256, 0, stream()>>>(N, (const float *)m1, (const float *)m3s, ab + 4);
         else
-            k_triple_sum<double><<<152 * 8, 256, 0, stream()>>>(N, (const double *)m1, (const double *)m3, acc + 4);
+            k_triple_sum<double><<<152 * 8, 256, 0, stream()>>>(N, (const double *)m1, (const double *)m3s, ab + 4);
         count_launch();
         MITOS_LAUNCH_CHECK("bispectrum sum");
-        MITOS_CUDA(cudaMemcpyAsync(h + 4, acc + 4, sizeof(double), cudaMemcpyDeviceToHost, stream()));
-        MITOS_CUDA(cudaStreamSynchronize(stream()));
-        bispectrum[i] = h[4];
-        k1_in_bins[i] = h[0] / h[2];
-        k2_in_bins[i] = h[0] / h[2];
-        k3_in_bins[i] = h[1] / h[3];
+    }
+    std::vector<double> h(5 * (size_t)bins);
+    MITOS_CUDA(cudaMemcpyAsync(h.data(), acc, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, stream()));
+    MITOS_CUDA(cudaStreamSynchronize(stream()));
+    for (int i = 0; i < bins; i++) {
+        if (!done[i]) continue;
+        const double *hb = h.data() + 5 * (size_t)i;
+        bispectrum[i] = hb[4];
+        k1_in_bins[i] = hb[0] / hb[2];
+        k2_in_bins[i] = hb[0] / hb[2];
+        k3_in_bins[i] = hb[1] / hb[3];
     }
     return 0;
 }

@@ -29,13 +29,16 @@ def _gpu_bispectrum_host(N, L, f, bins, bins3, vol, btype, theta, k3):
     return dict(zip(("k1", "k2", "k3", "B"), out))
 
 
-@pytest.mark.parametrize("N,btype,vol", [(32, 0, False), (32, 1, False), (32, 0, True), (48, 0, False)])
-def test_bispectrum_fp64_vs_oracle(N, btype, vol):
+@pytest.mark.parametrize("N,btype,vol,bins3", [(32, 0, False, 10), (32, 1, False, 10), (32, 0, True, 10),
+                                              (48, 0, False, 10), (32, 0, False, 14)])
+def test_bispectrum_fp64_vs_oracle(N, btype, vol, bins3):
+    """bins3 = bins with type 0 and theta = 4 pi / 3 puts shell 3 on shell 1 (one c2r serves both);
+    bins3 != bins and type 1 take two"""
     L = 4.0 * N
     f = _field(N, L, 3)
-    args = dict(bins=10, bins3=10, vol=vol, btype=btype, theta=4 * np.pi / 3, k3=0.4)
+    args = dict(bins=10, bins3=bins3, vol=vol, btype=btype, theta=4 * np.pi / 3, k3=0.4)
     got = _gpu_bispectrum_host(N, L, None if vol else f, **args)
-    ref = oracle.bispectrum(N, L, None if vol else f, bins=10, bins3=10, volume_mode=vol, btype=btype,
+    ref = oracle.bispectrum(N, L, None if vol else f, bins=10, bins3=bins3, volume_mode=vol, btype=btype,
                             theta=4 * np.pi / 3, k3=0.4)
     full = ref["B"] != 0
     assert full.sum() >= 3
