@@ -298,8 +298,21 @@ def extras(ml, table, spline, args) -> dict:
     t0 = time.perf_counter()
     bsp = ml.calc_bispectrum(gb_, 16, 16, btype=0, theta=4 * np.pi / 3)
     ml.calc_bispectrum(gb_, 16, 16, volume_mode=True, btype=0, theta=4 * np.pi / 3)
-    out["bispectrum"] = {"N": N, "bins": 16, "ms_field_and_volumes": (time.perf_counter() - t0) * 1e3,
-                         "nonempty_bins": int(np.count_nonzero(bsp["k1"]))}
+    ms_eq = (time.perf_counter() - t0) * 1e3
+    # squeezed (type 1, k3 = 0.02 h/Mpc): two c2r a bin; kernel times of the field call
+    ml.kernel_timing(True)
+    ml.calc_bispectrum(gb_, 16, 16, btype=1, k3=0.02)
+    kt = ml.kernel_times()
+    ml.kernel_timing(False)
+    Gb = N * N * (N // 2 + 1) * 8
+    mk = [t for n_, t in kt if n_ == "bispec_mask"]
+    sk = [t for n_, t in kt if n_ == "bispec_sum"]
+    out["bispectrum"] = {"N": N, "bins": 16, "ms_field_and_volumes": ms_eq,
+                         "nonempty_bins": int(np.count_nonzero(bsp["k1"])),
+                         "squeezed_field_ms": sum(t for _, t in kt),
+                         # mask: the field read, two masks written (3 G); sum: two real grids read (2 G)
+                         "mask_ms": sum(mk) / max(len(mk), 1), "mask_GBps": 3 * Gb / (sum(mk) / max(len(mk), 1) / 1e3) / 1e9,
+                         "sum_ms": sum(sk) / max(len(sk), 1), "sum_GBps": 2 * Gb / (sum(sk) / max(len(sk), 1) / 1e3) / 1e9}
     ml.free_local_grid(gb_)
 
     # 48 realisations (16 x 64^3 / 256, 16 x 96^3 / 384, 16 x 128^3 / 512 Mpc/h; 4 Mpc/h cells),
