@@ -224,6 +224,11 @@ int alloc_local_grid_prec(struct distributed_grid *dg, int N, double boxlen, MPI
 /* Copy a grid between host and device.  which = 0: fbox (N*N*(N/2+1) complex),
  * which = 1: box (N*N*(N+2) reals).  Element type follows dg->precision. */
 int dg_copy_to_host(const struct distributed_grid *dg, int which, void *host);
+/* The /Field/Field dataset of writeFieldFile_dg (src/output_mpi.c:52-141): the real-space grid as
+ * N x N x (N + 2) doubles, padding included, from a grid of either precision (no reference
+ * counterpart; the HDF5 calls stay with the caller).  Returns 2 for a grid in momentum space, as
+ * the reference refuses it (:81-84). */
+int dg_field_to_host(const struct distributed_grid *dg, double *host);
 int dg_copy_from_host(struct distributed_grid *dg, int which, const void *host);
 
 /* Description of the last failure (empty when none), and the number of kernels launched. */
@@ -286,6 +291,9 @@ struct ic_config {
     double thermal_T_eV;        /* MicroscopyTemperature * kBoltzmann / ElectronVolt */
     double speed_of_light;      /* us.SpeedOfLight in internal units */
     uint64_t thermal_draw_offset; /* draws taken after the white noise by earlier thermal species */
+    /* snapshot datasets (ic_result.coords / vels / masses / ids) */
+    double particle_mass;        /* ptype->Mass (stored as float in struct particle, src/particle.c:104) */
+    long long id_first_particle; /* ptype->FirstID */
 };
 struct ic_result {
     double *pk_k;       /* host [pk_bins] */
@@ -299,6 +307,13 @@ struct ic_result {
                            potential from 2LPT with the reference's velocity factors (:453-455) for
                            2LPT configurations, else the inverse Poisson kernel (:457); plus the
                            thermal motion when cfg->thermal is set */
+    /* optional host arrays: the particle datasets of the snapshot as src/mitos.c:1106-1117 hands them
+     * to H5Dwrite (Coordinates, Velocities [M^3 * 3] and Masses [M^3] as double, ParticleIDs [M^3]),
+     * made on the device from the wrapped positions and the velocities; vels needs index_vel */
+    double *coords;
+    double *vels;
+    double *masses;
+    long long *ids;
 };
 int ic_pipeline_run(const struct ic_config *cfg, const struct perturb_spline *spline,
                     struct ic_result *res);

@@ -281,6 +281,21 @@ extern "C" int dg_copy_to_host(const struct distributed_grid *dg, int which, voi
     MITOS_CUDA(cudaMemcpyAsync(host, src, grid_bytes(dg), cudaMemcpyDeviceToHost, stream()));
     return sync_all();
 }
+extern "C" int dg_field_to_host(const struct distributed_grid *dg, double *host) {
+    if (!dg || !dg->box || !host) { set_error(1, "grid part not allocated"); return 1; }
+    if (dg->momentum_space == 1) { set_error(2, "attempting to export while in momentum space"); return 2; }
+    const long n = (long)dg->N * dg->N * (dg->N + 2);
+    if (dg->precision == MITOS_FP64) {
+        MITOS_CUDA(cudaMemcpyAsync(host, dg->box, sizeof(double) * n, cudaMemcpyDeviceToHost, stream()));
+    } else {
+        double *t = (double *)workspace(sizeof(double) * n, 23);
+        if (!t) return 5;
+        int e = widen_to_double(n, (const float *)dg->box, t);
+        if (e) return e;
+        MITOS_CUDA(cudaMemcpyAsync(host, t, sizeof(double) * n, cudaMemcpyDeviceToHost, stream()));
+    }
+    return sync_all();
+}
 extern "C" int dg_copy_from_host(struct distributed_grid *dg, int which, const void *host) {
     void *dst = which == 0 ? (void *)dg->fbox : (void *)dg->box;
     if (!dst) { set_error(1, "grid part not allocated"); return 1; }

@@ -652,6 +652,47 @@ int velocity_gather(long np, int N, double boxlen, int precision, const float *p
     return 0;
 }
 
+// the particle datasets of the snapshot (src/mitos.c:1106-1117): Coordinates and Velocities as
+// double (from the float particle fields), Masses as double of the float mass, ParticleIDs the
+// row-major lattice index plus the species' first id (src/particle.c:114-121); any output may be null
+__global__ void k_snapshot(long n, const float *__restrict__ pos, const float *__restrict__ vel, float mass,
+                           long long id_first, double *__restrict__ coords, double *__restrict__ vels,
+                           double *__restrict__ masses, long long *__restrict__ ids) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        if (coords)
+            for (int c = 0; c < 3; c++) coords[3 * i + c] = (double)pos[3 * i + c];
+        if (vels)
+            for (int c = 0; c < 3; c++) vels[3 * i + c] = vel ? (double)vel[3 * i + c] : 0.0;
+        if (masses) masses[i] = (double)mass;
+        if (ids) ids[i] = id_first + i;
+    }
+}
+
+int snapshot_arrays(long n, const float *pos, const float *vel, float mass, long long id_first, double *coords,
+                    double *vels, double *masses, long long *ids) {
+    const unsigned blocks = (unsigned)std::min<long>((n + 255) / 256, 152L * 16);
+    launch_begin("snapshot");
+    k_snapshot<<<blocks, 256, 0, stream()>>>(n, pos, vel, mass, id_first, coords, vels, masses, ids);
+    count_launch();
+    MITOS_LAUNCH_CHECK("snapshot arrays");
+    return 0;
+}
+
+// real-space grid of either precision as doubles in its padded layout (N x N x (N + 2))
+__global__ void k_widen(long n, const float *__restrict__ src, double *__restrict__ dst) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        dst[i] = (double)src[i];
+}
+
+int widen_to_double(long n, const float *src, double *dst) {
+    const unsigned blocks = (unsigned)std::min<long>((n + 255) / 256, 152L * 16);
+    launch_begin("widen");
+    k_widen<<<blocks, 256, 0, stream()>>>(n, src, dst);
+    count_launch();
+    MITOS_LAUNCH_CHECK("widen to double");
+    return 0;
+}
+
 int cic_positions(long n, int N, double boxlen, int precision, const float *pos, double val, void *rho) {
     const double gfac = boxlen / N;
     const unsigned blocks = (unsigned)((n + 255) / 256);

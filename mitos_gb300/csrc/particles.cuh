@@ -22,5 +22,11 @@ int velocity_gather(long np, int N, double boxlen, int precision, const float *p
                     const void *v2, float *vel);
 // CIC of n given positions with per-particle value val
 int cic_positions(long n, int N, double boxlen, int precision, const float *pos, double val, void *rho);
+// snapshot particle datasets (src/mitos.c:1106-1117) from device positions / velocities (vel may be
+// null: zero velocities); outputs device, any may be null
+int snapshot_arrays(long n, const float *pos, const float *vel, float mass, long long id_first, double *coords,
+                    double *vels, double *masses, long long *ids);
+// n floats to doubles (device)
+int widen_to_double(long n, const float *src, double *dst);
 
 }  // namespace mitos

@@ -185,14 +185,15 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     // of realisation b at b * bs bytes from the first; one launch per pass covers all of them
     const int B = (opt && opt->batch > 1) ? opt->batch : 1;
     const size_t bs = B > 1 ? ((std::max(gb1, db1) + 255) & ~(size_t)255) : 0;
+    const bool want_snap = res && (res->coords || res->vels || res->masses || res->ids);
     if (B > 1 && (!opt->states || !opt->acc || cfg->method == MITOS_METHOD_MONGE_AMPERE || !aligned ||
-                  (res && res->pos))) {
+                  (res && res->pos) || want_snap)) {
         set_error(3, "batched runs need device start states and accumulators, a lattice-aligned "
                      "Zel'dovich or 2LPT configuration and no positions");
         return 3;
     }
     const size_t gb = B > 1 ? B * bs : gb1, db = B > 1 ? B * bs : db1;
-    const bool want_vel = res && res->vel;
+    const bool want_vel = res && (res->vel || res->vels);
     if (want_vel && (!tvlo || !tvhi || B > 1)) {
         set_error(1, "velocities need a velocity transfer function (ic_config.index_vel) and an unbatched run");
         return 1;
@@ -406,7 +407,7 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     float *dpos = nullptr, *dposraw = nullptr;
     const int pslot = (opt && opt->async_slot >= 0) ? opt->async_slot : 0;
     const size_t pos_bytes = sizeof(float) * 3 * (size_t)M * M * M;
-    if (res && res->pos) {
+    if (res && (res->pos || want_snap)) {
         dpos = (float *)workspace(pos_bytes, 108 + pslot);
         if (!dpos) return 5;
     }
@@ -426,7 +427,7 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     e = aligned ? lattice_deposit(N, L, prec, D0, D1, D2, disp_pitch, rhoD, rho_pitch, dpos, B, bs, dposraw)
                 : displace_and_deposit(N, M, L, prec, D0, D1, D2, rhoD, dpos, dposraw);
     if (e) return e;
-    if (dpos) {
+    if (res && res->pos) {
         MITOS_CUDA(cudaEventRecord(pos_event(pslot, 0), stream()));
         MITOS_CUDA(cudaStreamWaitEvent(copy_stream(), pos_event(pslot, 0), 0));
         MITOS_CUDA(cudaMemcpyAsync(res->pos, dpos, pos_bytes, cudaMemcpyDeviceToHost, copy_stream()));
@@ -440,10 +441,11 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     // order potential otherwise (:457), the TSC window undone (:461-467), three derivative grids
     // (:470-483, pitch N + 2, no on-node stencil: the gather is at displaced positions), and the
     // TSC gather of each at the unwrapped positions.  Every workspace of S1-S4 is free again here.
+    float *dvel = nullptr;
     if (want_vel) {
         T *filtv = (T *)workspace(sizeof(T) * (n2max + 1), 116);
         void *V0 = workspace(gb, 19), *V1 = workspace(gb, 20), *V2 = workspace(gb, 21);
-        float *dvel = (float *)workspace(pos_bytes, 110 + pslot);
+        dvel = (float *)workspace(pos_bytes, 110 + pslot);
         if (!filtv || !V0 || !V1 || !V2 || !dvel) return 5;
         if ((e = filter_launch(dtab + 3 * k_size, 1, filtv))) return e;
         e = noise_generate(g, prec, L, st, filtv, phi);
@@ -516,9 +518,31 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
             if (e) return e;
         }
         // to the caller on the copy stream, behind the positions (pos_event(pslot, 1) then covers both)
+        if (res->vel) {
+            MITOS_CUDA(cudaEventRecord(pos_event(pslot, 0), stream()));
+            MITOS_CUDA(cudaStreamWaitEvent(copy_stream(), pos_event(pslot, 0), 0));
+            MITOS_CUDA(cudaMemcpyAsync(res->vel, dvel, pos_bytes, cudaMemcpyDeviceToHost, copy_stream()));
+            MITOS_CUDA(cudaEventRecord(pos_event(pslot, 1), copy_stream()));
+        }
+    }
+
+    // the particle datasets of the snapshot (src/mitos.c:1106-1117), made on the device from the
+    // wrapped positions and the velocities, to the caller on the copy stream behind the rest
+    if (want_snap) {
+        const long np = (long)M * M * M;
+        double *dc = res->coords ? (double *)workspace(2 * pos_bytes, 160 + 4 * pslot) : nullptr;
+        double *dv = res->vels ? (double *)workspace(2 * pos_bytes, 161 + 4 * pslot) : nullptr;
+        double *dm = res->masses ? (double *)workspace(sizeof(double) * np, 162 + 4 * pslot) : nullptr;
+        long long *di = res->ids ? (long long *)workspace(sizeof(long long) * np, 163 + 4 * pslot) : nullptr;
+        if ((res->coords && !dc) || (res->vels && !dv) || (res->masses && !dm) || (res->ids && !di)) return 5;
+        e = snapshot_arrays(np, dpos, dvel, (float)cfg->particle_mass, cfg->id_first_particle, dc, dv, dm, di);
+        if (e) return e;
         MITOS_CUDA(cudaEventRecord(pos_event(pslot, 0), stream()));
         MITOS_CUDA(cudaStreamWaitEvent(copy_stream(), pos_event(pslot, 0), 0));
-        MITOS_CUDA(cudaMemcpyAsync(res->vel, dvel, pos_bytes, cudaMemcpyDeviceToHost, copy_stream()));
+        if (dc) MITOS_CUDA(cudaMemcpyAsync(res->coords, dc, 2 * pos_bytes, cudaMemcpyDeviceToHost, copy_stream()));
+        if (dv) MITOS_CUDA(cudaMemcpyAsync(res->vels, dv, 2 * pos_bytes, cudaMemcpyDeviceToHost, copy_stream()));
+        if (dm) MITOS_CUDA(cudaMemcpyAsync(res->masses, dm, sizeof(double) * np, cudaMemcpyDeviceToHost, copy_stream()));
+        if (di) MITOS_CUDA(cudaMemcpyAsync(res->ids, di, sizeof(long long) * np, cudaMemcpyDeviceToHost, copy_stream()));
         MITOS_CUDA(cudaEventRecord(pos_event(pslot, 1), copy_stream()));
     }
 
@@ -691,7 +715,8 @@ int finish_slot(int k) {
     if (!s.busy) return 0;
     s.busy = false;
     MITOS_CUDA(cudaEventSynchronize(acc_event(k)));
-    if (s.res && (s.res->pos || s.res->vel)) MITOS_CUDA(cudaEventSynchronize(pos_event(k, 1)));
+    if (s.res && (s.res->pos || s.res->vel || s.res->coords || s.res->vels || s.res->masses || s.res->ids))
+        MITOS_CUDA(cudaEventSynchronize(pos_event(k, 1)));
     if (!s.res) return 0;
     const double *ksum;
     const long long *count;

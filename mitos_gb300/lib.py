@@ -85,7 +85,8 @@ class ICConfig(ctypes.Structure):
                 ("keep_outputs", ctypes.c_int), ("index_vel", ctypes.c_int),
                 ("thermal", ctypes.c_int), ("thermal_M_eV", ctypes.c_double),
                 ("thermal_T_eV", ctypes.c_double), ("speed_of_light", ctypes.c_double),
-                ("thermal_draw_offset", ctypes.c_uint64)]
+                ("thermal_draw_offset", ctypes.c_uint64),
+                ("particle_mass", ctypes.c_double), ("id_first_particle", ctypes.c_longlong)]
 
 
 class Interval(ctypes.Structure):
@@ -109,7 +110,8 @@ FERMION, BOSON = 1, 2
 
 class ICResult(ctypes.Structure):
     _fields_ = [("pk_k", _dp), ("pk_p", _dp), ("pk_obs", _lp), ("pos", _fp),
-                ("ma_iterations", ctypes.c_int), ("ma_residual", ctypes.c_double), ("vel", _fp)]
+                ("ma_iterations", ctypes.c_int), ("ma_residual", ctypes.c_double), ("vel", _fp),
+                ("coords", _dp), ("vels", _dp), ("masses", _dp), ("ids", ctypes.POINTER(ctypes.c_longlong))]
 
 
 _lib = None
@@ -347,14 +349,15 @@ def cic_deposit_dg(rho, pos: np.ndarray, mass: float) -> float:
 def ic_config(N, M, boxlen, seed, table, method=METHOD_2LPT, pk_bins=32, pk_linear=True,
               precision=FP32, z_ini=31.0, ma_cycles=0, ma_tol=0.0, index_src=0, index_vel=None,
               thermal=0, thermal_M_eV=0.0, thermal_T_eV=0.0, speed_of_light=0.0,
-              thermal_draw_offset=0) -> ICConfig:
+              thermal_draw_offset=0, particle_mass=1.0, id_first_particle=0) -> ICConfig:
     """index_vel: the velocity transfer function (default: the table's ``t_cdm`` when it has one);
     thermal: FERMION or BOSON adds thermal motion to the velocities (0: none)"""
     if index_vel is None:
         index_vel = table.index_of("t_cdm") if "t_cdm" in getattr(table, "titles", []) else -1
     return ICConfig(N, M, boxlen, seed, table.A_s, table.n_s, table.k_pivot, z_ini, index_src,
                     method, ma_cycles, ma_tol, pk_bins, int(pk_linear), precision, 0, index_vel,
-                    int(thermal), thermal_M_eV, thermal_T_eV, speed_of_light, thermal_draw_offset)
+                    int(thermal), thermal_M_eV, thermal_T_eV, speed_of_light, thermal_draw_offset,
+                    particle_mass, id_first_particle)
 
 
 def thermal_sampler(kind: int, T_eV: float) -> Sampler:
@@ -410,16 +413,30 @@ def calc_bispectrum(g, bins, bins3, volume_mode=False, btype=0, theta=0.0, k3=0.
     return {"k1": k1, "k2": k2, "k3": k3o, "B": b}
 
 
-def ic_pipeline_run(cfg: ICConfig, spline: Spline, want_pos: bool = False, want_vel: bool = False) -> dict:
+def ic_pipeline_run(cfg: ICConfig, spline: Spline, want_pos: bool = False, want_vel: bool = False,
+                    want_snapshot: bool = False) -> dict:
+    """want_snapshot: the snapshot datasets coords, vels (with index_vel), masses and ids"""
     bins = cfg.pk_bins
     k = np.zeros(bins)
     p = np.zeros(bins)
     o = np.zeros(bins, np.int64)
-    pos = np.zeros((cfg.M ** 3, 3), np.float32) if want_pos else None
-    vel = np.zeros((cfg.M ** 3, 3), np.float32) if want_vel else None
+    n = cfg.M ** 3
+    pos = np.zeros((n, 3), np.float32) if want_pos else None
+    vel = np.zeros((n, 3), np.float32) if want_vel else None
+    snap = {}
+    if want_snapshot:
+        snap = {"coords": np.zeros((n, 3)), "masses": np.zeros(n), "ids": np.zeros(n, np.int64)}
+        if cfg.index_vel >= 0:
+            snap["vels"] = np.zeros((n, 3))
     res = ICResult(k.ctypes.data_as(_dp), p.ctypes.data_as(_dp), o.ctypes.data_as(_lp),
                    pos.ctypes.data_as(_fp) if pos is not None else None, 0, 0.0,
                    vel.ctypes.data_as(_fp) if vel is not None else None)
+    if snap:
+        res.coords = snap["coords"].ctypes.data_as(_dp)
+        res.masses = snap["masses"].ctypes.data_as(_dp)
+        res.ids = snap["ids"].ctypes.data_as(ctypes.POINTER(ctypes.c_longlong))
+        if "vels" in snap:
+            res.vels = snap["vels"].ctypes.data_as(_dp)
     _check(load().ic_pipeline_run(ctypes.byref(cfg), ctypes.byref(spline.sp), ctypes.byref(res)))
     out = {"pk_k": k, "pk_p": p, "pk_obs": o, "ma_iterations": res.ma_iterations,
            "ma_residual": res.ma_residual}
@@ -427,6 +444,14 @@ def ic_pipeline_run(cfg: ICConfig, spline: Spline, want_pos: bool = False, want_
         out["pos"] = pos
     if vel is not None:
         out["vel"] = vel
+    out.update(snap)
+    return out
+
+
+def field_to_host(dg) -> np.ndarray:
+    """dg_field_to_host: the /Field/Field dataset (N, N, N + 2) doubles of a real-space grid"""
+    out = np.zeros((dg.N, dg.N, dg.N + 2))
+    _check(load().dg_field_to_host(ctypes.byref(dg), out.ctypes.data_as(_dp)))
     return out
 
 
