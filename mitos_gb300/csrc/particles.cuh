@@ -16,10 +16,10 @@ int lattice_deposit(int N, double boxlen, int precision, const void *d0, const v
                     int disp_pitch, void *rho, int rho_pitch, float *pos_out, int batch = 1, size_t bstride = 0,
                     float *posraw_out = nullptr);
 bool lattice_aligned(int N, int M, double boxlen);
-// particle velocities: TSC gather of the three velocity grids (pitch N + 2) at the unwrapped
-// positions pos (np x 3), float velocities out (np x 3)
-int velocity_gather(long np, int N, double boxlen, int precision, const float *pos, const void *v0, const void *v1,
-                    const void *v2, float *vel);
+// particle velocities: TSC gather of the three velocity grids (row pitch `pitch` reals) at the
+// unwrapped positions pos (np x 3), float velocities out (np x 3)
+int velocity_gather(long np, int N, int pitch, double boxlen, int precision, const float *pos, const void *v0,
+                    const void *v1, const void *v2, float *vel);
 // CIC of n given positions with per-particle value val
 int cic_positions(long n, int N, double boxlen, int precision, const float *pos, double val, void *rho);
 // snapshot particle datasets (src/mitos.c:1106-1117) from device positions / velocities (vel may be

@@ -444,7 +444,11 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     float *dvel = nullptr;
     if (want_vel) {
         T *filtv = (T *)workspace(sizeof(T) * (n2max + 1), 116);
-        void *V0 = workspace(gb, 19), *V1 = workspace(gb, 20), *V2 = workspace(gb, 21);
+        // velocity grids: pitch N + 4 for the lattice-aligned gather (16-byte aligned rows for its
+        // tile staging), N + 2 otherwise
+        const int vpitch = aligned ? N + 4 : N + 2;
+        const size_t vb = (size_t)N * N * vpitch * sizeof(T);
+        void *V0 = workspace(vb, 19), *V1 = workspace(vb, 20), *V2 = workspace(vb, 21);
         dvel = (float *)workspace(pos_bytes, 110 + pslot);
         if (!filtv || !V0 || !V1 || !V2 || !dvel) return 5;
         if ((e = filter_launch(dtab + 3 * k_size, 1, filtv))) return e;
@@ -501,10 +505,10 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
         a.out[0] = V0;
         a.out[1] = V1;
         a.out[2] = V2;
-        a.rp_out = N + 2;
+        a.rp_out = vpitch;
         a.scale = 1.0 / V;
         e = launch_z_c2r<T>(g, ZOP_DISP, a);
-        if (!e) e = velocity_gather((long)M * M * M, N, L, prec, dposraw, V0, V1, V2, dvel);
+        if (!e) e = velocity_gather((long)M * M * M, N, vpitch, L, prec, dposraw, V0, V1, V2, dvel);
         if (e) return e;
         // thermal motion (src/mitos.c:910-1064) from the stream the white noise left: four draws a
         // mode with k > 0 (src/grf.c:47-63), then those of earlier thermal species

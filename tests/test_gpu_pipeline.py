@@ -141,6 +141,18 @@ def test_velocities_fp64_vs_oracle(N, M, method, table, spline):
     assert err < 1e-8, err
 
 
+def test_velocities_large_displacements(table, spline):
+    """z = 0 in 1 Mpc/h cells: the velocity gather's particles leave its staged tiles and read global
+    memory; still the oracle's velocities"""
+    N, L = 64, 64.0
+    iv = table.index_of("t_cdm")
+    cfg = ml.ic_config(N, N, L, 5, table, pk_bins=12, precision=ml.FP64, index_vel=iv, z_ini=0.0)
+    out = ml.ic_pipeline_run(cfg, spline, want_vel=True)
+    ref = oracle.ic_pipeline(oracle.ic_params(N, N, L, 5, table, pk_bins=12, index_vel=iv, z_ini=0.0),
+                             want=("vel", "pk"))
+    assert rel_err(out["vel"], ref["vel"]) < 1e-8
+
+
 def test_velocities_leave_positions_and_pk_unchanged(table, spline):
     N, L = 64, 256.0
     cfg = ml.ic_config(N, N, L, 9, table, pk_bins=16, precision=ml.FP32)
