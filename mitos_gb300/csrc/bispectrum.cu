@@ -20,44 +20,50 @@
 
 namespace mitos {
 
-// acc: [k1 sum, k3 sum, k1 multiplicity, k3 multiplicity]
+// acc: [k1 sum, k3 sum, k1 multiplicity, k3 multiplicity].  One warp a row (x, y) of the half-complex
+// grid, its lanes along z (one division a row, none an element).
+// The shells are the |n|^2 ranges [lo1, hi1] and [lo3, hi3] of the bins (log bins are monotone in
+// |n|^2), so the mask needs no table reads.
 template <typename T>
-__global__ void k_bispec_mask(int N, double dk, const cplx<T> *__restrict__ f, const int *__restrict__ tab1,
-                              const int *__restrict__ tab3, int b1, int b3, int volume, cplx<T> *__restrict__ o1,
-                              cplx<T> *__restrict__ o3, double *acc) {
+__global__ void k_bispec_mask(int N, double dk, const cplx<T> *__restrict__ f, int lo1, int hi1, int lo3, int hi3,
+                              int volume, cplx<T> *__restrict__ o1, cplx<T> *__restrict__ o3, double *acc) {
     const int H = N / 2 + 1;
-    const long total = (long)N * N * H;
+    const int lane = threadIdx.x & 31;
+    const long warps = (long)gridDim.x * (blockDim.x >> 5);
     double s1 = 0, s3 = 0, c1 = 0, c3 = 0;
-    for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < total; id += (long)gridDim.x * blockDim.x) {
-        const int z = (int)(id % H);
-        const long xy = id / H;
-        const int y = (int)(xy % N), x = (int)(xy / N);
+    for (long row = (long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); row < (long)N * N; row += warps) {
+        const int x = (int)(row / N), y = (int)(row - (long)x * N);
         const int jx = kint(x, N), jy = kint(y, N);
-        const long n2 = (long)jx * jx + (long)jy * jy + (long)z * z;
-        cplx<T> v1 = mk<T>(0, 0), v3 = mk<T>(0, 0);
-        if (n2 > 0) {
-            const int bb1 = tab1[n2], bb3 = tab3[n2];
-            if (bb1 == b1 || bb3 == b3) {
-                const cplx<T> val = volume ? mk<T>(1, 0) : f[id];
-                const double mult = (z == 0 || z == N / 2) ? 1.0 : 2.0;
-                // fft_wavevector's k (src/fft.c:29-35), without contractions
-                const double kx = __dmul_rn((double)jx, dk), ky = __dmul_rn((double)jy, dk),
-                             kz = __dmul_rn((double)z, dk);
-                const double k = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(kx, kx), __dmul_rn(ky, ky)), __dmul_rn(kz, kz)));
-                if (bb1 == b1) {
-                    v1 = val;
-                    s1 += mult * k;
-                    c1 += mult;
-                }
-                if (bb3 == b3) {
-                    v3 = val;
-                    s3 += mult * k;
-                    c3 += mult;
+        const int b2 = jx * jx + jy * jy;
+        const long base = row * H;
+        for (int z = lane; z < H; z += 32) {
+            const long id = base + z;
+            const int n2 = b2 + z * z;
+            cplx<T> v1 = mk<T>(0, 0), v3 = mk<T>(0, 0);
+            if (n2 > 0) {
+                const bool in1 = n2 >= lo1 && n2 <= hi1, in3 = n2 >= lo3 && n2 <= hi3;
+                if (in1 || in3) {
+                    const cplx<T> val = volume ? mk<T>(1, 0) : f[id];
+                    const double mult = (z == 0 || z == N / 2) ? 1.0 : 2.0;
+                    // fft_wavevector's k (src/fft.c:29-35), without contractions
+                    const double kx = __dmul_rn((double)jx, dk), ky = __dmul_rn((double)jy, dk),
+                                 kz = __dmul_rn((double)z, dk);
+                    const double k = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(kx, kx), __dmul_rn(ky, ky)), __dmul_rn(kz, kz)));
+                    if (in1) {
+                        v1 = val;
+                        s1 += mult * k;
+                        c1 += mult;
+                    }
+                    if (in3) {
+                        v3 = val;
+                        s3 += mult * k;
+                        c3 += mult;
+                    }
                 }
             }
+            o1[id] = v1;
+            if (o3) o3[id] = v3;
         }
-        o1[id] = v1;
-        if (o3) o3[id] = v3;
     }
     for (int off = 16; off > 0; off >>= 1) {
         s1 += __shfl_down_sync(0xffffffffu, s1, off);
@@ -65,7 +71,7 @@ __global__ void k_bispec_mask(int N, double dk, const cplx<T> *__restrict__ f, c
         c1 += __shfl_down_sync(0xffffffffu, c1, off);
         c3 += __shfl_down_sync(0xffffffffu, c3, off);
     }
-    if ((threadIdx.x & 31) == 0 && (c1 != 0 || c3 != 0)) {
+    if (lane == 0 && (c1 != 0 || c3 != 0)) {
         atomicAdd(acc, s1);
         atomicAdd(acc + 1, s3);
         atomicAdd(acc + 2, c1);
@@ -73,19 +79,22 @@ __global__ void k_bispec_mask(int N, double dk, const cplx<T> *__restrict__ f, c
     }
 }
 
-// sum of m1^2 m3 over the N^3 cells of two padded real grids (row pitch N + 2)
+// sum of m1^2 m3 over the N^3 cells of two padded real grids (row pitch N + 2): one warp a row
 template <typename T>
 __global__ void k_triple_sum(int N, const T *__restrict__ m1, const T *__restrict__ m3, double *out) {
-    const long total = (long)N * N * N;
+    const int lane = threadIdx.x & 31;
+    const long warps = (long)gridDim.x * (blockDim.x >> 5);
     T s = 0;
-    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
-        const long o = (i / N) * (N + 2) + i % N;
-        const T a = m1[o];
-        s += a * a * m3[o];
+    for (long row = (long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); row < (long)N * N; row += warps) {
+        const T *r1 = m1 + row * (N + 2), *r3 = m3 + row * (N + 2);
+        for (int z = lane; z < N; z += 32) {
+            const T a = r1[z];
+            s += a * a * r3[z];
+        }
     }
     double d = (double)s;
     for (int off = 16; off > 0; off >>= 1) d += __shfl_down_sync(0xffffffffu, d, off);
-    if ((threadIdx.x & 31) == 0) atomicAdd(out, d);
+    if (lane == 0) atomicAdd(out, d);
 }
 
 int bispectrum_run(int N, double boxlen, int prec, const void *fbox, int bins, int bins3, double *k1_in_bins,
@@ -99,14 +108,13 @@ int bispectrum_run(int N, double boxlen, int prec, const void *fbox, int bins, i
     if (!gp) return 3;
     const GridGeom &g = *gp;
     const size_t gb = (size_t)g.cells * csize(prec);
-    const int *tab1 = bin_table(N, bins, 0, boxlen), *tab3 = bin_table(N, bins3, 0, boxlen);
     const double *ks1, *ks3;
     const long long *cn1, *cn3;
     if (bin_geometry(N, bins, 0, boxlen, &ks1, &cn1) || bin_geometry(N, bins3, 0, boxlen, &ks3, &cn3)) return 5;
     void *o1 = workspace(gb, 30), *o3 = workspace(gb, 31), *m1 = workspace(gb, 32), *m3 = workspace(gb, 33);
     // per bin: [k1 sum, k3 sum, k1 multiplicity, k3 multiplicity, sum delta_1^2 delta_3]
     double *acc = (double *)workspace(sizeof(double) * 5 * bins, 34);
-    if (!tab1 || !tab3 || !o1 || !o3 || !m1 || !m3 || !acc) return 5;
+    if (!o1 || !o3 || !m1 || !m3 || !acc) return 5;
     const double dk = 2 * M_PI / boxlen;
     const double max_k = sqrt(3) * dk * N / 2;
     const double min_k = dk;
@@ -144,14 +152,19 @@ int bispectrum_run(int N, double boxlen, int prec, const void *fbox, int bins, i
         if (c1 == 0 || c3 == 0) continue;
         done[i] = 1;
         const bool same = bins == bins3 && required_bin3 == i;
+        long lo1, hi1, lo3, hi3;
+        int er = bin_n2_range(N, bins, 0, boxlen, i, &lo1, &hi1);
+        if (!er) er = bin_n2_range(N, bins3, 0, boxlen, required_bin3, &lo3, &hi3);
+        if (er) return er;
         double *ab = acc + 5 * (size_t)i;
         launch_begin("bispec_mask");
         if (prec == MITOS_FP32)
-            k_bispec_mask<float><<<blocks, 256, 0, stream()>>>(N, dk, (const float2 *)fbox, tab1, tab3, i, required_bin3,
-                                                               volume_mode, (float2 *)o1, same ? nullptr : (float2 *)o3, ab);
+            k_bispec_mask<float><<<blocks, 256, 0, stream()>>>(N, dk, (const float2 *)fbox, (int)lo1, (int)hi1, (int)lo3,
+                                                               (int)hi3, volume_mode, (float2 *)o1,
+                                                               same ? nullptr : (float2 *)o3, ab);
         else
-            k_bispec_mask<double><<<blocks, 256, 0, stream()>>>(N, dk, (const double2 *)fbox, tab1, tab3, i,
-                                                                required_bin3, volume_mode, (double2 *)o1,
+            k_bispec_mask<double><<<blocks, 256, 0, stream()>>>(N, dk, (const double2 *)fbox, (int)lo1, (int)hi1,
+                                                                (int)lo3, (int)hi3, volume_mode, (double2 *)o1,
                                                                 same ? nullptr : (double2 *)o3, ab);
         count_launch();
         MITOS_LAUNCH_CHECK("bispectrum mask");

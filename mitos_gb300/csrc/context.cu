@@ -258,6 +258,8 @@ struct BinEntry {
     std::vector<int> host;
     std::vector<double> ksum;        // sum over modes of multiplicity * |k| per bin
     std::vector<long long> count;    // sum over modes of multiplicity per bin
+    std::vector<long> lo, hi;        // |n|^2 range of each bin (lo > hi: empty)
+    std::vector<char> contiguous;    // the bin's |n|^2 values form that one range
 };
 static std::map<std::tuple<int, int, int, double>, BinEntry *> g_bins;
 static std::map<int, std::vector<long long>> g_n2hist;
@@ -306,6 +308,16 @@ static BinEntry *bin_entry(int N, int bins, int linear, double boxlen) {
             }
         }
     }
+    be->lo.assign(bins, 1);
+    be->hi.assign(bins, 0);
+    be->contiguous.assign(bins, 1);
+    for (long n2 = 1; n2 <= n2max; n2++) {
+        const int b = tab[n2];
+        if (b < 0) continue;
+        if (be->lo[b] > be->hi[b]) be->lo[b] = n2;
+        else if (be->hi[b] != n2 - 1) be->contiguous[b] = 0;
+        be->hi[b] = n2;
+    }
     be->ksum.assign(bins, 0.0);
     be->count.assign(bins, 0);
     for (long n2 = 1; n2 <= n2max; n2++) {
@@ -322,6 +334,24 @@ const int *bin_table(int N, int bins, int linear, double boxlen) {
     std::lock_guard<std::mutex> lk(g_mu);
     BinEntry *be = bin_entry(N, bins, linear, boxlen);
     return be ? be->dev : nullptr;
+}
+
+int bin_n2_range(int N, int bins, int linear, double boxlen, int b, long *lo, long *hi) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    BinEntry *be = bin_entry(N, bins, linear, boxlen);
+    if (!be) return 5;
+    if (b < 0 || b >= bins) {  // no mode falls in a bin outside the table: an empty range
+        *lo = 1;
+        *hi = 0;
+        return 0;
+    }
+    if (!be->contiguous[b]) {
+        set_error(3, "bin %d is not one range of |n|^2", b);
+        return 3;
+    }
+    *lo = be->lo[b];
+    *hi = be->hi[b];
+    return 0;
 }
 
 int bin_geometry(int N, int bins, int linear, double boxlen, const double **ksum, const long long **count) {

@@ -8,6 +8,9 @@ namespace mitos {
 const void *window_table(int N, int order, int precision);
 const void *stencil_table(int N, int precision);
 const int *bin_table(int N, int bins, int linear, double boxlen);
+// the |n|^2 range [lo, hi] of bin b (bins are monotone in |n|^2, so one range; lo > hi when empty);
+// status 3 if the bin's |n|^2 values are not contiguous
+int bin_n2_range(int N, int bins, int linear, double boxlen, int b, long *lo, long *hi);
 // per-bin multiplicity-weighted mode counts and |k| sums of the half-complex grid (host arrays)
 int bin_geometry(int N, int bins, int linear, double boxlen, const double **ksum, const long long **count);
 // grid-sized scratch buffer number `slot` of `bytes` bytes (kept until mitos_release_all)
