@@ -310,8 +310,9 @@ def extras(ml, table, spline, args) -> dict:
     out["bispectrum"] = {"N": N, "bins": 16, "ms_field_and_volumes": ms_eq,
                          "nonempty_bins": int(np.count_nonzero(bsp["k1"])),
                          "squeezed_field_ms": sum(t for _, t in kt),
-                         # mask: the field read, two masks written (3 G); sum: two real grids read (2 G)
-                         "mask_ms": sum(mk) / max(len(mk), 1), "mask_GBps": 3 * Gb / (sum(mk) / max(len(mk), 1) / 1e3) / 1e9,
+                         # mask: two masks written (2 G; the field is read in the shells only);
+                         # sum: two real grids read (2 G)
+                         "mask_ms": sum(mk) / max(len(mk), 1), "mask_GBps": 2 * Gb / (sum(mk) / max(len(mk), 1) / 1e3) / 1e9,
                          "sum_ms": sum(sk) / max(len(sk), 1), "sum_GBps": 2 * Gb / (sum(sk) / max(len(sk), 1) / 1e3) / 1e9}
     ml.free_local_grid(gb_)
 
