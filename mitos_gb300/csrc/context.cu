@@ -426,6 +426,8 @@ extern "C" long mitos_launch_count(void) { return mitos::g_launches; }
 extern "C" int mitos_release_all(void) {
     cudaDeviceSynchronize();
     mitos::release_all();
+    mitos::release_jump_tables();
+    mitos::release_thermal_tables();
     return 0;
 }
 

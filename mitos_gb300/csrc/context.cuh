@@ -20,6 +20,9 @@ void *workspace(size_t bytes, int slot);
 int set_tiles(int N, int precision, int p_xy, int p_z);
 int get_tiles(int N, int precision, int *p_xy, int *p_z);
 void release_all();
+// the cached xoshiro jump-polynomial tables (noise.cu) and thermal sampler tables (thermal.cu)
+void release_jump_tables();
+void release_thermal_tables();
 
 // white noise (noise.cu)
 struct NoiseFilter {

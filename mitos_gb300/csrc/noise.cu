@@ -244,6 +244,14 @@ const uint64_t *affine_jump_polys(unsigned long long first, unsigned long long s
     return d;
 }
 
+void release_jump_tables() {
+    std::lock_guard<std::mutex> lk(g_nmu);
+    for (auto &kv : g_ptabs) cudaFree(kv.second);
+    g_ptabs.clear();
+    for (auto &kv : g_atabs) cudaFree(kv.second);
+    g_atabs.clear();
+}
+
 #define NOISE_THREADS 128
 #define NOISE_CHUNK 16
 

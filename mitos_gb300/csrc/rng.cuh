@@ -135,7 +135,7 @@ __device__ __forceinline__ void jump_state(const ulonglong4 *tab, const uint64_t
 }
 
 // device table of the polynomials x^(first + stride c) mod p, c < count (four words each); cached
-// per (first, stride, count) for the life of the library
+// per (first, stride, count) until mitos_release_all
 const uint64_t *affine_jump_polys(unsigned long long first, unsigned long long stride, long count);
 
 }  // namespace mitos

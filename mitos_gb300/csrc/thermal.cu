@@ -387,7 +387,7 @@ static int thermal_launch(int prec, long n, const uint64_t s0[4], unsigned long 
     return 0;
 }
 
-// sampler tables of the pipeline's species, per (kind, T): device copies kept until exit
+// sampler tables of the pipeline's species, per (kind, T): device copies kept until mitos_release_all
 struct CachedTable {
     void *dev;
     int n;
@@ -396,6 +396,12 @@ static std::mutex g_tmu;
 static std::map<std::pair<int, double>, CachedTable> g_tables;
 
 static int sampler_build(struct sampler *s, int kind, double T_eV);
+
+void release_thermal_tables() {
+    std::lock_guard<std::mutex> lk(g_tmu);
+    for (auto &kv : g_tables) cudaFree(kv.second.dev);
+    g_tables.clear();
+}
 
 int thermal_add(int prec, long n, const uint64_t seed_state[4], unsigned long long skip, int kind, double T_eV,
                 double M_eV, double a_ini, double c, float *dvel, long stride, int *derr) {

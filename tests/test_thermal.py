@@ -311,3 +311,23 @@ def test_thermal_few_particles(n):
     st2 = _gpu_thermal(ml.BOSON, T_NU, st, out, ml.FP64)
     assert _ulps(out, ref).max() <= 1
     assert np.array_equal(st2, oracle.rng_state(99, 5 + 7 * n))
+
+
+@pytest.mark.gpu
+def test_release_all_then_rerun(table, spline):
+    """mitos_release_all frees the cached jump and sampler tables with the workspaces; the next calls
+    rebuild them and give the same results"""
+    N, L = 32, 128.0
+    iv = table.index_of("t_cdm")
+    cfg = ml.ic_config(N, N, L, 42, table, pk_bins=12, precision=ml.FP32, index_vel=iv, thermal=ml.FERMION,
+                       thermal_M_eV=0.06, thermal_T_eV=T_NU, speed_of_light=C_KMS)
+    a = ml.ic_pipeline_run(cfg, spline, want_vel=True)
+    v = np.zeros((5000, 3), np.float32)
+    st = oracle.rng_state(3, 0)
+    va = v.copy()
+    _gpu_thermal(ml.FERMION, T_NU, st, va, ml.FP32)
+    assert ml.load().mitos_release_all() == 0
+    b = ml.ic_pipeline_run(cfg, spline, want_vel=True)
+    vb = v.copy()
+    _gpu_thermal(ml.FERMION, T_NU, st, vb, ml.FP32)
+    assert np.array_equal(a["vel"], b["vel"]) and np.array_equal(va, vb)
