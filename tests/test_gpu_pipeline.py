@@ -153,6 +153,18 @@ def test_velocities_large_displacements(table, spline):
     assert rel_err(out["vel"], ref["vel"]) < 1e-8
 
 
+def test_velocities_256_fp32_vs_fp64(table, spline):
+    """the 256^3 test configuration (L = 500, seed 7): FP32 velocities (tiled gather) against FP64"""
+    N, L = 256, 500.0
+    o = {}
+    for prec in (ml.FP32, ml.FP64):
+        cfg = ml.ic_config(N, N, L, 7, table, pk_bins=16, precision=prec)
+        o[prec] = ml.ic_pipeline_run(cfg, spline, want_vel=True)["vel"]
+    err = rel_err(o[ml.FP32], o[ml.FP64])
+    print(f"velocities FP32 vs FP64 at 256^3: rel err {err:.3e}")
+    assert err < 2e-5
+
+
 def test_velocities_leave_positions_and_pk_unchanged(table, spline):
     N, L = 64, 256.0
     cfg = ml.ic_config(N, N, L, 9, table, pk_bins=16, precision=ml.FP32)
