@@ -15,27 +15,27 @@ def _wrapdiff(a, b, L):
     return d - L * np.round(d / L)
 
 
-@pytest.mark.parametrize("prec", [ml.FP64, ml.FP32])
-def test_snapshot_datasets(prec, table, spline):
+@pytest.mark.parametrize("prec,M", [(ml.FP64, 32), (ml.FP32, 32), (ml.FP32, 16)])
+def test_snapshot_datasets(prec, M, table, spline):
     """Coordinates / Velocities are the float particle fields as double (wrapped positions, velocities
     with thermal motion), Masses the float mass as double, ParticleIDs the row-major lattice index plus
     FirstID (src/particle.c:114-121); the positions also match the oracle's"""
     N, L = 32, 128.0
     iv = table.index_of("t_cdm")
-    cfg = ml.ic_config(N, N, L, 42, table, pk_bins=12, precision=prec, index_vel=iv, thermal=ml.FERMION,
+    cfg = ml.ic_config(N, M, L, 42, table, pk_bins=12, precision=prec, index_vel=iv, thermal=ml.FERMION,
                        thermal_M_eV=0.06, thermal_T_eV=1.68e-4, speed_of_light=299792.458,
                        particle_mass=3.3e-3, id_first_particle=1000)
     out = ml.ic_pipeline_run(cfg, spline, want_pos=True, want_vel=True, want_snapshot=True)
-    n = N ** 3
+    n = M ** 3
     assert np.array_equal(out["coords"], out["pos"].astype(np.float64))
     assert np.array_equal(out["vels"], out["vel"].astype(np.float64))
     assert np.array_equal(out["masses"], np.full(n, np.float32(3.3e-3), np.float64))
     assert np.array_equal(out["ids"], np.arange(n, dtype=np.int64) + 1000)
     assert out["coords"].min() >= 0 and out["coords"].max() < L
-    ref = oracle.ic_pipeline(oracle.ic_params(N, N, L, 42, table, pk_bins=12), want=("pos",))
+    ref = oracle.ic_pipeline(oracle.ic_params(N, M, L, 42, table, pk_bins=12), want=("pos",))
     assert np.abs(_wrapdiff(out["coords"], ref["pos"], L)).max() < 1e-4
     # without velocities requested the snapshot has no Velocities array; the rest is the same
-    cfg0 = ml.ic_config(N, N, L, 42, table, pk_bins=12, precision=prec, index_vel=-1, particle_mass=3.3e-3,
+    cfg0 = ml.ic_config(N, M, L, 42, table, pk_bins=12, precision=prec, index_vel=-1, particle_mass=3.3e-3,
                         id_first_particle=1000)
     o0 = ml.ic_pipeline_run(cfg0, spline, want_snapshot=True)
     assert "vels" not in o0

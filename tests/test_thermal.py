@@ -213,17 +213,18 @@ def test_thermal_fp32_large_ragged():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("prec", [ml.FP64, ml.FP32])
-def test_pipeline_thermal_vs_oracle(prec, table, spline):
+@pytest.mark.parametrize("prec,M", [(ml.FP64, 32), (ml.FP32, 32), (ml.FP64, 16)])
+def test_pipeline_thermal_vs_oracle(prec, M, table, spline):
     """the pipeline's thermal stage: the species' draws start after the white noise's (and after
-    thermal_draw_offset more), on top of the gathered velocities"""
+    thermal_draw_offset more), on top of the gathered velocities; M = N (lattice-aligned deposit and
+    gather) and M < N (the general ones)"""
     N, L = 32, 128.0
     iv = table.index_of("t_cdm")
     for kind, off in ((ml.FERMION, 0), (ml.BOSON, 4242)):
-        cfg = ml.ic_config(N, N, L, 42, table, pk_bins=12, precision=prec, index_vel=iv, thermal=kind,
+        cfg = ml.ic_config(N, M, L, 42, table, pk_bins=12, precision=prec, index_vel=iv, thermal=kind,
                            thermal_M_eV=0.06, thermal_T_eV=T_NU, speed_of_light=C_KMS, thermal_draw_offset=off)
         out = ml.ic_pipeline_run(cfg, spline, want_vel=True)
-        ref = oracle.ic_pipeline(oracle.ic_params(N, N, L, 42, table, pk_bins=12, index_vel=iv, thermal=kind,
+        ref = oracle.ic_pipeline(oracle.ic_params(N, M, L, 42, table, pk_bins=12, index_vel=iv, thermal=kind,
                                                   thermal_T_eV=T_NU, thermal_M_eV=0.06, speed_of_light=C_KMS,
                                                   thermal_draw_offset=off), want=("vel", "pk"))
         if prec == ml.FP64:
