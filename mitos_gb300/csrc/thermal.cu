@@ -11,10 +11,10 @@
 //
 // The sampler's piece choice compares u = (double)w / 2^64 (w the 64-bit draw; (double)UINT64_MAX
 // is 2^64) with the pieces' CDF values.  Each comparison is exact in integers: the host finds, per
-// piece, the largest w with u <= Fr.  Both precisions therefore pick the reference's piece for
-// every draw.  The
-// FP64 build then evaluates the cubic, the momentum, the directions (GPU libm) and the float update
-// with the reference's operations and rounding; the FP32 build evaluates them in float from the same
+// piece, the largest w with u <= Fr, and a 1024-bucket table over the top bits of w gives the piece
+// to start from.  Both precisions therefore pick the reference's piece for every draw.  The FP64
+// build then evaluates the cubic, the momentum, the directions (GPU libm) and the float update with
+// the reference's operations and rounding; the FP32 build evaluates them in float from the same
 // piece (u - Fl taken exactly in integers first, so the cancellation costs no precision), with
 // normals whose cosine is accurate near its zeros (a normalised triple of small normals would
 // magnify an absolute error).
