@@ -379,6 +379,9 @@ int thermal_velocities(const struct sampler *s, rng_state *state, long n, double
  * reference's cleanSampler). */
 int thermal_sampler_init(struct sampler *s, int kind, double T_eV);
 int thermal_sampler_free(struct sampler *s);
+/* Host-only check (no GPU): the piece thermal_velocities' kernel takes for each 64-bit draw w[i]
+ * (exact integer thresholds on u = w / 2^64, no reference counterpart); returns 0 or 3. */
+int mitos_thermal_pieces(const struct sampler *s, const uint64_t *w, long n, int *piece);
 
 /* P(k) binning that allocates no device memory.  No counterpart in the reference: for callers
  * that must not allocate device memory in their loop, because another allocator already holds

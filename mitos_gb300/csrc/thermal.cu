@@ -505,6 +505,24 @@ extern "C" int thermal_sampler_free(struct sampler *s) {
     return 0;
 }
 
+// the kernel's piece choice for n draws w, on the host from the same table image (no GPU): the
+// threshold compares and bucket table the kernel reads
+extern "C" int mitos_thermal_pieces(const struct sampler *s, const uint64_t *w, long n, int *piece) {
+    using namespace mitos;
+    std::vector<unsigned char> img;
+    int nn = 0;
+    const int e = table_image(s, img, nn);
+    if (e) return e;
+    const ThermPiece *pc = (const ThermPiece *)img.data();
+    const unsigned short *bucket = (const unsigned short *)(img.data() + sizeof(ThermPiece) * nn);
+    for (long i = 0; i < n; i++) {
+        int pk = bucket[w[i] >> (64 - kBucketBits)];
+        while (pk + 1 < nn && w[i] > pc[pk + 1].le) pk++;
+        piece[i] = pk;
+    }
+    return 0;
+}
+
 extern "C" int thermal_velocities(const struct sampler *s, rng_state *state, long n, double M_eV, double a_ini,
                                   double speed_of_light, float *vel, long stride) {
     using namespace mitos;

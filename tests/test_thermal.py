@@ -63,6 +63,64 @@ def test_sampler_moments():
         assert abs(d.mean() / mean - 1) < 0.01, d.mean()
 
 
+def _reference_pick(Fr, r, table, w):
+    """samplerCustom's piece choice (src/random.c:264-281), restated literally in Python doubles"""
+    u = float(np.uint64(w).astype(np.float64)) / 18446744073709551616.0  # (double)UINT64_MAX = 2^64
+    t = int(np.floor(u * 1000))
+    idx = int(table[t if t < 1000 else 999])
+    rmax, pick = 0.0, idx
+    for i in range(idx, len(Fr)):
+        if Fr[i] < u and r[i] > rmax:
+            rmax, pick = r[i], i
+        else:
+            break
+    return pick
+
+
+@pytest.mark.parametrize("kind", [ml.FERMION, ml.BOSON])
+def test_kernel_piece_choice_is_the_reference_scan(kind):
+    """the kernel's integer piece choice (thresholds on w and a bucket table; evaluated on the host
+    from the same table image) equals the reference scan on u = w / 2^64 for random draws and for
+    the draws around every threshold, search-table step and bucket edge, and the extremes"""
+    import ctypes
+    from fractions import Fraction
+    s = ml.thermal_sampler(kind, T_NU)
+    try:
+        rows, table = ml.sampler_rows(s), ml.sampler_index(s)
+        Fr, r = rows[:, 3], rows[:, 1]
+        ws = set(int(x) for x in np.random.default_rng(kind).integers(0, 2 ** 63, 40000, dtype=np.uint64))
+        ws |= set(int(x) * 2 + 1 for x in np.random.default_rng(kind + 5).integers(0, 2 ** 63, 20000, dtype=np.uint64))
+        edges = [int(Fraction(f) * 2 ** 64) for f in Fr] + [int(Fraction(i, 1000) * 2 ** 64) for i in range(1, 1001)]
+        for e in edges:
+            ws.update(w for w in range(e - 2100, e + 2100, 37) if 0 <= w < 2 ** 64)
+            ws.update(w for w in (e - 1, e, e + 1) if 0 <= w < 2 ** 64)
+        # the exact threshold of each piece: the largest w with (double)w / 2^64 <= Fr, and the next w
+        for f in Fr:
+            lo, hi = 0, 2 ** 64 - 1
+            if float(np.uint64(hi).astype(np.float64)) / 2.0 ** 64 <= f:
+                continue
+            while hi - lo > 1:
+                mid = (lo + hi) // 2
+                if float(np.uint64(mid).astype(np.float64)) / 2.0 ** 64 <= f:
+                    lo = mid
+                else:
+                    hi = mid
+            ws.update((lo, lo + 1))
+        for b in range(1024):
+            ws.update(w for w in ((b << 54) - 1, b << 54, (b << 54) + 1) if 0 <= w < 2 ** 64)
+        ws.update((0, 1, 2 ** 64 - 1, 2 ** 64 - 1024, 2 ** 64 - 1025, 2 ** 64 - 2048))
+        w = np.array(sorted(ws), np.uint64)
+        got = np.zeros(w.size, np.int32)
+        assert ml.load().mitos_thermal_pieces(ctypes.byref(s), w.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                                             ctypes.c_long(w.size),
+                                             got.ctypes.data_as(ctypes.POINTER(ctypes.c_int))) == 0
+        want = np.array([_reference_pick(Fr, r, table, int(x)) for x in w])
+        bad = np.nonzero(got != want)[0]
+        assert bad.size == 0, (w[bad[:5]], got[bad[:5]], want[bad[:5]])
+    finally:
+        ml.thermal_sampler_free(s)
+
+
 @pytest.mark.parametrize("kind,T", CASES)
 def test_library_sampler_matches_oracle(kind, T):
     """thermal_sampler_init is host code (no GPU): its pieces, search table and norm equal the oracle's"""
