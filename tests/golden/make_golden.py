@@ -8,6 +8,10 @@ needs the reference tree) through oracle.ref_* and stores small fixtures:
   pipeline.npz       positions and P(k) of src/mitos.c + analyse/src/mitos_read.c at 16^3 / 32^3
   thermal.npz        initSampler pieces and search tables (src/random.c:87-209), samplerCustom
                      draws (:261-289) and the thermal-motion loop of src/mitos.c:928-1062
+  bispectrum.npz     calc_bispectrum (src/calc_powerspec.c:295-508) of a 16^3 / 32^3 field, types 0
+                     and 1, field and volume mode
+  velocity.npz       particle velocities of src/mitos.c:425-490,865-908 (t_cdm) at 16^3, 2LPT and
+                     Zel'dovich
 Usage: python tests/golden/make_golden.py
 """
 import os
@@ -46,6 +50,8 @@ def main():
         fx[name + "_pk"] = out["pk_p"]
     np.savez_compressed(os.path.join(HERE, "pipeline.npz"), **fx)
     thermal_fixture()
+    bispectrum_fixture()
+    velocity_fixture()
     print("golden vectors written to", HERE)
 
 
@@ -69,6 +75,35 @@ def thermal_fixture():
         fx[name + "_vel_in"] = vel
         fx[name + "_vel_out"] = oracle.ref_thermal(kind, T, 0.06, 1 / 32.0, 299792.458, st, vel)
     np.savez_compressed(os.path.join(HERE, "thermal.npz"), **fx)
+
+
+
+BISPEC_CASES = ((16, 0, False), (16, 1, False), (32, 0, False), (16, 0, True))
+
+
+def bispectrum_fixture():
+    oracle.build(ref=True)
+    fx = {}
+    for N, btype, vol in BISPEC_CASES:
+        L = 4.0 * N
+        f = oracle.apply_kernel(N, L, oracle.grf(N, L, 3), "gaussian", np.sqrt(1 / 0.02))
+        name = f"b_{N}_{btype}_{int(vol)}"
+        r = oracle.ref_bispectrum(N, L, None if vol else f, 8, 8, volume_mode=vol, btype=btype,
+                                  theta=4 * np.pi / 3, k3=0.4)
+        for key in ("k1", "k2", "k3", "B"):
+            fx[f"{name}_{key}"] = r[key]
+    np.savez_compressed(os.path.join(HERE, "bispectrum.npz"), **fx)
+
+
+def velocity_fixture():
+    oracle.build(ref=True)
+    table = load_table()
+    fx = {}
+    for lpt in (2, 1):
+        prm = oracle.ic_params(16, 16, 64.0, 42, table, lpt_order=lpt, pk_bins=8,
+                               index_vel=table.index_of("t_cdm"))
+        fx[f"v_16_{lpt}"] = oracle.ref_ic_pipeline(prm, want=("vel", "pk"))["vel"]
+    np.savez_compressed(os.path.join(HERE, "velocity.npz"), **fx)
 
 
 if __name__ == "__main__":

@@ -46,6 +46,28 @@ def test_golden_pipeline(table):
         assert np.array_equal(out["pk_p"], g[name + "_pk"], equal_nan=True), name
 
 
+def test_golden_bispectrum():
+    """the oracle's calc_bispectrum against the reference build's outputs (carried to machines
+    without the reference tree)"""
+    g = np.load(os.path.join(GOLDEN, "bispectrum.npz"))
+    for name in sorted({k.rsplit("_", 1)[0] for k in g.files}):
+        N, btype, vol = [int(v) for v in name.split("_")[1:]]
+        L = 4.0 * N
+        f = oracle.apply_kernel(N, L, oracle.grf(N, L, 3), "gaussian", np.sqrt(1 / 0.02))
+        r = oracle.bispectrum(N, L, None if vol else f, 8, 8, volume_mode=bool(vol), btype=btype,
+                              theta=4 * np.pi / 3, k3=0.4)
+        for key in ("k1", "k2", "k3", "B"):
+            assert np.array_equal(r[key], g[f"{name}_{key}"]), (name, key)
+
+
+def test_golden_velocities(table):
+    """the oracle's particle velocities against the reference build's (16^3, 2LPT and Zel'dovich)"""
+    g = np.load(os.path.join(GOLDEN, "velocity.npz"))
+    for lpt in (2, 1):
+        prm = oracle.ic_params(16, 16, 64.0, 42, table, lpt_order=lpt, pk_bins=8, index_vel=table.index_of("t_cdm"))
+        assert np.array_equal(oracle.ic_pipeline(prm, want=("vel", "pk"))["vel"], g[f"v_16_{lpt}"]), lpt
+
+
 @pytest.mark.skipif(oracle.ref_lib() is None, reason="reference build not present here")
 @pytest.mark.parametrize("N,lin,lpt,ma", [(16, True, 2, 0), (32, False, 2, 0), (16, True, 1, 0),
                                           (16, False, 2, 2)])
