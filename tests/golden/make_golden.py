@@ -12,6 +12,8 @@ needs the reference tree) through oracle.ref_* and stores small fixtures:
                      and 1, field and volume mode
   velocity.npz       particle velocities of src/mitos.c:425-490,865-908 (t_cdm) at 16^3, 2LPT and
                      Zel'dovich
+  stages.npz         every stage grid of the 2LPT and Monge-Ampere (3 cycles) ICs at 16^3: noise,
+                     delta(k), phi(k), the displacement grids and the CIC overdensity
 Usage: python tests/golden/make_golden.py
 """
 import os
@@ -52,6 +54,7 @@ def main():
     thermal_fixture()
     bispectrum_fixture()
     velocity_fixture()
+    stages_fixture()
     print("golden vectors written to", HERE)
 
 
@@ -104,6 +107,20 @@ def velocity_fixture():
                                index_vel=table.index_of("t_cdm"))
         fx[f"v_16_{lpt}"] = oracle.ref_ic_pipeline(prm, want=("vel", "pk"))["vel"]
     np.savez_compressed(os.path.join(HERE, "velocity.npz"), **fx)
+
+
+
+def stages_fixture():
+    oracle.build(ref=True)
+    table = load_table()
+    fx = {}
+    want = ("grf", "delta_k", "phi_k", "disp", "rho", "pk")
+    for lpt, ma in ((2, 0), (2, 3)):
+        prm = oracle.ic_params(16, 16, 64.0, 42, table, lpt_order=lpt, ma_cycles=ma, pk_bins=8)
+        out = oracle.ref_ic_pipeline(prm, want=want)
+        for key in ("grf", "delta_k", "phi_k", "disp0", "disp1", "disp2", "rho"):
+            fx[f"s_{lpt}_{ma}_{key}"] = out[key]
+    np.savez_compressed(os.path.join(HERE, "stages.npz"), **fx)
 
 
 if __name__ == "__main__":

@@ -60,6 +60,17 @@ def test_golden_bispectrum():
             assert np.array_equal(r[key], g[f"{name}_{key}"]), (name, key)
 
 
+def test_golden_stages(table):
+    """every stage grid of the oracle's 2LPT and Monge-Ampere ICs at 16^3 against the reference
+    build's (noise, delta(k), phi(k), displacement grids, CIC overdensity)"""
+    g = np.load(os.path.join(GOLDEN, "stages.npz"))
+    for lpt, ma in ((2, 0), (2, 3)):
+        prm = oracle.ic_params(16, 16, 64.0, 42, table, lpt_order=lpt, ma_cycles=ma, pk_bins=8)
+        out = oracle.ic_pipeline(prm, want=("grf", "delta_k", "phi_k", "disp", "rho", "pk"))
+        for key in ("grf", "delta_k", "phi_k", "disp0", "disp1", "disp2", "rho"):
+            assert np.array_equal(out[key], g[f"s_{lpt}_{ma}_{key}"]), (lpt, ma, key)
+
+
 def test_golden_velocities(table):
     """the oracle's particle velocities against the reference build's (16^3, 2LPT and Zel'dovich)"""
     g = np.load(os.path.join(GOLDEN, "velocity.npz"))
