@@ -71,3 +71,26 @@ def test_bispectrum_dg_fp32_vs_fp64():
     with pytest.raises(ml.MitosError):  # not in momentum space
         ml.calc_bispectrum(g, 12, 12)
     ml.free_local_grid(g)
+
+
+def test_bispectrum_256_fp32_vs_fp64():
+    """256^3 (the mask, c2r and triple-sum kernels at a size whose grids together exceed L2): the FP32
+    grid form against FP64, equilateral, bins above 1e-6 of the largest"""
+    N, L = 256, 500.0
+    out = {}
+    for prec in (ml.FP32, ml.FP64):
+        g = ml.alloc_local_grid(N, L, prec)
+        try:
+            ml.generate_complex_grf(g, ml.rng_init(9))
+            g.momentum_space = b"\x01"
+            out[prec] = ml.calc_bispectrum(g, 12, 12, btype=0, theta=4 * np.pi / 3)
+        finally:
+            ml.free_local_grid(g)
+    a, b = out[ml.FP32], out[ml.FP64]
+    assert np.array_equal(a["k1"] == 0, b["k1"] == 0)
+    assert np.allclose(a["k1"], b["k1"], rtol=1e-12)
+    big = np.abs(b["B"]) > 1e-6 * np.abs(b["B"]).max()
+    assert big.sum() >= 6
+    rel = np.abs(a["B"][big] / b["B"][big] - 1)
+    print(f"bispectrum FP32 vs FP64 at 256^3: max rel {rel.max():.2e}")
+    assert rel.max() < 1e-3
