@@ -390,3 +390,29 @@ def test_release_all_then_rerun(table, spline):
     vb = v.copy()
     _gpu_thermal(ml.FERMION, T_NU, st, vb, ml.FP32)
     assert np.array_equal(a["vel"], b["vel"]) and np.array_equal(va, vb)
+
+
+def test_reference_built_sampler_is_accepted():
+    """the drop-in case: a struct sampler filled from the reference's own initSampler (its pieces in
+    its order, its search table) is taken by the library, with the same piece choice as the literal
+    samplerCustom scan (CPU: the kernel's table, evaluated on the host)"""
+    import ctypes
+    _needs_ref()
+    for kind, T in CASES:
+        ref = oracle.ref_sampler_table(kind, T)
+        rows, table = ref["pieces"], ref["table"]
+        n = rows.shape[0]
+        iv = (ml.Interval * n)()
+        for j in range(n):
+            iv[j].id = j
+            iv[j].l, iv[j].r, iv[j].Fl, iv[j].Fr, iv[j].a0, iv[j].a1, iv[j].a2, iv[j].a3 = rows[j]
+            iv[j].nid = j + 1
+        index = (ctypes.c_double * 1000)(*[float(t) for t in table])
+        s = ml.Sampler(ref["norm"], 1e-10 * T, 15.0 * T, None, None, iv, n, 1000, index)
+        w = np.random.default_rng(kind).integers(0, 2 ** 63, 20000, dtype=np.uint64) * np.uint64(2)
+        got = np.zeros(w.size, np.int32)
+        assert ml.load().mitos_thermal_pieces(ctypes.byref(s), w.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                                             ctypes.c_long(w.size),
+                                             got.ctypes.data_as(ctypes.POINTER(ctypes.c_int))) == 0
+        want = np.array([_reference_pick(rows[:, 3], rows[:, 1], table, int(x)) for x in w])
+        assert np.array_equal(got, want), (kind, T)
