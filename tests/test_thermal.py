@@ -416,3 +416,29 @@ def test_reference_built_sampler_is_accepted():
                                              got.ctypes.data_as(ctypes.POINTER(ctypes.c_int))) == 0
         want = np.array([_reference_pick(rows[:, 3], rows[:, 1], table, int(x)) for x in w])
         assert np.array_equal(got, want), (kind, T)
+
+
+def test_thermal_arguments_checked_before_any_launch():
+    """empty and invalid inputs are settled on the host (no GPU): n = 0 leaves the stream where it is;
+    a bad stride, mass or scale factor is status 1; pieces out of order are status 3"""
+    import ctypes
+    s = ml.thermal_sampler(ml.FERMION, T_NU)
+    try:
+        st = oracle.rng_state(1, 0)
+        v = np.zeros((10, 3), np.float32)
+        assert np.array_equal(ml.thermal_velocities(s, st, v, 0.06, 1 / 32.0, C_KMS, n=0), st)
+        for args, kw in (((0.06, 1 / 32.0), dict(stride=2)), ((0.0, 1 / 32.0), {}), ((0.06, -1.0), {})):
+            with pytest.raises(ml.MitosError) as e:
+                ml.thermal_velocities(s, st, v, *args, C_KMS, **kw)
+            assert e.value.code == 1
+        n = s.intervalNum
+        rev = (ml.Interval * n)(*[s.intervals[n - 1 - j] for j in range(n)])
+        bad = ml.Sampler(s.norm, s.xl, s.xr, None, None, rev, n, s.I_max, s.index)
+        with pytest.raises(ml.MitosError) as e:
+            ml.thermal_velocities(bad, st, v, 0.06, 1 / 32.0, C_KMS)
+        assert e.value.code == 3
+        out = np.zeros(4, np.int32)
+        assert ml.load().mitos_thermal_pieces(ctypes.byref(bad), np.zeros(4, np.uint64).ctypes.data_as(
+            ctypes.POINTER(ctypes.c_uint64)), ctypes.c_long(4), out.ctypes.data_as(ctypes.POINTER(ctypes.c_int))) == 3
+    finally:
+        ml.thermal_sampler_free(s)
