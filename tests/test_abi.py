@@ -77,3 +77,45 @@ def test_host_kernel_callbacks_follow_reference():
     assert k.kern[0] == -1.0 / k.k / k.k and k.kern[1] == 0
     lib.kernel_dy(ctypes.byref(k))
     assert k.kern[0] == 0 and k.kern[1] == -0.2
+
+
+def _check_layouts(tmp_path, include_dir, header, structs):
+    """compile a program printing sizeof / offsetof of each struct against `header` and compare them
+    with the ctypes mirrors"""
+    import shutil
+    import subprocess
+    import pytest
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lines = ["#include <stdio.h>", "#include <stddef.h>", f'#include "{header}"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof(struct {cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'printf("{cname} {fname} %zu\\n", offsetof(struct {cname}, {fname}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c11", "-I", include_dir, str(src), "-o", str(exe)], check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.splitlines():
+        c, f, v = line.split()
+        got[(c, f)] = int(v)
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
+
+
+def test_struct_layouts_match_ctypes(tmp_path):
+    """every struct the Python binding mirrors has the header's field offsets and size"""
+    _check_layouts(tmp_path, os.path.join(ROOT, "include"), "mitos_gb300.h",
+                   {"distributed_grid": ml.DistributedGrid, "ic_config": ml.ICConfig, "ic_result": ml.ICResult,
+                    "interval": ml.Interval, "sampler": ml.Sampler, "xoshiro256ss_state": ml.RngState})
+
+
+def test_oracle_struct_layouts_match_ctypes(tmp_path):
+    """the oracle's parameter and output structs as the test binding mirrors them"""
+    _check_layouts(tmp_path, os.path.join(ROOT, "oracle"), "mitos_oracle.h",
+                   {"orc_ic_params": oracle.OrcICParams, "orc_ic_out": oracle.OrcICOut})
