@@ -226,7 +226,6 @@ static ThermTable table_view(const void *dev, int n) {
 // ---- kernel ------------------------------------------------------------------------------------
 #define THERMAL_THREADS 128
 #define THERMAL_CHUNK 8
-static_assert(THERMAL_CHUNK == 8, "the packed add loop divides f < 24 by 3 as (11 f) >> 5");
 
 // Shared memory: the block's table of A^i s0 (8 KB) while the threads jump to their start states,
 // then, in the same bytes, the bucket table, the thresholds and (FP32) the pieces.
@@ -235,12 +234,15 @@ __host__ __device__ constexpr size_t thermal_smem(int n) {
     return tables > 256 * sizeof(ulonglong4) ? tables : 256 * sizeof(ulonglong4);
 }
 
-template <typename T>
+// PACKED: velocities at stride 3 from a 16-byte aligned base and runs of a multiple of 4 particles,
+// so each thread adds its increments itself, three float4 a group of 4 particles (loaded before the
+// group computes); otherwise increments are staged in shared memory and the block adds them with
+// consecutive threads on consecutive addresses
+template <typename T, bool PACKED>
 __global__ void __launch_bounds__(THERMAL_THREADS, sizeof(T) == 4 ? 10 : 6)
 k_thermal(long n, int R, RngState s0, const uint64_t *__restrict__ polys, ThermTable tt, double a_ini, double M_eV,
           double c, float vfac, float *__restrict__ vel, long stride, int *err) {
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ T stage[THERMAL_THREADS][3 * THERMAL_CHUNK + 1];
     ulonglong4 *tab = (ulonglong4 *)smem;
     noise_state_table(s0, tab);
     const long g = (long)blockIdx.x * THERMAL_THREADS + threadIdx.x;
@@ -261,86 +263,111 @@ k_thermal(long n, int R, RngState s0, const uint64_t *__restrict__ polys, ThermT
     __syncthreads();
     const long block_first = (long)blockIdx.x * THERMAL_THREADS * R;
     bool bad = false;
-    const long rem = n - block_first;  // particles from the block's first on
-    for (int k0 = 0; k0 < R; k0 += THERMAL_CHUNK) {
-        // the velocities this chunk adds to, on their way to L2 while the chunk computes
-        if (first + k0 < n) {
-            const long last = min(first + k0 + THERMAL_CHUNK, min(first + R, n)) - 1;
-            prefetch_l2(vel + (first + k0) * stride);
-            prefetch_l2(vel + last * stride + 2);
-        }
-        for (int j = 0; j < THERMAL_CHUNK; j++) {
-            T d[3] = {0, 0, 0};
-            if (k0 + j < R && first + k0 + j < n) {
-                const uint64_t w = dnext(r0, r1, r2, r3);
-                int pk = sbk[w >> (64 - kBucketBits)];
-                while (pk + 1 < tt.n && w > sle[pk + 1]) pk++;
-                if constexpr (sizeof(T) == 8) {
-                    // src/random.c:284-286, src/mitos.c:935-965 with the reference's rounding
-                    const ThermPiece &P = tt.piece[pk];
-                    const double u = __dmul_rn(__ull2double_rn(w), 0x1p-64);
-                    const double v = __ddiv_rn(__dsub_rn(u, P.Fl), __dsub_rn(P.Fr, P.Fl));
-                    const double H = __dadd_rn(__dadd_rn(__dadd_rn(P.a0, __dmul_rn(P.a1, v)), __dmul_rn(__dmul_rn(P.a2, v), v)),
-                                               __dmul_rn(__dmul_rn(__dmul_rn(P.a3, v), v), v));
-                    const double p = __ddiv_rn(H, a_ini);
-                    bad |= isnan(p) || p <= 0;
-                    const double V = __dmul_rn(__ddiv_rn(p, M_eV), c);
-                    double e[3];
-                    for (int m = 0; m < 3; m++) {
-                        const uint64_t A = dnext(r0, r1, r2, r3), B = dnext(r0, r1, r2, r3);
-                        e[m] = gauss64(A, B);
-                    }
-                    const double len = hypot(e[0], hypot(e[1], e[2]));
-                    if (len > 0)
-                        for (int m = 0; m < 3; m++) e[m] = __ddiv_rn(e[m], len);
-                    for (int m = 0; m < 3; m++) d[m] = __dmul_rn(e[m], V);
-                } else {
-                    const PieceF P = spf[pk];
-                    const long long diff = (long long)(w - P.flfix);  // (u - Fl) 2^64, exact
-                    const float dv = fmaf((float)(int)(diff >> 32), 4294967296.f, (float)(unsigned)diff);
-                    const float v = dv * P.invw;
-                    const float H = fmaf(fmaf(fmaf(P.b3, v, P.b2), v, P.b1), v, P.b0);
-                    bad |= !(H > 0.f);
-                    const float V = H * vfac;
-                    float e[3];
-                    for (int m = 0; m < 3; m++) {
-                        const uint64_t A = dnext(r0, r1, r2, r3), B = dnext(r0, r1, r2, r3);
-                        e[m] = gauss32_cospi(A, B);
-                    }
-                    const float l2 = e[0] * e[0] + e[1] * e[1] + e[2] * e[2];
-                    const float sc = l2 > 0.f ? rsqrtf(l2) * V : V;
-                    for (int m = 0; m < 3; m++) d[m] = e[m] * sc;
-                }
+    // one particle: its seven draws, momentum and direction; d = its velocity increment
+    auto one = [&](T *d) {
+        const uint64_t w = dnext(r0, r1, r2, r3);
+        int pk = sbk[w >> (64 - kBucketBits)];
+        while (pk + 1 < tt.n && w > sle[pk + 1]) pk++;
+        if constexpr (sizeof(T) == 8) {
+            // src/random.c:284-286, src/mitos.c:935-965 with the reference's rounding
+            const ThermPiece &P = tt.piece[pk];
+            const double u = __dmul_rn(__ull2double_rn(w), 0x1p-64);
+            const double v = __ddiv_rn(__dsub_rn(u, P.Fl), __dsub_rn(P.Fr, P.Fl));
+            const double H = __dadd_rn(__dadd_rn(__dadd_rn(P.a0, __dmul_rn(P.a1, v)), __dmul_rn(__dmul_rn(P.a2, v), v)),
+                                       __dmul_rn(__dmul_rn(__dmul_rn(P.a3, v), v), v));
+            const double p = __ddiv_rn(H, a_ini);
+            bad |= isnan(p) || p <= 0;
+            const double V = __dmul_rn(__ddiv_rn(p, M_eV), c);
+            double e[3];
+            for (int m = 0; m < 3; m++) {
+                const uint64_t A = dnext(r0, r1, r2, r3), B = dnext(r0, r1, r2, r3);
+                e[m] = gauss64(A, B);
             }
-            for (int m = 0; m < 3; m++) stage[threadIdx.x][3 * j + m] = d[m];
-        }
-        __syncthreads();
-        // add the block's increments: thread t's run starts at particle block_first + t R
-        if (stride == 3) {
-            // packed velocities: thread t's chunk is 24 consecutive floats; 32-bit offsets in the block
-            float *base = vel + 3 * (block_first + k0);
-            for (int idx = threadIdx.x; idx < THERMAL_THREADS * 3 * THERMAL_CHUNK; idx += THERMAL_THREADS) {
-                const int t = idx / (3 * THERMAL_CHUNK), f = idx - t * (3 * THERMAL_CHUNK);
-                const int j = (f * 11) >> 5;  // f / 3 for f < 24
-                if (k0 + j < R && (long)(t * R + k0 + j) < rem) {
-                    float *a = base + (3 * t * R + f);
-                    if constexpr (sizeof(T) == 8) *a = __double2float_rn(__dadd_rn((double)*a, stage[t][f]));
-                    else *a += stage[t][f];
-                }
-            }
+            const double len = hypot(e[0], hypot(e[1], e[2]));
+            if (len > 0)
+                for (int m = 0; m < 3; m++) e[m] = __ddiv_rn(e[m], len);
+            for (int m = 0; m < 3; m++) d[m] = __dmul_rn(e[m], V);
         } else {
+            const PieceF P = spf[pk];
+            const long long diff = (long long)(w - P.flfix);  // (u - Fl) 2^64, exact
+            const float dv = fmaf((float)(int)(diff >> 32), 4294967296.f, (float)(unsigned)diff);
+            const float v = dv * P.invw;
+            const float H = fmaf(fmaf(fmaf(P.b3, v, P.b2), v, P.b1), v, P.b0);
+            bad |= !(H > 0.f);
+            const float V = H * vfac;
+            float e[3];
+            for (int m = 0; m < 3; m++) {
+                const uint64_t A = dnext(r0, r1, r2, r3), B = dnext(r0, r1, r2, r3);
+                e[m] = gauss32_cospi(A, B);
+            }
+            const float l2 = e[0] * e[0] + e[1] * e[1] + e[2] * e[2];
+            const float sc = l2 > 0.f ? rsqrtf(l2) * V : V;
+            for (int m = 0; m < 3; m++) d[m] = e[m] * sc;
+        }
+    };
+    // v + d in the reference's arithmetic: float + double rounded once (FP64), float (FP32)
+    auto addv = [](float v, T d) -> float {
+        if constexpr (sizeof(T) == 8) return __double2float_rn(__dadd_rn((double)v, d));
+        else return v + d;
+    };
+    if constexpr (PACKED) {
+        for (int k0 = 0; k0 < R; k0 += 4) {
+            const long p0 = first + k0;
+            if (p0 >= n) break;
+            const int cnt = n - p0 < 4 ? (int)(n - p0) : 4;
+            float *q = vel + 3 * p0;
+            float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = q0, q2 = q0;
+            if (cnt == 4) {
+                q0 = reinterpret_cast<const float4 *>(q)[0];
+                q1 = reinterpret_cast<const float4 *>(q)[1];
+                q2 = reinterpret_cast<const float4 *>(q)[2];
+            }
+            T d[12];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                if (j < cnt) one(d + 3 * j);
+                else d[3 * j] = d[3 * j + 1] = d[3 * j + 2] = 0;
+            }
+            if (cnt == 4) {
+                q0 = make_float4(addv(q0.x, d[0]), addv(q0.y, d[1]), addv(q0.z, d[2]), addv(q0.w, d[3]));
+                q1 = make_float4(addv(q1.x, d[4]), addv(q1.y, d[5]), addv(q1.z, d[6]), addv(q1.w, d[7]));
+                q2 = make_float4(addv(q2.x, d[8]), addv(q2.y, d[9]), addv(q2.z, d[10]), addv(q2.w, d[11]));
+                reinterpret_cast<float4 *>(q)[0] = q0;
+                reinterpret_cast<float4 *>(q)[1] = q1;
+                reinterpret_cast<float4 *>(q)[2] = q2;
+            } else {
+#pragma unroll
+                for (int i = 0; i < 12; i++)
+                    if (i < 3 * cnt) q[i] = addv(q[i], d[i]);
+            }
+        }
+    } else {
+        __shared__ T stage[THERMAL_THREADS][3 * THERMAL_CHUNK + 1];
+        for (int k0 = 0; k0 < R; k0 += THERMAL_CHUNK) {
+            // the velocities this chunk adds to, on their way to L2 while the chunk computes
+            if (first + k0 < n) {
+                const long last = min(first + k0 + THERMAL_CHUNK, min(first + R, n)) - 1;
+                prefetch_l2(vel + (first + k0) * stride);
+                prefetch_l2(vel + last * stride + 2);
+            }
+            for (int j = 0; j < THERMAL_CHUNK; j++) {
+                T d[3] = {0, 0, 0};
+                if (k0 + j < R && first + k0 + j < n) one(d);
+                for (int m = 0; m < 3; m++) stage[threadIdx.x][3 * j + m] = d[m];
+            }
+            __syncthreads();
+            // add the block's increments: thread t's run starts at particle block_first + t R
             for (int idx = threadIdx.x; idx < THERMAL_THREADS * 3 * THERMAL_CHUNK; idx += THERMAL_THREADS) {
                 const int t = idx / (3 * THERMAL_CHUNK), f = idx - t * (3 * THERMAL_CHUNK);
                 const int j = f / 3, m = f - 3 * j;
                 const long p = block_first + (long)t * R + k0 + j;
                 if (k0 + j < R && p < n) {
                     float *a = vel + p * stride + m;
-                    if constexpr (sizeof(T) == 8) *a = __double2float_rn(__dadd_rn((double)*a, stage[t][f]));
-                    else *a += stage[t][f];
+                    *a = addv(*a, stage[t][f]);
                 }
             }
+            __syncthreads();
         }
-        __syncthreads();
     }
     if (bad) atomicOr(err, 1);
 }
@@ -352,22 +379,25 @@ static int thermal_launch(int prec, long n, const uint64_t s0[4], unsigned long 
                           double a_ini, double M_eV, double c, float *vel, long stride, int *err) {
     if (n <= 0) return 0;
     const size_t smem = thermal_smem(tt.n);
+    const bool packed = stride == 3 && ((uintptr_t)vel & 15) == 0;
     int dev = 0, sms = 0, per_sm = 0;
     MITOS_CUDA(cudaGetDevice(&dev));
     MITOS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    if (prec == MITOS_FP32) {
-        if (smem > 48 * 1024) MITOS_CUDA(cudaFuncSetAttribute(k_thermal<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        MITOS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_thermal<float>, THERMAL_THREADS, smem));
-    } else {
-        if (smem > 48 * 1024) MITOS_CUDA(cudaFuncSetAttribute(k_thermal<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        MITOS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_thermal<double>, THERMAL_THREADS, smem));
-    }
+    auto occupancy = [&](auto kern) -> int {
+        if (smem > 48 * 1024) MITOS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        MITOS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, THERMAL_THREADS, smem));
+        return 0;
+    };
+    int e = prec == MITOS_FP32 ? (packed ? occupancy(k_thermal<float, true>) : occupancy(k_thermal<float, false>))
+                               : (packed ? occupancy(k_thermal<double, true>) : occupancy(k_thermal<double, false>));
+    if (e) return e;
     if (per_sm < 1) {
         set_error(3, "thermal sampler of %d pieces does not fit the kernel's shared memory", tt.n);
         return 3;
     }
     const long wave = (long)sms * per_sm * THERMAL_THREADS;
-    const int R = (int)((n + wave - 1) / wave);
+    int R = (int)((n + wave - 1) / wave);
+    if (packed) R = (R + 3) & ~3;  // runs of whole float4 groups: 16-byte aligned starts
     const long G = (n + R - 1) / R;
     const uint64_t *polys = affine_jump_polys(skip, 7ULL * (unsigned long long)R, G);
     if (!polys) return 5;
@@ -376,12 +406,21 @@ static int thermal_launch(int prec, long n, const uint64_t s0[4], unsigned long 
     const unsigned blocks = (unsigned)((G + THERMAL_THREADS - 1) / THERMAL_THREADS);
     const float vfac = (float)(c / (a_ini * M_eV));
     launch_begin("thermal");
-    if (prec == MITOS_FP32)
-        k_thermal<float><<<blocks, THERMAL_THREADS, smem, stream()>>>(n, R, st, polys, tt, a_ini, M_eV, c, vfac, vel,
-                                                                       stride, err);
-    else
-        k_thermal<double><<<blocks, THERMAL_THREADS, smem, stream()>>>(n, R, st, polys, tt, a_ini, M_eV, c, vfac, vel,
-                                                                        stride, err);
+    if (prec == MITOS_FP32) {
+        if (packed)
+            k_thermal<float, true><<<blocks, THERMAL_THREADS, smem, stream()>>>(n, R, st, polys, tt, a_ini, M_eV, c,
+                                                                               vfac, vel, stride, err);
+        else
+            k_thermal<float, false><<<blocks, THERMAL_THREADS, smem, stream()>>>(n, R, st, polys, tt, a_ini, M_eV, c,
+                                                                                vfac, vel, stride, err);
+    } else {
+        if (packed)
+            k_thermal<double, true><<<blocks, THERMAL_THREADS, smem, stream()>>>(n, R, st, polys, tt, a_ini, M_eV, c,
+                                                                                vfac, vel, stride, err);
+        else
+            k_thermal<double, false><<<blocks, THERMAL_THREADS, smem, stream()>>>(n, R, st, polys, tt, a_ini, M_eV, c,
+                                                                                 vfac, vel, stride, err);
+    }
     count_launch();
     MITOS_LAUNCH_CHECK("thermal velocities");
     return 0;
