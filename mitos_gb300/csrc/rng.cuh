@@ -47,7 +47,9 @@ __device__ __forceinline__ double gauss64(uint64_t A, uint64_t B) {
 // rate on this part): the uniform is hi 2^32 + lo from the two 32-bit halves (one FMA: within an
 // ulp of the rounded 64-bit value, 2^-24 relative at every magnitude), the cosine argument the
 // top 32 bits (absolute error below 2^-32).
-__device__ __forceinline__ float gauss32(uint64_t A, uint64_t B) {
+//
+// -2 ln u of the uniform of draw A
+__device__ __forceinline__ float gauss32_r2(uint64_t A) {
     const float inv64 = 5.42101086242752217e-20f;  // 2^-64
     const bool hi = (A >> 63) != 0;
     const uint64_t a = hi ? ~A : A;
@@ -63,7 +65,10 @@ __device__ __forceinline__ float gauss32(uint64_t A, uint64_t B) {
     p = fmaf(p, s2, 1.f / 3.f);
     p = fmaf(p, s2, 1.f);
     const float lnu = hi ? -2.f * s * p : __logf(t);
-    const float x = -2.f * lnu;  // > 0
+    return -2.f * lnu;  // > 0
+}
+__device__ __forceinline__ float gauss32(uint64_t A, uint64_t B) {
+    const float x = gauss32_r2(A);
     // cos(2 pi v) = -cos(2 pi (v - 1/2)), argument in (-pi, pi) for the hardware cosine
     const float w = ((float)(int)((unsigned)(B >> 32) ^ 0x80000000u) + 0.5f) * 2.3283064365386963e-10f;  // 2^-32
     return -(x * rsqrtf(x)) * __cosf(6.28318530717958647692f * w);
@@ -73,22 +78,7 @@ __device__ __forceinline__ float gauss32(uint64_t A, uint64_t B) {
 // is near zero (__cosf's error is absolute, 2^-21.4), for uses that normalise a triple of normals,
 // where a small length would magnify that absolute error
 __device__ __forceinline__ float gauss32_cospi(uint64_t A, uint64_t B) {
-    const float inv64 = 5.42101086242752217e-20f;  // 2^-64
-    const bool hi = (A >> 63) != 0;
-    const uint64_t a = hi ? ~A : A;
-    const float af = fmaf((float)(unsigned)(a >> 32), 4294967296.f, (float)(unsigned)a);
-    const float t = (af + 0.5f) * inv64;
-    const float s = __fdividef(t, 2.f - t), s2 = s * s;
-    float p = 1.f / 15.f;
-    p = fmaf(p, s2, 1.f / 13.f);
-    p = fmaf(p, s2, 1.f / 11.f);
-    p = fmaf(p, s2, 1.f / 9.f);
-    p = fmaf(p, s2, 1.f / 7.f);
-    p = fmaf(p, s2, 1.f / 5.f);
-    p = fmaf(p, s2, 1.f / 3.f);
-    p = fmaf(p, s2, 1.f);
-    const float lnu = hi ? -2.f * s * p : __logf(t);
-    const float x = -2.f * lnu;
+    const float x = gauss32_r2(A);
     // cos(2 pi v) = -cos(pi (2 v - 1)), 2 v - 1 in (-1, 1) from the top 32 bits of B
     const float w2 = ((float)(int)((unsigned)(B >> 32) ^ 0x80000000u) + 0.5f) * 4.6566128730773926e-10f;  // 2^-31
     return -(x * rsqrtf(x)) * cospif(w2);
