@@ -401,9 +401,10 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     if (e) return e;
     tim.mark();
 
-    // S5: particles + CIC.  The positions are staged in a device buffer of the run's slot and copied
-    // to the caller on the copy stream as soon as the deposit ends, under the P(k) passes (and, for
-    // ic_pipeline_submit, under the next IC); the buffer is reused once its last copy is done.
+    // S5: particles + CIC.  The positions are staged in a device buffer of the run's slot (for the
+    // caller's res->pos and for the snapshot datasets) and copied to the caller on the copy stream as
+    // soon as the deposit ends, under the P(k) passes (and, for ic_pipeline_submit, under the next
+    // IC); the buffer is reused once its last copy is done.
     float *dpos = nullptr, *dposraw = nullptr;
     const int pslot = (opt && opt->async_slot >= 0) ? opt->async_slot : 0;
     const size_t pos_bytes = sizeof(float) * 3 * (size_t)M * M * M;
@@ -662,7 +663,7 @@ int mitos::pipeline_table(const struct ic_config *cfg, int k_size, int tau_size,
     find_tau_h(&pd, lt, &tau_index, &u_tau);
     const double *arr = delta + (long)cfg->index_src * k_size * tau_size;
     const double *tlo = arr + (long)k_size * tau_index, *thi = arr + (long)k_size * (tau_index + 1);
-    // the velocity transfer function's rows at the same time (used when res->vel is set)
+    // the velocity transfer function's rows at the same time (used when res->vel or res->vels is set)
     const double *tvlo = nullptr, *tvhi = nullptr;
     if (cfg->index_vel >= 0 && cfg->index_vel < n_functions) {
         const double *va = delta + (long)cfg->index_vel * k_size * tau_size;
