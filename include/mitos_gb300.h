@@ -201,6 +201,9 @@ void calc_cross_powerspec(int N, double boxlen, const mitos_c128 *box1, const mi
 void calc_cross_powerspec_float(int N, double boxlen, const mitos_c64 *box1,
                                 const mitos_c64 *box2, int bins, double *k_in_bins,
                                 double *power_in_bins, int *obs_in_bins);
+/* box1/box2 hold the x-slab X0 .. X0+NX-1 of the grid (NX*N*(N/2+1) elements, as each rank of the
+ * reference holds); the bins average that slab's modes (the reference's MPI_Allreduce over ranks,
+ * src/calc_powerspec.c:203-205, is the identity on one rank) */
 void calc_cross_powerspec_float_mpi(long int N, long int X0, long int NX, double boxlen,
                                     const mitos_c64 *box1, const mitos_c64 *box2, int bins,
                                     double *k_in_bins, double *power_in_bins,
@@ -386,12 +389,17 @@ int mitos_thermal_pieces(const struct sampler *s, const uint64_t *w, long n, int
 /* P(k) binning that allocates no device memory.  No counterpart in the reference: for callers
  * that must not allocate device memory in their loop, because another allocator already holds
  * the device's memory or because cudaMalloc / cudaFree would synchronise a streaming pipeline.
- * dev_box1 / dev_box2 are device complex grids (N*N*(N/2+1), FP64 or FP32 per `precision`);
- * linear = 0 gives the reference log bins of calc_cross_powerspec, 1 linear shells to k_Nyquist.
- * Scratch: a fixed device array for at most 4096 bins (96 KB, held by every GPU that loads the
- * library until exit); more bins return status 3.  The array is shared by all calls and cleared
- * by each: calls whose GPU work overlaps race.  The first call on a device looks up the array's
- * address (cudaGetSymbolAddress); make it before any stream capture.  Outputs are host arrays. */
+ * dev_box1 / dev_box2 are device complex grids (N*N*(N/2+1), FP64 or FP32 per `precision`, on the
+ * library's device: the device current at the library's first call; another device gives status
+ * 3); linear = 0 gives the reference log bins of calc_cross_powerspec, 1 linear shells to
+ * k_Nyquist, each mode in the bin the regular entry points give it.  Outputs are host arrays.
+ * Scratch: a fixed device array for at most 4096 bins (128 KB) that the GPU holds until the
+ * process exits; more bins return status 3.  The array is shared by all calls and keeps the last
+ * call's contents; every call clears what it sums into, so calls whose GPU work overlaps race.
+ * Set-up: the first call looks up the array's device address (cudaGetSymbolAddress).  Under
+ * CUDA's lazy module loading (the default) the array is also reserved on the device then, so make
+ * the first call -- N = 0 with both grids NULL does the set-up alone and returns 0 -- before
+ * another allocator reserves the device's memory, and before any stream capture. */
 int calc_cross_powerspec_noalloc(int N, double boxlen, const void *dev_box1, const void *dev_box2,
                                  int precision, int bins, int linear, double *k_in_bins,
                                  double *power_in_bins, long *obs_in_bins);

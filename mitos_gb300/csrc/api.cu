@@ -145,19 +145,19 @@ int axpby(int prec, long n, double a, const void *x, double b, const void *y, vo
 
 // cross power of two complex grids into log or linear bins (device accumulators)
 template <typename T>
-__global__ void k_bin_cross(int N, double dk, const cplx<T> *f1, const cplx<T> *f2, const int *bin_of_n2,
-                            int nbins, double *bk, double *bp, unsigned long long *bn) {
+__global__ void k_bin_cross(int N, int x0, int nx, double dk, const cplx<T> *f1, const cplx<T> *f2,
+                            const int *bin_of_n2, int nbins, double *bk, double *bp, unsigned long long *bn) {
     extern __shared__ double shb[];
     double *sk = shb, *sp = shb + nbins;
     unsigned long long *sn = (unsigned long long *)(shb + 2 * nbins);
     for (int i = threadIdx.x; i < nbins; i += blockDim.x) { sk[i] = 0; sp[i] = 0; sn[i] = 0; }
     __syncthreads();
     const int H = N / 2 + 1;
-    const long total = (long)N * N * H;
+    const long total = (long)nx * N * H;  // the rows x0 .. x0 + nx - 1 (a slab, or the whole grid)
     for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < total; id += (long)gridDim.x * blockDim.x) {
         const int z = (int)(id % H);
         const long xy = id / H;
-        const int y = (int)(xy % N), x = (int)(xy / N);
+        const int y = (int)(xy % N), x = x0 + (int)(xy / N);
         const int jx = kint(x, N), jy = kint(y, N);
         const long n2 = (long)jx * jx + (long)jy * jy + (long)z * z;
         const int b = bin_of_n2[n2];
@@ -181,7 +181,7 @@ __global__ void k_bin_cross(int N, double dk, const cplx<T> *f1, const cplx<T> *
     }
 }
 
-int bin_cross(int N, double boxlen, int prec, const void *f1, const void *f2, int bins, int linear,
+int bin_cross(int N, int x0, int nx, double boxlen, int prec, const void *f1, const void *f2, int bins, int linear,
               double *k_out, double *p_out, long long *n_out) {
     const int *tab = bin_table(N, bins, linear, boxlen);
     if (!tab) return 5;
@@ -189,16 +189,16 @@ int bin_cross(int N, double boxlen, int prec, const void *f1, const void *f2, in
     if (!acc) return 5;
     MITOS_CUDA(cudaMemsetAsync(acc, 0, sizeof(double) * 3 * bins, stream()));
     const size_t smem = sizeof(double) * 3 * bins;
-    const long total = (long)N * N * (N / 2 + 1);
+    const long total = (long)nx * N * (N / 2 + 1);
     int blocks = (int)((total + 255) / 256);
     if (blocks > 152 * 8) blocks = 152 * 8;
     const double dk = 2 * M_PI / boxlen;
     launch_begin("bin_cross");
     if (prec == MITOS_FP32)
-        k_bin_cross<float><<<blocks, 256, smem, stream()>>>(N, dk, (const float2 *)f1, (const float2 *)f2, tab, bins,
-                                                            acc, acc + bins, (unsigned long long *)(acc + 2 * bins));
+        k_bin_cross<float><<<blocks, 256, smem, stream()>>>(N, x0, nx, dk, (const float2 *)f1, (const float2 *)f2, tab,
+                                                            bins, acc, acc + bins, (unsigned long long *)(acc + 2 * bins));
     else
-        k_bin_cross<double><<<blocks, 256, smem, stream()>>>(N, dk, (const double2 *)f1, (const double2 *)f2, tab,
+        k_bin_cross<double><<<blocks, 256, smem, stream()>>>(N, x0, nx, dk, (const double2 *)f1, (const double2 *)f2, tab,
                                                              bins, acc, acc + bins, (unsigned long long *)(acc + 2 * bins));
     count_launch();
     MITOS_LAUNCH_CHECK("power spectrum binning");
@@ -570,9 +570,16 @@ static void finish_bins(int bins, double boxlen, double *k, double *p, const lon
     }
 }
 
-static int cross_common(int N, double boxlen, int prec, const void *b1, const void *b2, int bins,
+// the reference's three cross spectra: box1 / box2 hold the rows x0 .. x0 + nx - 1 of the
+// half-complex grid (host or device); bins over those rows' modes (on one rank the reduction of
+// calc_cross_powerspec_float_mpi, src/calc_powerspec.c:203-205, is the identity)
+static int cross_common(int N, int x0, int nx, double boxlen, int prec, const void *b1, const void *b2, int bins,
                         double *k, double *p, long long *n) {
-    const size_t bytes = (size_t)N * N * (N / 2 + 1) * csize(prec);
+    if (N < 2 || (N & 1) || bins < 1 || x0 < 0 || nx < 1 || x0 + nx > N || !b1 || !b2 || !(boxlen > 0)) {
+        set_error(1, "power spectrum: invalid grid, slab or bins");
+        return 1;
+    }
+    const size_t bytes = (size_t)nx * N * (N / 2 + 1) * csize(prec);
     const void *d1 = b1, *d2 = b2;
     if (!is_device_ptr(b1)) {
         void *t = workspace(bytes, 20);
@@ -588,7 +595,7 @@ static int cross_common(int N, double boxlen, int prec, const void *b1, const vo
         MITOS_CUDA(cudaMemcpyAsync(t, b2, bytes, cudaMemcpyHostToDevice, stream()));
         d2 = t;
     }
-    int e = bin_cross(N, boxlen, prec, d1, d2, bins, 0, k, p, n);
+    int e = bin_cross(N, x0, nx, boxlen, prec, d1, d2, bins, 0, k, p, n);
     if (e) return e;
     finish_bins(bins, boxlen, k, p, n);
     return 0;
@@ -597,24 +604,24 @@ static int cross_common(int N, double boxlen, int prec, const void *b1, const vo
 extern "C" void calc_cross_powerspec(int N, double boxlen, const mitos_c128 *box1, const mitos_c128 *box2,
                                      int bins, double *k_in_bins, double *power_in_bins, int *obs_in_bins) {
     std::vector<long long> n(bins);
-    if (cross_common(N, boxlen, MITOS_FP64, box1, box2, bins, k_in_bins, power_in_bins, n.data())) return;
+    if (cross_common(N, 0, N, boxlen, MITOS_FP64, box1, box2, bins, k_in_bins, power_in_bins, n.data())) return;
     for (int i = 0; i < bins; i++) obs_in_bins[i] = (int)n[i];
 }
 
 extern "C" void calc_cross_powerspec_float(int N, double boxlen, const mitos_c64 *box1, const mitos_c64 *box2,
                                            int bins, double *k_in_bins, double *power_in_bins, int *obs_in_bins) {
     std::vector<long long> n(bins);
-    if (cross_common(N, boxlen, MITOS_FP32, box1, box2, bins, k_in_bins, power_in_bins, n.data())) return;
+    if (cross_common(N, 0, N, boxlen, MITOS_FP32, box1, box2, bins, k_in_bins, power_in_bins, n.data())) return;
     for (int i = 0; i < bins; i++) obs_in_bins[i] = (int)n[i];
 }
 
 extern "C" void calc_cross_powerspec_float_mpi(long int N, long int X0, long int NX, double boxlen,
                                                const mitos_c64 *box1, const mitos_c64 *box2, int bins,
                                                double *k_in_bins, double *power_in_bins, long int *obs_in_bins) {
-    (void)X0;
-    (void)NX;
     std::vector<long long> n(bins);
-    if (cross_common((int)N, boxlen, MITOS_FP32, box1, box2, bins, k_in_bins, power_in_bins, n.data())) return;
+    if (cross_common((int)N, (int)X0, (int)NX, boxlen, MITOS_FP32, box1, box2, bins, k_in_bins, power_in_bins,
+                     n.data()))
+        return;
     for (int i = 0; i < bins; i++) obs_in_bins[i] = (long)n[i];
 }
 

@@ -62,6 +62,7 @@ __device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefe
 
 // the library's stream (created on first use) and kernel-launch counter
 cudaStream_t stream();
+int library_device();                 // the device the library stream was created on
 void set_stream(cudaStream_t s);      // this thread's launches go to s (nullptr: the library stream)
 void set_workspace_set(int s);        // this thread's workspace() buffers come from set s
 void count_launch(int n = 1);

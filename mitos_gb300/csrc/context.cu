@@ -41,10 +41,18 @@ int check_cuda(cudaError_t e, const char *what) {
 static thread_local cudaStream_t t_stream = nullptr;
 static thread_local int t_ws_set = 0;
 
+static int g_stream_dev = -1;
 cudaStream_t stream() {
     if (t_stream) return t_stream;
-    if (!g_stream) cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking);
+    if (!g_stream) {
+        cudaGetDevice(&g_stream_dev);
+        cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking);
+    }
     return g_stream;
+}
+int library_device() {
+    stream();
+    return g_stream_dev;
 }
 void set_stream(cudaStream_t s) { t_stream = s; }
 void set_workspace_set(int s) { t_ws_set = s; }
@@ -253,6 +261,20 @@ static long isqrt_l(long a) {
     while ((r + 1) * (r + 1) <= a) r++;
     return r;
 }
+int pk_bin_of_n2(long n2, int N, int bins, int linear, double dk, double lmin, double lmax) {
+    int b;
+    if (linear) {
+        // linear shells of width k_Nyquist / bins: b = isqrt(n2 bins^2) / (N/2)
+        b = (int)(isqrt_l(n2 * (long)bins * bins) / (N / 2));
+    } else {
+        // src/calc_powerspec.c:61-63 with k = dk sqrt(n2)
+        const double k = sqrt((double)n2) * dk;
+        const float u = (log(k) - lmin) / (lmax - lmin);
+        b = (int)floor((bins - 1) * u);
+    }
+    return (b >= 0 && b < bins) ? b : -1;
+}
+
 struct BinEntry {
     int *dev = nullptr;
     std::vector<int> host;
@@ -275,19 +297,7 @@ static BinEntry *bin_entry(int N, int bins, int linear, double boxlen) {
     const double dk = 2 * M_PI / boxlen;
     const double max_k = sqrt(3) * dk * N / 2, min_k = dk;
     const double lmax = log(max_k), lmin = log(min_k);
-    for (long n2 = 1; n2 <= n2max; n2++) {
-        int b;
-        if (linear) {
-            // linear shells of width k_Nyquist / bins: b = isqrt(n2 bins^2) / (N/2)
-            b = (int)(isqrt_l(n2 * (long)bins * bins) / (N / 2));
-        } else {
-            // src/calc_powerspec.c:61-63 with k = dk sqrt(n2)
-            const double k = sqrt((double)n2) * dk;
-            const float u = (log(k) - lmin) / (lmax - lmin);
-            b = (int)floor((bins - 1) * u);
-        }
-        tab[n2] = (b >= 0 && b < bins) ? b : -1;
-    }
+    for (long n2 = 1; n2 <= n2max; n2++) tab[n2] = pk_bin_of_n2(n2, N, bins, linear, dk, lmin, lmax);
     if (cudaMalloc(&be->dev, sizeof(int) * (n2max + 1)) != cudaSuccess) {
         cudaGetLastError();
         delete be;

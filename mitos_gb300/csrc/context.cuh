@@ -8,6 +8,10 @@ namespace mitos {
 const void *window_table(int N, int order, int precision);
 const void *stencil_table(int N, int precision);
 const int *bin_table(int N, int bins, int linear, double boxlen);
+// the bin of a mode of squared integer wavevector norm n2 (-1: outside the bins): linear shells of
+// width k_Nyquist / bins, or the reference's log bins (src/calc_powerspec.c:61-63) with
+// k = dk sqrt(n2), lmin = log(dk), lmax = log(sqrt(3) dk N / 2); non-decreasing in n2 where >= 0
+int pk_bin_of_n2(long n2, int N, int bins, int linear, double dk, double lmin, double lmax);
 // the |n|^2 range [lo, hi] of bin b (bins are monotone in |n|^2, so one range; lo > hi when empty);
 // status 3 if the bin's |n|^2 values are not contiguous
 int bin_n2_range(int N, int bins, int linear, double boxlen, int b, long *lo, long *hi);

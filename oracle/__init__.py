@@ -14,7 +14,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liborc.so")
 REF_PATH = os.path.join(HERE, "_ref", "libmitos_ref.so")
-REF_DIR = os.environ.get("MITOS_REF_DIR", "/root/reference")
+# the reference checkout beside this repository, unless MITOS_REF_DIR names another
+REF_DIR = os.environ.get("MITOS_REF_DIR") or os.path.normpath(os.path.join(HERE, "..", "..", "reference"))
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _fp = ctypes.POINTER(ctypes.c_float)
@@ -198,6 +199,35 @@ def powerspec(N: int, boxlen: float, f1: np.ndarray, f2: np.ndarray, bins: int, 
     fn = lib().orc_powerspec_lin if linear else lib().orc_powerspec_log
     with np.errstate(all="ignore"):
         fn(N, ctypes.c_double(boxlen), P(a), P(b), bins, P(k), P(p), P(o, _lp))
+    return k, p, o
+
+
+def _float_slab_args(box1, box2):
+    a = np.ascontiguousarray(np.stack([box1.real, box1.imag], -1).astype(np.float32))
+    b = np.ascontiguousarray(np.stack([box2.real, box2.imag], -1).astype(np.float32))
+    return a, b
+
+
+def powerspec_float_slab(N: int, X0: int, NX: int, boxlen: float, box1: np.ndarray, box2: np.ndarray, bins: int):
+    """calc_cross_powerspec_float_mpi on one rank; box1/box2: complex64 slabs (NX, N, N/2+1)"""
+    a, b = _float_slab_args(box1, box2)
+    k, p, o = np.zeros(bins), np.zeros(bins), np.zeros(bins, np.int64)
+    with np.errstate(all="ignore"):
+        lib().orc_powerspec_float_slab(ctypes.c_long(N), ctypes.c_long(X0), ctypes.c_long(NX), ctypes.c_double(boxlen),
+                                       P(a, _fp), P(b, _fp), bins, P(k), P(p), P(o, _lp))
+    return k, p, o
+
+
+def ref_powerspec_float_slab(N: int, X0: int, NX: int, boxlen: float, box1: np.ndarray, box2: np.ndarray, bins: int):
+    """the reference build's calc_cross_powerspec_float_mpi (one rank), or None without it"""
+    r = ref_lib()
+    if r is None:
+        return None
+    a, b = _float_slab_args(box1, box2)
+    k, p, o = np.zeros(bins), np.zeros(bins), np.zeros(bins, np.int64)
+    with np.errstate(all="ignore"):
+        r.calc_cross_powerspec_float_mpi(ctypes.c_long(N), ctypes.c_long(X0), ctypes.c_long(NX), ctypes.c_double(boxlen),
+                                         P(a, _fp), P(b, _fp), bins, P(k), P(p), P(o, _lp))
     return k, p, o
 
 

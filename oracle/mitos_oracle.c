@@ -1188,6 +1188,45 @@ void orc_powerspec_lin(int N, double boxlen, const double *f1, const double *f2,
     }
 }
 
+/* calc_cross_powerspec_float_mpi: src/calc_powerspec.c:152-217 on one rank (its three
+ * MPI_Allreduce calls, :203-205, leave the slab's sums unchanged).  The slab's row x - X0 holds
+ * the modes of x (row_major_half_mpi); the float components are widened to double before the
+ * products. */
+void orc_powerspec_float_slab(long N, long X0, long NX, double boxlen, const float *box1, const float *box2,
+                              int bins, double *k_in_bins, double *power_in_bins, long *obs_in_bins) {
+    const double boxvol = boxlen * boxlen * boxlen;
+    const double dk = 2 * M_PI / boxlen;
+    const double max_k = sqrt(3) * dk * N / 2;
+    const double min_k = dk;
+    const double log_max_k = log(max_k);
+    const double log_min_k = log(min_k);
+    for (int i = 0; i < bins; i++) { k_in_bins[i] = 0; power_in_bins[i] = 0; obs_in_bins[i] = 0; }
+    double kx, ky, kz, k;
+    for (long x = X0; x < X0 + NX; x++) {
+        for (long y = 0; y < N; y++) {
+            for (long z = 0; z <= N / 2; z++) {
+                orc_wavevector((int)x, (int)y, (int)z, (int)N, dk, &kx, &ky, &kz, &k);
+                if (k == 0) continue;
+                const int bin = log_bin_k(k, bins, log_min_k, log_max_k);
+                if (bin < 0 || bin >= bins) continue;
+                const long id = ((x - X0) * N + y) * (N / 2 + 1) + z;
+                double a1 = box1[2 * id], a2 = box2[2 * id];
+                double b1 = box1[2 * id + 1], b2 = box2[2 * id + 1];
+                double Power = a1 * a2 + b1 * b2;
+                int multiplicity = (z == 0 || z == N / 2) ? 1 : 2;
+                k_in_bins[bin] += multiplicity * k;
+                power_in_bins[bin] += multiplicity * Power;
+                obs_in_bins[bin] += multiplicity;
+            }
+        }
+    }
+    for (int i = 0; i < bins; i++) {
+        k_in_bins[i] /= obs_in_bins[i];
+        power_in_bins[i] /= obs_in_bins[i];
+        power_in_bins[i] /= boxvol;
+    }
+}
+
 /* ===================================================================================== */
 /* The initial-condition pipeline                                                         */
 /* ===================================================================================== */

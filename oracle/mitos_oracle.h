@@ -104,6 +104,10 @@ void orc_powerspec_log(int N, double boxlen, const double *f1, const double *f2,
 void orc_powerspec_lin(int N, double boxlen, const double *f1, const double *f2, int bins,
                        double *k_in_bins, double *power_in_bins, long *obs_in_bins);
 int  orc_lin_bin(int N, int bins, long n2);
+/* calc_cross_powerspec_float_mpi (src/calc_powerspec.c:152-217) on one rank: float boxes holding
+ * the x-slab X0 .. X0+NX-1, log bins over that slab's modes */
+void orc_powerspec_float_slab(long N, long X0, long NX, double boxlen, const float *box1, const float *box2,
+                              int bins, double *k_in_bins, double *power_in_bins, long *obs_in_bins);
 void orc_bispectrum(int N, double boxlen, const double *fbox, int bins, int bins3, double *k1_in_bins,
                     double *k2_in_bins, double *k3_in_bins, double *bispectrum, int volume_mode, int type,
                     double theta, double k3);

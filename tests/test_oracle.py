@@ -203,3 +203,20 @@ def test_pin_bispectrum_against_reference_build(btype, vol):
     assert np.any(a["B"] != 0)
     for key in ("k1", "k2", "k3", "B"):
         assert np.array_equal(a[key], b[key]), key
+
+
+@pytest.mark.skipif(oracle.ref_lib() is None, reason="reference build not present here")
+@pytest.mark.parametrize("X0,NX", [(0, 32), (0, 8), (5, 11), (24, 8)])
+def test_pin_float_slab_spectrum_against_reference_build(X0, NX):
+    """orc_powerspec_float_slab equals the reference's calc_cross_powerspec_float_mpi
+    (src/calc_powerspec.c:152-217, one rank) bit for bit on x-slabs of a 32^3 grid"""
+    N, L, bins = 32, 100.0, 12
+    r = np.random.default_rng(X0 + 100 * NX)
+    sh = (N, N, N // 2 + 1)
+    a = (r.standard_normal(sh) + 1j * r.standard_normal(sh)).astype(np.complex64)[X0:X0 + NX]
+    b = (r.standard_normal(sh) + 1j * r.standard_normal(sh)).astype(np.complex64)[X0:X0 + NX]
+    got = oracle.powerspec_float_slab(N, X0, NX, L, a, b, bins)
+    ref = oracle.ref_powerspec_float_slab(N, X0, NX, L, a, b, bins)
+    assert got[2].sum() > 0
+    for x, y in zip(got, ref):
+        assert np.array_equal(x, y, equal_nan=True)
