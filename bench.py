@@ -11,7 +11,9 @@ gather) + wrap -> CIC -> overdensity r2c -> CIC window undo -> P(k) in 128 linea
   e2e    the same call with the particle positions (512^3 x 3 floats) copied to pinned host
          memory every step, plus the table upload and the P(k) read.
   --impl reference   the reference algorithm restated in C (oracle/, OpenMP, FP64) on the
-         host cores: one 256^3 IC per step, scaled by the cell count (x8) to 512^3 ICs.
+         host cores: one full 512^3 IC per step.
+  noise_exact   (CPU leg) the GPU's white noise of the 64^3 and 256^3 precision configurations
+         against the reference's, value by value.
 
 N > 1 GPUs run independent replicas (different seeds): the IC does not shard.
 """
@@ -164,22 +166,23 @@ def ncu_traffic(kernel: str, N: int):
 
 
 def cpu_baseline(args, table, steps=1):
-    """the oracle (reference algorithm in C, FP64, all host threads) on one 256^3 IC per step"""
+    """the oracle (the reference's algorithm restated in C, FP64, all host threads) on one full IC of
+    the benchmark configuration per step"""
     import oracle
-    Ns = 256
-    Ls = args.boxlen * Ns / args.N
-    prm = oracle.ic_params(Ns, Ns, Ls, args.seed, table, pk_bins=args.bins // 2, pk_linear=True)
     times = []
-    for _ in range(steps):
+    for i in range(steps):
+        prm = oracle.ic_params(args.N, args.N, args.boxlen, args.seed + i, table, pk_bins=args.bins, pk_linear=True)
         t0 = time.perf_counter()
         oracle.ic_pipeline(prm)
         times.append(time.perf_counter() - t0)
-    scale = (args.N / Ns) ** 3
-    sec_per_ic = statistics.median(times) * scale
+    sec_per_ic = sum(times) / len(times)
     return {"value": 1.0 / sec_per_ic, "unit": UNIT, "cores": oracle.lib().orc_num_threads(),
             "kind": "port",
-            "sample": f"one {Ns}^3 IC (L = {Ls:g}) per step, {statistics.median(times):.2f} s, "
-                      f"scaled x{scale:g} by cell count to a {args.N}^3 IC"}, times
+            "sample": f"{steps} full {args.N}^3 IC(s) (L = {args.boxlen:g}, {args.bins} linear shells), "
+                      f"{sec_per_ic:.1f} s each: the reference's algorithm (src/mitos.c:205-422,794-863, "
+                      "analyse/src/mitos_read.c:278-419) restated in C, FP64, OpenMP over the host cores "
+                      "where the reference loops are parallel, its CIC serial as in mitos_read; the FFTs are "
+                      "the project's CPU FFT with FFTW's conventions, not FFTW (absent on this host)"}, times
 
 
 def run_reference(args):
@@ -188,18 +191,65 @@ def run_reference(args):
         return 0
     from mitos_gb300.perturb import load_table
     table = load_table()
-    for _ in range(args.warmup):
-        pass  # the CPU port has no warm-up state; warm-up steps would only repeat the work
+    # no warm-up runs: the C port keeps no state between ICs (its FFT twiddles are built on first
+    # use, a few milliseconds), so a warm-up would only repeat a full IC
     base, times = cpu_baseline(args, table, steps=args.steps)
-    total = sum(times) * (args.N / 256) ** 3
+    cfg = config(args)
+    cfg["precision"] = "fp64"
     line = {"impl": "reference", "metric": METRIC, "value": base["value"], "unit": UNIT,
             "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 / base["value"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (xoshiro noise, BBKS table)",
-            "config": config(args), "cpu_baseline": base,
+            "config": cfg, "cpu_baseline": base,
             "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
+
+
+NOISE_CASES = (("64^3 seed 42 L 256 (C1)", 64, 42, 256.0), ("256^3 seed 7 L 500 (C2)", 256, 7, 500.0))
+
+
+def gpu_noise(ml) -> dict:
+    """FP64 and FP32 white noise of the two precision configurations from the GPU (host copies)"""
+    out = {}
+    for name, N, seed, L in NOISE_CASES:
+        for prec in (ml.FP64, ml.FP32):
+            g = ml.alloc_local_grid(N, L, prec)
+            ml.generate_complex_grf(g, ml.rng_init(seed))
+            out[(name, prec)] = ml.get_fbox(g)
+            ml.free_local_grid(g)
+    return out
+
+
+def noise_exactness(ml, noise: dict) -> dict:
+    """(CPU leg: the oracle as the checker) the GPU's Gaussians against the reference's (the oracle,
+    host libm): FP64 equal bit for bit except where the host libm misrounded log or cos (each such
+    value checked to be the exactly rounded one); FP32 against the reference rounded to float"""
+    import math
+    import oracle
+    from oracle import crcheck
+    out = {}
+    for name, N, seed, L in NOISE_CASES:
+        ref = oracle.grf(N, L, seed, hermitian=False).view(np.float64).ravel()[2:]
+        g64 = noise[(name, ml.FP64)].view(np.float64).ravel()[2:]
+        g32 = noise[(name, ml.FP32)].view(np.float32).ravel()[2:]
+        d = oracle.draws(seed, 2 * len(ref))
+        factor = math.sqrt(L ** 3 / 2)
+        differ = np.nonzero(g64 != ref)[0]
+        explained = 0
+        for i in differ:
+            u, y = crcheck.sample_norm_parts(int(d[2 * i]), int(d[2 * i + 1]))
+            lu, cy = crcheck.exact_log(u), crcheck.exact_cos(y)
+            misround = math.log(u) != lu or math.cos(y) != cy
+            explained += int(misround and g64[i] == math.sqrt(-2.0 * lu) * cy * factor)
+        u32 = crcheck.ulps(g32, ref.astype(np.float32))
+        out[name] = {"gaussians": int(len(ref)),
+                     "fp64": {"equal": int(len(ref) - len(differ)), "differ": int(len(differ)),
+                              "differ_at_libm_misroundings_exact": explained,
+                              "max_ulp": float(crcheck.ulps(g64, ref).max())},
+                     "fp32": {"equal_to_float_of_reference": float(np.mean(g32 == ref.astype(np.float32))),
+                              "max_ulp": float(u32.max()), "p999_ulp": float(np.percentile(u32, 99.9))}}
+    return out
 
 
 def config(args):
@@ -231,6 +281,62 @@ def extras(ml, table, spline, args) -> dict:
     rel = np.abs(r32["pk_p"][ok] / r64["pk_p"][ok] - 1)
     out["fp64"] = {"ms_per_ic": ms64, "ic_per_s": 1e3 / ms64,
                    "pk_fp32_vs_fp64": {"max_rel": float(rel.max()), "bins": int(ok.sum()), "target": 1e-4}}
+
+    # the precision study at 256^3 (box 500 Mpc/h, seed 7, 128 linear shells): FP32 against the FP64
+    # GPU path for the first- and second-order displacement grids separately and P(k) per bin
+    from mitos_gb300 import study
+    d64 = study.displacement_orders(256, 500.0, 7, table, spline, ml.FP64)
+    d32 = study.displacement_orders(256, 500.0, 7, table, spline, ml.FP32)
+    c64 = ml.ic_pipeline_run(cfg(ml.FP64, 7, 256, 500.0, 128), spline)
+    c32 = ml.ic_pipeline_run(cfg(ml.FP32, 7, 256, 500.0, 128), spline)
+    okc = c64["pk_obs"] > 0
+    out["precision_256"] = {"disp1_rms_rel": study.rms_rel(d32[1], d64[1]),
+                            "disp2_rms_rel": study.rms_rel(d32[2], d64[2]),
+                            "disp_target": 1e-5,
+                            "pk_max_rel_per_bin": float(np.abs(c32["pk_p"][okc] / c64["pk_p"][okc] - 1).max()),
+                            "pk_bins": int(okc.sum()), "pk_target": 1e-4,
+                            "pk_obs_equal": bool(np.array_equal(c32["pk_obs"], c64["pk_obs"]))}
+    del d64, d32
+
+    # the library's 3D FFTs against cuFFT (torch.fft) at 512^3 FP32: a comparison line only (cuFFT is
+    # never on the path); both CUDA-event timed on their own streams, median of 5 after a warm-up
+    import torch
+    g = ml.alloc_local_grid(N, L, ml.FP32)
+    ml.set_box(g, np.random.default_rng(1).standard_normal((N, N, N)).astype(np.float32))
+    ours = {"r2c": [], "c2r": []}
+    for i in range(6):
+        ml.timer_start()
+        ml.fft_r2c_dg(g)
+        t_r2c = ml.timer_stop()
+        ml.timer_start()
+        ml.fft_c2r_dg(g)
+        t_c2r = ml.timer_stop()
+        if i:
+            ours["r2c"].append(t_r2c)
+            ours["c2r"].append(t_c2r)
+    ml.free_local_grid(g)
+    x = torch.randn((N, N, N), dtype=torch.float32, device="cuda")
+    cu = {"r2c": [], "c2r": []}
+    for i in range(6):
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        e[0].record()
+        k = torch.fft.rfftn(x)
+        e[1].record()
+        y = torch.fft.irfftn(k, s=(N, N, N))
+        e[2].record()
+        torch.cuda.synchronize()
+        if i:
+            cu["r2c"].append(e[0].elapsed_time(e[1]))
+            cu["c2r"].append(e[1].elapsed_time(e[2]))
+    del x, k, y
+    torch.cuda.empty_cache()
+    Gc = N * N * (N // 2 + 1) * 8
+    med = statistics.median
+    out["fft_vs_cufft"] = {
+        "N": N, "precision": "fp32", "note": "read real + write complex (or the reverse) once = 2 G per transform",
+        "ours_ms": {k: med(v) for k, v in ours.items()}, "cufft_ms": {k: med(v) for k, v in cu.items()},
+        "ours_GBps_at_2G": {k: 2 * Gc / (med(v) / 1e3) / 1e9 for k, v in ours.items()},
+        "cufft_GBps_at_2G": {k: 2 * Gc / (med(v) / 1e3) / 1e9 for k, v in cu.items()}}
 
     # particle velocities (the velocity transfer function t_cdm, 2LPT with the reference's velocity
     # factors, TSC gather at the displaced positions): the 512^3 FP32 IC with positions and velocities
@@ -560,9 +666,12 @@ def main():
             "kernels": kernels, "clocks": clk}
     if not args.no_extras and N == 512 and prec == ml.FP32:
         line["extras"] = extras(ml, table, spline, args)
+    noise = gpu_noise(ml) if not args.no_cpu_baseline else None
     if not args.no_cpu_baseline:
         base, _ = cpu_baseline(args, table, steps=1)
         line["cpu_baseline"] = base
+        if noise is not None:
+            line["noise_exact"] = noise_exactness(ml, noise)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

@@ -255,6 +255,15 @@ int mitos_ma_history(double *eps, double *rel, int max);
  * the start state of noise column c of an N grid. */
 int mitos_rng_jump(uint64_t s[4], unsigned long long n);
 int mitos_noise_column_state(int N, long c, const uint64_t s0[4], uint64_t out[4]);
+/* Host copies of the FP64 white noise's arithmetic (no reference counterpart; the device kernel
+ * performs the same operations): the correctly rounded log (x > 0) and cos (|y| < 8), and
+ * sampleNorm (src/random.c:34-49) of the draws A, B with them.  mitos_cr_steps gives the two steps
+ * of the evaluation separately (fn 0: log, 1: cos): the fast step's rounding, NaN when it cannot
+ * decide, and the accurate step's. */
+double mitos_cr_log(double x);
+double mitos_cr_cos(double y);
+double mitos_sample_norm_cr(uint64_t A, uint64_t B);
+int mitos_cr_steps(int fn, double x, double *fast, double *accurate);
 
 /* CIC mass assignment of n particles (float x,y,z triples, host or device pointer) onto the
  * real part of rho (padded layout), accumulated on top of its contents:

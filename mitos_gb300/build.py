@@ -19,8 +19,10 @@ SOURCES = ["context.cu", "noise.cu", "kspace.cu", "fft_passes.cu", "particles.cu
 NO_FMAD = {"kspace.cu"}
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-         "-Xptxas", "-warn-spills"]
+# host code uncontracted: the host copies of the correctly rounded log / cos (crmath.cuh) then
+# perform the device's exact operation sequence
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+         "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 
 
 def nvcc() -> str:

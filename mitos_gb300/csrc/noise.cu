@@ -402,3 +402,24 @@ extern "C" int mitos_noise_column_state(int N, long c, const uint64_t s0[4], uin
     for (int i = 0; i < 4; i++) out[i] = s[i];
     return 0;
 }
+
+// ---- host copies of the FP64 Box-Muller transform and its correctly rounded log and cos ------
+// (the device's operation sequence on the host; for checks without a GPU)
+extern "C" double mitos_cr_log(double x) { return crm::cr_log(x); }
+extern "C" double mitos_cr_cos(double y) { return crm::cr_cos(y); }
+extern "C" double mitos_sample_norm_cr(uint64_t A, uint64_t B) { return crm::box_muller(A, B); }
+// the fast step's rounding (NaN when its error interval straddles a rounding boundary) and the
+// accurate step's, separately
+extern "C" int mitos_cr_steps(int fn, double x, double *fast, double *accurate) {
+    if (fn == 0) {
+        const crm::LogArg a = crm::log_reduce(x);
+        *fast = crm::ziv_round(crm::log_fast(a), crm::kZivEps);
+        *accurate = crm::round_td(crm::log_accurate(a));
+    } else {
+        crm::CosArg ca;
+        crm::td t;
+        *fast = crm::ziv_round(crm::cos_fast(x, ca, t), crm::kZivEps);
+        *accurate = crm::round_td(crm::cos_accurate(ca, t));
+    }
+    return 0;
+}

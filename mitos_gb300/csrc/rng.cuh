@@ -9,6 +9,7 @@
 #include <stdint.h>
 
 #include "context.cuh"
+#include "crmath.cuh"
 
 namespace mitos {
 
@@ -30,8 +31,14 @@ __device__ __forceinline__ uint64_t dnext(uint64_t &s0, uint64_t &s1, uint64_t &
     return result;
 }
 
-// sampleNorm in FP64: src/random.c:34-49 (2^64 = (double)UINT64_MAX + 1)
-__device__ __forceinline__ double gauss64(uint64_t A, uint64_t B) {
+// sampleNorm in FP64: src/random.c:34-49 (2^64 = (double)UINT64_MAX + 1), with the correctly
+// rounded log and cos of crmath.cuh: the reference formula's exactly rounded value, which the host
+// libm gives too except where it misrounds by an ulp
+__device__ __forceinline__ double gauss64(uint64_t A, uint64_t B) { return crm::box_muller(A, B); }
+
+// the same with the device libm's log and cos (within an ulp or two): for the thermal normals,
+// whose float outputs absorb such differences
+__device__ __forceinline__ double gauss64_libm(uint64_t A, uint64_t B) {
     const double RMax = 18446744073709551616.0;
     const double u = (__ull2double_rn(A) + 0.5) / RMax;
     const double v = (__ull2double_rn(B) + 0.5) / RMax;

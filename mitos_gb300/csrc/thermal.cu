@@ -281,7 +281,7 @@ k_thermal(long n, int R, RngState s0, const uint64_t *__restrict__ polys, ThermT
             double e[3];
             for (int m = 0; m < 3; m++) {
                 const uint64_t A = dnext(r0, r1, r2, r3), B = dnext(r0, r1, r2, r3);
-                e[m] = gauss64(A, B);
+                e[m] = gauss64_libm(A, B);
             }
             const double len = hypot(e[0], hypot(e[1], e[2]));
             if (len > 0)

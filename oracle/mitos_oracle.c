@@ -903,6 +903,13 @@ void orc_lattice(int M, double boxlen, float *pos) {
 }
 
 static inline long wrapi(long i, long N) { return ((i % N) + N) % N; }
+/* the same, without divisions for i in [-N, 2N) */
+static inline long wrap1(long i, long N) {
+    if (i >= 0 && i < N) return i;
+    if (i < 0 && i >= -N) return i + N;
+    if (i >= N && i < 2 * N) return i - N;
+    return wrapi(i, N);
+}
 
 /* gridTSC_dg + access_grid on one rank: src/grids_interp.c:267-309, :180-207 */
 double orc_tsc_gather(const double *box, int N, double boxlen, double x, double y, double z) {
@@ -919,21 +926,34 @@ double orc_tsc_gather(const double *box, int N, double boxlen, double x, double 
     int lookRgtY = (int)floor((Y - iY) + lookLength);
     int lookLftZ = (int)floor((Z - iZ) - lookLength);
     int lookRgtZ = (int)floor((Z - iZ) + lookLength);
-    double sum = 0;
-    for (int i = lookLftX; i <= lookRgtX; i++) {
-        for (int j = lookLftY; j <= lookRgtY; j++) {
-            for (int k = lookLftZ; k <= lookRgtZ; k++) {
-                double xx = fabs(X - (iX + i));
-                double yy = fabs(Y - (iY + j));
-                double zz = fabs(Z - (iZ + k));
-                double part_x = xx < 0.5 ? (0.75 - xx * xx) : (xx < 1.5 ? 0.5 * (1.5 - xx) * (1.5 - xx) : 0);
-                double part_y = yy < 0.5 ? (0.75 - yy * yy) : (yy < 1.5 ? 0.5 * (1.5 - yy) * (1.5 - yy) : 0);
-                double part_z = zz < 0.5 ? (0.75 - zz * zz) : (zz < 1.5 ? 0.5 * (1.5 - zz) * (1.5 - zz) : 0);
-                long gx = wrapi(iX + i, N), gy = wrapi(iY + j, N), gz = wrapi(iZ + k, N);
-                sum += box[(gx * N + gy) * (N + 2) + gz] * (part_x * part_y * part_z);
-            }
-        }
+    /* the per-axis weights and wrapped indices, each evaluated once (the same operations as the
+     * reference's triple loop, so the same values; the sum keeps its order) */
+    double wx[4], wy[4], wz[4];
+    long gx[4], gy[4], gz[4];
+    const int nx = lookRgtX - lookLftX + 1, ny = lookRgtY - lookLftY + 1, nz = lookRgtZ - lookLftZ + 1;
+    if (nx > 4 || ny > 4 || nz > 4) return NAN;
+    for (int a = 0; a < nx; a++) {
+        const int i = lookLftX + a;
+        double xx = fabs(X - (iX + i));
+        wx[a] = xx < 0.5 ? (0.75 - xx * xx) : (xx < 1.5 ? 0.5 * (1.5 - xx) * (1.5 - xx) : 0);
+        gx[a] = (long)N * (N + 2) * wrap1(iX + i, N);
     }
+    for (int a = 0; a < ny; a++) {
+        const int j = lookLftY + a;
+        double yy = fabs(Y - (iY + j));
+        wy[a] = yy < 0.5 ? (0.75 - yy * yy) : (yy < 1.5 ? 0.5 * (1.5 - yy) * (1.5 - yy) : 0);
+        gy[a] = (N + 2) * wrap1(iY + j, N);
+    }
+    for (int a = 0; a < nz; a++) {
+        const int k = lookLftZ + a;
+        double zz = fabs(Z - (iZ + k));
+        wz[a] = zz < 0.5 ? (0.75 - zz * zz) : (zz < 1.5 ? 0.5 * (1.5 - zz) * (1.5 - zz) : 0);
+        gz[a] = wrap1(iZ + k, N);
+    }
+    double sum = 0;
+    for (int a = 0; a < nx; a++)
+        for (int b = 0; b < ny; b++)
+            for (int c = 0; c < nz; c++) sum += box[gx[a] + gy[b] + gz[c]] * (wx[a] * wy[b] * wz[c]);
     return sum;
 }
 
@@ -975,7 +995,7 @@ double orc_cic_deposit(long n, const float *pos, double mass, int N, double boxl
         double dx = X - iX, dy = Y - iY, dz = Z - iZ;
         double tx = 1.0 - dx, ty = 1.0 - dy, tz = 1.0 - dz;
         double val = Mp / grid_cell_vol;
-#define RM(i, j, k) ((wrapi(i, N) * N + wrapi(j, N)) * N + wrapi(k, N))
+#define RM(i, j, k) ((wrap1(i, N) * N + wrap1(j, N)) * N + wrap1(k, N))
         box[RM(iX, iY, iZ)] += val * tx * ty * tz;
         box[RM(iX + 1, iY, iZ)] += val * dx * ty * tz;
         box[RM(iX, iY + 1, iZ)] += val * tx * dy * tz;

@@ -9,7 +9,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def test_reference_arm_json_line():
-    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1", "--N", "64", "--boxlen", "125",
                         "--warmup", "3"], capture_output=True, text=True, timeout=600, cwd=ROOT)
     assert r.returncode == 0, r.stderr[-2000:]
     line = json.loads(r.stdout.strip().splitlines()[-1])
@@ -18,7 +18,7 @@ def test_reference_arm_json_line():
         assert key in line, key
     assert line["impl"] == "reference" and line["steps"] == 1 and line["warmup"] >= 3
     assert line["value"] > 0 and line["higher_is_better"] is True
-    assert "workload" in line["config"]
+    assert "workload" in line["config"] and line["config"]["precision"] == "fp64" and line["dtype"] == "f64"
     cb = line["cpu_baseline"]
     assert {"value", "unit", "cores", "kind", "sample"} <= set(cb) and cb["kind"] in ("port", "reference")
     assert cb["value"] == line["value"]

@@ -75,15 +75,18 @@ def test_noalloc_matches_oracle(N, L, bins, linear):
         ok = ro > 0
         assert np.abs(p[ok] - rp[ok]).max() <= 1e-12 * np.abs(rp[ok]).max()
         assert np.abs(k[ok] / rk[ok] - 1).max() < 1e-12
-    # the six |n| = 1 modes (multiplicity 1 on the kz = 0 plane, 2 for kz = 1) sit in bin 0
+    # the six |n| = 1 modes (multiplicity 1 on the kz = 0 plane, 2 for kz = 1) sit in log bin 0
+    # (u = 0 exactly), or in linear shell bins / (N/2) (shells of width (N/2) / bins in |n|)
     one = np.zeros((N, N, N // 2 + 1), complex)
     for x, y, z in ((1, 0, 0), (N - 1, 0, 0), (0, 1, 0), (0, N - 1, 0), (0, 0, 1)):
         one[x, y, z] = 1.0
     ml.set_fbox(g1, one)
     st, k, p, o = _noalloc(N, L, g1, g1, bins, linear)
     assert st == 0
-    assert o[0] >= 6
-    assert p[0] > 0 and np.all(p[1:][o[1:] > 0] == 0)
+    b1 = bins // (N // 2) if linear else 0
+    assert o[b1] >= 6
+    others = np.arange(bins) != b1
+    assert p[b1] > 0 and np.all(p[others & (o > 0)] == 0)
     ml.free_local_grid(g1)
     ml.free_local_grid(g2)
 
