@@ -234,6 +234,34 @@ int dg_copy_to_host(const struct distributed_grid *dg, int which, void *host);
 int dg_field_to_host(const struct distributed_grid *dg, double *host);
 int dg_copy_from_host(struct distributed_grid *dg, int which, const void *host);
 
+/* The attribute values of the snapshot's /Header, /Cosmology and /Units groups, as
+ * writeHeaderAttributes (src/header.c:26-175) writes them; the file, group and attribute calls
+ * stay with the caller's HDF5 writer (host I/O).  The particle numbers come from the types whose
+ * export name is "PartType0" .. "PartType6" (summed per name, as the reference does). */
+struct snapshot_header {
+    double BoxSize[3];                /* /Header */
+    int Dimension;
+    double Redshift;
+    int Flag_Entropy_ICs;
+    int NumFilesPerSnapshot;
+    long NumPart_Total[7];
+    long NumPart_Total_HighWord[7];
+    double MassTable[7];
+    double Cosmology_Redshift;        /* /Cosmology */
+    double Unit_mass_cgs;             /* /Units: "Unit mass in cgs (U_M)" and the rest */
+    double Unit_length_cgs;
+    double Unit_time_cgs;
+    double Unit_temperature_cgs;
+    double Unit_current_cgs;
+};
+/* boxlen (pars->BoxLen), z_ini (cosmo->z_ini); per particle type its ExportName and
+ * TotalNumber; the unit system (us->UnitMassKilogram, UnitLengthMetres, UnitTimeSeconds,
+ * UnitTemperatureKelvin, UnitCurrentAmpere).  Host only; returns 0, or 1 for invalid arguments. */
+int snapshot_header_attributes(double boxlen, double z_ini, int num_types, const char *const *export_names,
+                               const long long *total_numbers, double unit_mass_kg, double unit_length_m,
+                               double unit_time_s, double unit_temperature_K, double unit_current_A,
+                               struct snapshot_header *out);
+
 /* Description of the last failure (empty when none), and the number of kernels launched. */
 const char *mitos_last_error(void);
 long mitos_launch_count(void);

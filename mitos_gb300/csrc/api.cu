@@ -1,5 +1,6 @@
 // api.cu -- the reference entry points (include/mitos_gb300.h) over device grids.
 #include <math.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -281,6 +282,39 @@ extern "C" int dg_copy_to_host(const struct distributed_grid *dg, int which, voi
     MITOS_CUDA(cudaMemcpyAsync(host, src, grid_bytes(dg), cudaMemcpyDeviceToHost, stream()));
     return sync_all();
 }
+// writeHeaderAttributes (src/header.c:26-175): the values of its attributes, without the HDF5 calls
+extern "C" int snapshot_header_attributes(double boxlen, double z_ini, int num_types, const char *const *export_names,
+                                          const long long *total_numbers, double unit_mass_kg, double unit_length_m,
+                                          double unit_time_s, double unit_temperature_K, double unit_current_A,
+                                          struct snapshot_header *out) {
+    if (!out || num_types < 0 || (num_types > 0 && (!export_names || !total_numbers))) {
+        mitos::set_error(1, "snapshot_header_attributes: invalid arguments");
+        return 1;
+    }
+    memset(out, 0, sizeof *out);
+    for (int c = 0; c < 3; c++) out->BoxSize[c] = boxlen;  // :38-40
+    out->Dimension = 3;
+    out->Redshift = z_ini;
+    out->Flag_Entropy_ICs = 0;
+    out->NumFilesPerSnapshot = 1;
+    // :79-92: types whose export name is PartType<i> add their total number to entry i; the high
+    // words and the mass table are written as zeros
+    for (int i = 0; i < 7; i++) {
+        char want[40];
+        snprintf(want, sizeof want, "PartType%d", i);
+        for (int t = 0; t < num_types; t++)
+            if (export_names[t] && strcmp(export_names[t], want) == 0) out->NumPart_Total[i] += (long)total_numbers[t];
+    }
+    out->Cosmology_Redshift = z_ini;  // :119-121
+    // :136-141: SI to cgs
+    out->Unit_mass_cgs = unit_mass_kg * 1000;
+    out->Unit_length_cgs = unit_length_m * 100;
+    out->Unit_time_cgs = unit_time_s;
+    out->Unit_temperature_cgs = unit_temperature_K;
+    out->Unit_current_cgs = unit_current_A;
+    return 0;
+}
+
 extern "C" int dg_field_to_host(const struct distributed_grid *dg, double *host) {
     if (!dg || !dg->box || !host) { set_error(1, "grid part not allocated"); return 1; }
     if (dg->momentum_space == 1) { set_error(2, "attempting to export while in momentum space"); return 2; }

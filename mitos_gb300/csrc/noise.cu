@@ -417,9 +417,8 @@ extern "C" int mitos_cr_steps(int fn, double x, double *fast, double *accurate) 
         *accurate = crm::round_td(crm::log_accurate(a));
     } else {
         crm::CosArg ca;
-        crm::td t;
-        *fast = crm::ziv_round(crm::cos_fast(x, ca, t), crm::kZivEps);
-        *accurate = crm::round_td(crm::cos_accurate(ca, t));
+        *fast = crm::ziv_round(crm::cos_fast(x, ca), crm::kZivEps);
+        *accurate = crm::round_td(crm::cos_accurate(x));
     }
     return 0;
 }

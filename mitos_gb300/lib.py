@@ -130,7 +130,8 @@ EXPORTS = ["alloc_local_grid", "free_local_grid", "free_local_real_grid", "free_
            "mitos_last_error", "mitos_launch_count", "mitos_release_all", "cic_deposit_dg",
            "ic_pipeline_run", "ic_pipeline_run_table", "mitos_timer_start", "mitos_timer_stop",
            "mitos_sync", "mitos_kernel_timing", "mitos_kernel_times", "mitos_stage_times",
-           "mitos_ma_history", "mitos_rng_jump", "mitos_noise_column_state"] + \
+           "mitos_ma_history", "mitos_rng_jump", "mitos_noise_column_state", "mitos_cr_log", "mitos_cr_cos",
+           "mitos_sample_norm_cr", "mitos_cr_steps", "snapshot_header_attributes"] + \
           ["kernel_" + k for k in KERNEL_NAMES]
 
 
@@ -445,6 +446,45 @@ def ic_pipeline_run(cfg: ICConfig, spline: Spline, want_pos: bool = False, want_
     if vel is not None:
         out["vel"] = vel
     out.update(snap)
+    return out
+
+
+class SnapshotHeader(ctypes.Structure):
+    _fields_ = [("BoxSize", ctypes.c_double * 3), ("Dimension", ctypes.c_int), ("Redshift", ctypes.c_double),
+                ("Flag_Entropy_ICs", ctypes.c_int), ("NumFilesPerSnapshot", ctypes.c_int),
+                ("NumPart_Total", ctypes.c_long * 7), ("NumPart_Total_HighWord", ctypes.c_long * 7),
+                ("MassTable", ctypes.c_double * 7), ("Cosmology_Redshift", ctypes.c_double),
+                ("Unit_mass_cgs", ctypes.c_double), ("Unit_length_cgs", ctypes.c_double),
+                ("Unit_time_cgs", ctypes.c_double), ("Unit_temperature_cgs", ctypes.c_double),
+                ("Unit_current_cgs", ctypes.c_double)]
+
+
+# (group, attribute name) of writeHeaderAttributes (src/header.c:26-175) -> SnapshotHeader field
+HEADER_ATTRIBUTES = {
+    ("/Header", "BoxSize"): "BoxSize", ("/Header", "Dimension"): "Dimension",
+    ("/Header", "Redshift"): "Redshift", ("/Header", "Flag_Entropy_ICs"): "Flag_Entropy_ICs",
+    ("/Header", "NumFilesPerSnapshot"): "NumFilesPerSnapshot", ("/Header", "NumPart_Total"): "NumPart_Total",
+    ("/Header", "NumPart_Total_HighWord"): "NumPart_Total_HighWord", ("/Header", "MassTable"): "MassTable",
+    ("/Cosmology", "Redshift"): "Cosmology_Redshift",
+    ("/Units", "Unit mass in cgs (U_M)"): "Unit_mass_cgs", ("/Units", "Unit length in cgs (U_L)"): "Unit_length_cgs",
+    ("/Units", "Unit time in cgs (U_t)"): "Unit_time_cgs",
+    ("/Units", "Unit temperature in cgs (U_T)"): "Unit_temperature_cgs",
+    ("/Units", "Unit current in cgs (U_I)"): "Unit_current_cgs"}
+
+
+def snapshot_header(boxlen: float, z_ini: float, types, units) -> dict:
+    """types: [(ExportName, TotalNumber)]; units: (kg, m, s, K, A) of the internal unit system.
+    Returns {(group, name): list of values} as writeHeaderAttributes writes them."""
+    n = len(types)
+    names = (ctypes.c_char_p * max(n, 1))(*[t[0].encode() for t in types])
+    tot = (ctypes.c_longlong * max(n, 1))(*[int(t[1]) for t in types])
+    h = SnapshotHeader()
+    _check(load().snapshot_header_attributes(ctypes.c_double(boxlen), ctypes.c_double(z_ini), n, names, tot,
+                                             *[ctypes.c_double(u) for u in units], ctypes.byref(h)))
+    out = {}
+    for key, f in HEADER_ATTRIBUTES.items():
+        v = getattr(h, f)
+        out[key] = list(v) if hasattr(v, "__len__") else [v]
     return out
 
 

@@ -231,6 +231,28 @@ def ref_powerspec_float_slab(N: int, X0: int, NX: int, boxlen: float, box1: np.n
     return k, p, o
 
 
+def ref_header_attributes(boxlen: float, z_ini: float, types, units):
+    """the attributes the reference's writeHeaderAttributes (src/header.c:26-175) writes, recorded by
+    the HDF5 stand-in: {(group, name): list of values}; None without the reference build"""
+    r = ref_lib()
+    if r is None:
+        return None
+    n = len(types)
+    names = (ctypes.c_char_p * max(n, 1))(*[t[0].encode() for t in types])
+    tot = (ctypes.c_longlong * max(n, 1))(*[int(t[1]) for t in types])
+    u = (ctypes.c_double * 5)(*units)
+    assert r.ref_header_attributes(ctypes.c_double(boxlen), ctypes.c_double(z_ini), n, names, tot, u) == 0
+    out = {}
+    g, nm = ctypes.create_string_buffer(32), ctypes.create_string_buffer(64)
+    ty, cnt = ctypes.c_int(), ctypes.c_int()
+    d, l = (ctypes.c_double * 8)(), (ctypes.c_longlong * 8)()
+    for i in range(r.orc_h5_count()):
+        r.orc_h5_get(i, g, nm, ctypes.byref(ty), ctypes.byref(cnt), d, l)
+        vals = [d[j] for j in range(cnt.value)] if ty.value == 1 else [l[j] for j in range(cnt.value)]
+        out[(g.value.decode(), nm.value.decode())] = vals
+    return out
+
+
 def ic_params(N, M, boxlen, seed, table, lpt_order=2, ma_cycles=0, pk_bins=32, pk_linear=True,
               z_ini=31.0, mass=1.0, index_src=0, index_vel=-1, thermal=0, thermal_T_eV=0.0,
               thermal_M_eV=0.0, speed_of_light=0.0, thermal_draw_offset=0):

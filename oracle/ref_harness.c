@@ -399,3 +399,34 @@ int ref_ic_pipeline(int N, int M, double L, uint64_t seed, double A_s, double n_
     cleanPerturbSpline(&spline);
     return 0;
 }
+
+/* writeHeaderAttributes (src/header.c:26-175) of a run with the given box, redshift, particle
+ * types (ExportName, TotalNumber) and units; the attributes it writes are recorded by the HDF5
+ * stand-in (orc_h5_count / orc_h5_get) */
+void orc_h5_reset(void);
+int ref_header_attributes(double boxlen, double z_ini, int ntypes, const char **export_names,
+                          const long long *total_numbers, const double *units5) {
+    struct params pars;
+    struct cosmology cosmo;
+    struct units us;
+    memset(&pars, 0, sizeof pars);
+    memset(&cosmo, 0, sizeof cosmo);
+    memset(&us, 0, sizeof us);
+    pars.BoxLen = boxlen;
+    pars.NumParticleTypes = ntypes;
+    cosmo.z_ini = z_ini;
+    us.UnitMassKilogram = units5[0];
+    us.UnitLengthMetres = units5[1];
+    us.UnitTimeSeconds = units5[2];
+    us.UnitTemperatureKelvin = units5[3];
+    us.UnitCurrentAmpere = units5[4];
+    struct particle_type *types = calloc(ntypes > 0 ? ntypes : 1, sizeof *types);
+    for (int i = 0; i < ntypes; i++) {
+        types[i].ExportName = (char *)export_names[i];
+        types[i].TotalNumber = total_numbers[i];
+    }
+    orc_h5_reset();
+    int err = writeHeaderAttributes(&pars, &cosmo, &us, &types, (hid_t)1);
+    free(types);
+    return err;
+}

@@ -3,6 +3,7 @@
  * reference's hot-path C files compile and run unmodified inside the oracle build.
  * TEST INFRASTRUCTURE ONLY (linked into oracle/_ref/libmitos_ref.so, never into the product).
  */
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #include "ref_shim/mpi.h"
@@ -96,5 +97,78 @@ struct distributed_grid;
 int writeFieldFile_dg(struct distributed_grid *dg, const char *fname) { (void)dg; (void)fname; return 0; }
 int sptChunked(int N, double boxlen, int cycles, char *basename, char *a, char *b, char *c, char *d) {
     (void)N; (void)boxlen; (void)cycles; (void)basename; (void)a; (void)b; (void)c; (void)d;
+    return 0;
+}
+
+/* ---- HDF5 attribute recorder (see ref_shim/hdf5.h) --------------------------------------- */
+#include "ref_shim/hdf5.h"
+#define ORC_H5_MAX 64
+struct orc_h5attr {
+    char group[32];
+    char name[64];
+    int type; /* 1 double, 2 int, 3 long */
+    int n;
+    double d[8];
+    long long l[8];
+};
+static struct orc_h5attr h5_attr[ORC_H5_MAX];
+static int h5_nattr = 0;
+static char h5_group[16][32];
+static int h5_ngroup = 0;
+static int h5_extent[16];
+static int h5_nspace = 0;
+
+hid_t H5Gcreate(hid_t loc, const char *name, hid_t lcpl, hid_t gcpl, hid_t gapl) {
+    (void)loc; (void)lcpl; (void)gcpl; (void)gapl;
+    if (h5_ngroup >= 16) return -1;
+    snprintf(h5_group[h5_ngroup], sizeof h5_group[0], "%s", name);
+    return 100 + h5_ngroup++;
+}
+herr_t H5Gclose(hid_t grp) { (void)grp; return 0; }
+hid_t H5Screate_simple(int rank, const hsize_t *dims, const hsize_t *maxdims) {
+    (void)rank; (void)maxdims;
+    if (h5_nspace >= 16) return -1;
+    h5_extent[h5_nspace] = (int)dims[0];
+    return 200 + h5_nspace++;
+}
+herr_t H5Sset_extent_simple(hid_t space, int rank, const hsize_t *dims, const hsize_t *maxdims) {
+    (void)rank; (void)maxdims;
+    h5_extent[space - 200] = (int)dims[0];
+    return 0;
+}
+herr_t H5Sclose(hid_t space) { (void)space; return 0; }
+hid_t H5Acreate1(hid_t loc, const char *name, hid_t type, hid_t space, hid_t acpl) {
+    (void)acpl;
+    if (h5_nattr >= ORC_H5_MAX) return -1;
+    struct orc_h5attr *a = &h5_attr[h5_nattr];
+    memset(a, 0, sizeof *a);
+    snprintf(a->group, sizeof a->group, "%s", h5_group[loc - 100]);
+    snprintf(a->name, sizeof a->name, "%s", name);
+    a->type = (int)type;
+    a->n = h5_extent[space - 200];
+    return 300 + h5_nattr++;
+}
+herr_t H5Awrite(hid_t attr, hid_t type, const void *buf) {
+    struct orc_h5attr *a = &h5_attr[attr - 300];
+    for (int i = 0; i < a->n && i < 8; i++) {
+        if (type == H5T_NATIVE_DOUBLE) a->d[i] = ((const double *)buf)[i];
+        else if (type == H5T_NATIVE_INT) a->l[i] = ((const int *)buf)[i];
+        else a->l[i] = ((const long *)buf)[i];
+    }
+    return 0;
+}
+herr_t H5Aclose(hid_t attr) { (void)attr; return 0; }
+
+void orc_h5_reset(void) { h5_nattr = h5_ngroup = h5_nspace = 0; }
+int orc_h5_count(void) { return h5_nattr; }
+/* attribute i: group and name (NUL-terminated, 32 and 64 bytes), type, count and values */
+int orc_h5_get(int i, char *group, char *name, int *type, int *n, double *d, long long *l) {
+    if (i < 0 || i >= h5_nattr) return 1;
+    memcpy(group, h5_attr[i].group, 32);
+    memcpy(name, h5_attr[i].name, 64);
+    *type = h5_attr[i].type;
+    *n = h5_attr[i].n;
+    memcpy(d, h5_attr[i].d, sizeof h5_attr[i].d);
+    memcpy(l, h5_attr[i].l, sizeof h5_attr[i].l);
     return 0;
 }

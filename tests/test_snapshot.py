@@ -59,3 +59,4 @@ def test_field_dataset(prec):
         assert e.value.code == 2
     finally:
         ml.free_local_grid(dg)
+
