@@ -474,6 +474,11 @@ int manet_train_step(struct manet *net, int N, int pitch, const float *delta, co
 /* out = scale_out * net(inputs) */
 int manet_infer(struct manet *net, int N, int pitch, const float *delta, const float *phi1,
                 const float *phi2, float *out);
+/* The grid the warm start of solveMongeAmpereTol runs the network on: 0 (default) the solve's own
+ * grid; Nw < N a coarser grid of the same box: the inputs are the solve's fields with the modes
+ * above Nw's Nyquist frequency dropped, and the correction enters phi(k) at those low modes only
+ * (the iteration then fixes the rest).  Nw must be a multiple of 32; returns 0 or 1. */
+int manet_set_warm_grid(struct manet *net, int Nw);
 
 /* Monge-Ampere to a tolerance (no reference counterpart; the cycle of src/monge_ampere.c:50-183
  * with phi kept in k space: phi(k) += G(k) r2c(res)(k)).  Stops when the relative rms residual

@@ -46,6 +46,107 @@ static int lap_diff(const GridGeom &g, double boxlen, const void *a, const void 
     return 0;
 }
 
+// ---- the warm start on a coarser grid ------------------------------------------------------
+// The modes of an Ns grid are the modes of the N grid (same box) with |k_i| <= Ns/2 in units of the
+// fundamental: Ns index xs <-> N index of the wavevector kint(xs, Ns).  The Ns grid's Nyquist modes
+// (an index at Ns/2) are left out in both directions: their mirror on the N grid is a different
+// mode, and their share of the correction is negligible.
+__device__ __forceinline__ int mode_index(int k, int N) { return k < 0 ? k + N : k; }
+
+// out (Ns modes) = in (N modes) at the shared wavevectors, zero at the Ns Nyquist modes
+template <typename T>
+__global__ void k_modes_down(int N, int Ns, const cplx<T> *__restrict__ in, cplx<T> *__restrict__ out) {
+    const int Hs = Ns / 2 + 1, H = N / 2 + 1;
+    const long n = (long)Ns * Ns * Hs;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const int zs = (int)(i % Hs);
+        const long xy = i / Hs;
+        const int ys = (int)(xy % Ns), xs = (int)(xy / Ns);
+        if (xs == Ns / 2 || ys == Ns / 2 || zs == Ns / 2) {
+            out[i] = mk<T>(0, 0);
+            continue;
+        }
+        const int x = mode_index(kint(xs, Ns), N), y = mode_index(kint(ys, Ns), N);
+        out[i] = in[((long)x * N + y) * H + zs];
+    }
+}
+
+// phi (N modes) += G(k) s(k) at the Ns modes but the Nyquist ones; G = -1/k^2, 1 at k = 0
+// (kernel_inv_poisson, include/fft_kernels.h:96-99)
+template <typename T>
+__global__ void k_add_poisson_up(int N, int Ns, T dk, const cplx<T> *__restrict__ s, cplx<T> *__restrict__ phi) {
+    const int Hs = Ns / 2 + 1, H = N / 2 + 1;
+    const long n = (long)Ns * Ns * Hs;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const int zs = (int)(i % Hs);
+        const long xy = i / Hs;
+        const int ys = (int)(xy % Ns), xs = (int)(xy / Ns);
+        if (xs == Ns / 2 || ys == Ns / 2 || zs == Ns / 2) continue;
+        const int kx = kint(xs, Ns), ky = kint(ys, Ns);
+        const T k2 = ((T)kx * kx + (T)ky * ky + (T)zs * zs) * dk * dk;
+        const T G = k2 > 0 ? -1 / k2 : (T)1;
+        const long j = ((long)mode_index(kx, N) * N + mode_index(ky, N)) * H + zs;
+        const cplx<T> v = s[i];
+        phi[j] = mk<T>(phi[j].x + G * v.x, phi[j].y + G * v.y);
+    }
+}
+
+template <typename T>
+static int modes_down(int N, int Ns, const void *in, void *out) {
+    const long n = (long)Ns * Ns * (Ns / 2 + 1);
+    launch_begin("modes_down");
+    k_modes_down<T><<<(unsigned)std::min<long>((n + 255) / 256, 152L * 16), 256, 0, stream()>>>(
+        N, Ns, (const cplx<T> *)in, (cplx<T> *)out);
+    count_launch();
+    MITOS_LAUNCH_CHECK("coarse-grid modes");
+    return 0;
+}
+
+template <typename T>
+static int add_poisson_up(int N, int Ns, double boxlen, const void *s, void *phi) {
+    const long n = (long)Ns * Ns * (Ns / 2 + 1);
+    launch_begin("add_poisson_up");
+    k_add_poisson_up<T><<<(unsigned)std::min<long>((n + 255) / 256, 152L * 16), 256, 0, stream()>>>(
+        N, Ns, (T)(2 * M_PI / boxlen), (const cplx<T> *)s, (cplx<T> *)phi);
+    count_launch();
+    MITOS_LAUNCH_CHECK("coarse-grid correction");
+    return 0;
+}
+
+int manet_warm_grid(const struct manet *net);
+
+// the network correction on the Ns grid: inputs delta, phi_1 = G delta and phi_2 = G r2c(S) reduced
+// to the Ns modes and back to real space there, inference, r2c, and phi(k) += G sigma(k) at those
+// modes (FP32 grids)
+static int warm_coarse(const GridGeom &g, int Ns, double L, struct manet *net, const void *dens_k, const void *S,
+                       void *Sk, void *phi) {
+    const int N = g.N, prec = MITOS_FP32;
+    const GridGeom *gsp = geom(Ns, prec);
+    if (!gsp) return 3;
+    const GridGeom &gs = *gsp;
+    const size_t sb = (size_t)gs.cells * csize(prec);
+    void *ck = workspace(sb, 40);
+    float *ds = (float *)workspace(sb, 41), *p1 = (float *)workspace(sb, 42), *p2 = (float *)workspace(sb, 43),
+          *sg = (float *)workspace(sb, 44);
+    if (!ck || !ds || !p1 || !p2 || !sg) return 5;
+    KernelParams kp;
+    memset(&kp, 0, sizeof kp);
+    kp.id = KID_INV_POISSON;
+    int e = modes_down<float>(N, Ns, dens_k, ck);
+    if (!e) e = grid_c2r(gs, prec, L, ck, ds);
+    if (!e) e = modes_down<float>(N, Ns, dens_k, ck);
+    if (!e) e = apply_kernel_launch(Ns, L, prec, kp, ck, ck);
+    if (!e) e = grid_c2r(gs, prec, L, ck, p1);
+    if (!e) e = grid_r2c(g, prec, L, S, N + 2, 1.0, 0.0, Sk);
+    if (!e) e = modes_down<float>(N, Ns, Sk, ck);
+    if (!e) e = apply_kernel_launch(Ns, L, prec, kp, ck, ck);
+    if (!e) e = grid_c2r(gs, prec, L, ck, p2);
+    if (!e) e = manet_infer(net, Ns, Ns + 2, ds, p1, p2, sg);
+    if (!e) e = grid_r2c(gs, prec, L, sg, Ns + 2, 1.0, 0.0, ck);
+    if (!e) e = add_poisson_up<float>(N, Ns, L, ck, phi);
+    return e;
+}
+
 // phi(k) += G(k) r2c(src)(k): src real (pitch N + 2); Sk complex scratch
 static int add_poisson(const GridGeom &g, int prec, double boxlen, const void *src, void *phi, void *Sk) {
     PassArgs a;
@@ -145,7 +246,18 @@ static int ma_run(struct distributed_grid *pot, struct distributed_grid *dens, s
         e = add_poisson(g, prec, L, work->box, pot->fbox, Sk);
         if (e) break;
         st->cycles++;
-        if (it == 0 && (warm || cap)) {
+        const int Nw = warm && !cap ? manet_warm_grid(warm) : 0;
+        if (it == 0 && Nw > 0 && Nw < N) {
+            // the network on the coarser grid
+            MITOS_CUDA(cudaEventRecord(ev[1], stream()));
+            e = warm_coarse(g, Nw, L, warm, dens->fbox, S, Sk, pot->fbox);
+            if (e) break;
+            MITOS_CUDA(cudaEventRecord(ev[2], stream()));
+            MITOS_CUDA(cudaEventSynchronize(ev[2]));
+            float wms = 0;
+            cudaEventElapsedTime(&wms, ev[1], ev[2]);
+            st->ms_warm = wms;
+        } else if (it == 0 && (warm || cap)) {
             // network inputs: delta(x) (the density box), phi_1(x), phi_2(x) = c2r(G S(k))
             MITOS_CUDA(cudaEventRecord(ev[1], stream()));
             float *d1 = cap ? cap->phi1 : (float *)workspace(gb, 34);

@@ -373,6 +373,7 @@ struct ManetState {
     unsigned char *live = nullptr;
     __nv_bfloat16 *wf = nullptr, *wb = nullptr;
     bool prepped = false;
+    int warm_N = 0;  // grid of the warm-start inference (0: the solve's own grid)
 };
 
 static ManetState *state(const struct manet *net) { return reinterpret_cast<ManetState *>(net->priv); }
@@ -632,3 +633,16 @@ extern "C" int manet_infer(struct manet *net, int N, int pitch, const float *del
     if (!e) e = forward(state(net), N, A, out, pitch, net->scale_out);
     return e;
 }
+
+extern "C" int manet_set_warm_grid(struct manet *net, int Nw) {
+    if (!net || !net->priv || Nw < 0 || (Nw && check_n(Nw))) {
+        mitos::set_error(1, "manet_set_warm_grid: a grid size that is a multiple of 32 (or 0)");
+        return 1;
+    }
+    state(net)->warm_N = Nw;
+    return 0;
+}
+
+namespace mitos {
+int manet_warm_grid(const struct manet *net) { return net && net->priv ? state(net)->warm_N : 0; }
+}  // namespace mitos

@@ -131,7 +131,7 @@ EXPORTS = ["alloc_local_grid", "free_local_grid", "free_local_real_grid", "free_
            "ic_pipeline_run", "ic_pipeline_run_table", "mitos_timer_start", "mitos_timer_stop",
            "mitos_sync", "mitos_kernel_timing", "mitos_kernel_times", "mitos_stage_times",
            "mitos_ma_history", "mitos_rng_jump", "mitos_noise_column_state", "mitos_cr_log", "mitos_cr_cos",
-           "mitos_sample_norm_cr", "mitos_cr_steps", "snapshot_header_attributes"] + \
+           "mitos_sample_norm_cr", "mitos_cr_steps", "snapshot_header_attributes", "manet_set_warm_grid"] + \
           ["kernel_" + k for k in KERNEL_NAMES]
 
 
@@ -583,6 +583,11 @@ def manet_train_step(net: Manet, N: int, pitch: int, delta, phi1, phi2, target, 
 
 def manet_infer(net: Manet, N: int, pitch: int, delta, phi1, phi2, out) -> None:
     _check(load().manet_infer(ctypes.byref(net), N, pitch, _vp(delta), _vp(phi1), _vp(phi2), _vp(out)))
+
+
+def manet_set_warm_grid(net: Manet, Nw: int) -> None:
+    """run the warm start's network on an Nw grid (0: the solve's own grid)"""
+    _check(load().manet_set_warm_grid(ctypes.byref(net), Nw))
 
 
 def manet_layers(p: np.ndarray):

@@ -82,3 +82,26 @@ def test_training_pair_and_warm_start(table, spline):
         ml.manet_free(net)
         train.free()
         held.free()
+
+
+def test_warm_start_on_a_coarser_grid(table, spline):
+    """the network trained on 32^3 grids of the same box corrects a 64^3 solve through its low
+    modes (manet_set_warm_grid): the residual after the first update drops and the solve meets the
+    tolerance; a grid that is not a multiple of 32 is refused"""
+    N, Nw, L = 64, 32, 125.0
+    train = manet.PairSet(Nw, L, range(2000, 2032), table, spline, cycles=10)
+    net = ml.manet_init(3)
+    try:
+        manet.set_scales(net, train.rms())
+        manet.train(net, train, 400, lr=2e-3)
+        ml.manet_set_warm_grid(net, Nw)
+        cmp = manet.compare(net, N, L, [3000, 3001], table, spline, tol=TOL64)
+        for c, w in zip(cmp["cold"], cmp["warm"]):
+            assert c["converged"] and w["converged"], (c, w)
+            assert w["rel_second"] < c["rel_second"], (c, w)
+            assert w["ms_warm"] > 0
+        with pytest.raises(ml.MitosError):
+            ml.manet_set_warm_grid(net, 48)
+    finally:
+        ml.manet_free(net)
+        train.free()
