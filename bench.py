@@ -425,10 +425,11 @@ def extras(ml, table, spline, args) -> dict:
     # 48 realisations (16 x 64^3 / 256, 16 x 96^3 / 384, 16 x 128^3 / 512 Mpc/h; 4 Mpc/h cells),
     # seeds 1000-1047, one captured CUDA graph over 8 streams, tiles from the autotuner
     sizes = [(64, 256.0), (96, 384.0), (128, 512.0)]
-    tiles = {}
+    tiles, radix = {}, {}
     for n, box in sizes:
         pxy, pz, _ = ml.autotune(cfg(ml.FP32, 1000, n, box, 32), spline)
         tiles[n] = [pxy, pz]
+        radix[n] = ml.get_radix(n, ml.FP32)
     cfgs = [cfg(ml.FP32, 1000 + 16 * k + i, n, box, 32) for k, (n, box) in enumerate(sizes) for i in range(16)]
     # batched units of the members of each size (one launch per pass per unit): the library's
     # default (16 per unit), 8 per unit, and unbatched (48 pipeline runs over 8 streams)
@@ -453,6 +454,7 @@ def extras(ml, table, spline, args) -> dict:
                        "max_batch": best, "units": units,
                        "ms_by_max_batch": {str(mb): v[0] for mb, v in by_batch.items()},
                        "latency_ms": lat, "gpu_launches_per_replay": launches, "tiles": tiles,
+                       "radix_schedules": {str(n): {"N": r[0], "N/2": r[1]} for n, r in radix.items()},
                        "roofline": {"model_bytes": model, "GBps": model / (t / 1e3) / 1e9,
                                     "frac": model / (t / 1e3) / 1e9 / peak}}
 

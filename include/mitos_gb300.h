@@ -528,12 +528,21 @@ int ic_ensemble_result(struct ic_ensemble *ens, int i, struct ic_result *res);
 int ic_ensemble_launches(const struct ic_ensemble *ens); /* kernel launches in one replay */
 int ic_ensemble_units(const struct ic_ensemble *ens);    /* batched pipeline runs in one replay */
 int ic_ensemble_destroy(struct ic_ensemble *ens);
-/* FFT tile autotuner: times the IC of cfg for every fitting pair of X/Y pencils per block and Z
- * rows per block, keeps the fastest for (N, precision) in this process and returns it. */
+/* FFT schedule autotuner: times the IC of cfg (best of three) over the radix schedules of the
+ * length-N transforms (X / Y passes), then of the length-N/2 transforms (Z passes), then over
+ * every fitting pair of X/Y pencils per block and Z rows per block; keeps the fastest for
+ * (N, precision) in this process and returns its tile (mitos_get_radix gives its radices). */
 int mitos_autotune(const struct ic_config *cfg, const struct perturb_spline *spline, int *p_xy,
                    int *p_z, double *ms);
 int mitos_set_tiles(int N, int precision, int p_xy, int p_z);
 int mitos_get_tiles(int N, int precision, int *p_xy, int *p_z);
+/* Radix schedules, first stage first: radices 2, 3, 4 or 8 that divide the elements a thread holds
+ * (8 for N = 2^k, 12 for 3 2^k), with product N (X / Y) and N/2 (Z); at most 11 stages.  Returns 1
+ * for a schedule that does not fit.  Any schedule but the default runs the FP32 sizes 256, 512
+ * and 1024 on the runtime-plan kernels instead of their compile-time ones.  mitos_get_radix fills
+ * arrays of at least 12 ints. */
+int mitos_set_radix(int N, int precision, const int *rad_n, int stages_n, const int *rad_h, int stages_h);
+int mitos_get_radix(int N, int precision, int *rad_n, int *stages_n, int *rad_h, int *stages_h);
 
 #ifdef __cplusplus
 }

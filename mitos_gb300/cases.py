@@ -1,0 +1,97 @@
+"""Small workloads that run one part of the library a few times, for profiling one kernel at a size
+whose grids still exceed L2 but whose device footprint stays at a few GB:
+
+    python -m mitos_gb300.cases conv 256     # network inference (k_conv), 4 layers
+    python -m mitos_gb300.cases ngenic 512   # the N-GenIC-like field (k_ngenic)
+    python -m mitos_gb300.cases ma 256       # Monge-Ampere cycles (z_hess_ma, x_add_poisson)
+    python -m mitos_gb300.cases noise 512    # white noise (k_noise), FP32
+    python -m mitos_gb300.cases ic 256       # one FP32 initial condition (every pass)
+
+Each runs its workload `reps` times (third argument, default 3) after one warm-up and prints the
+device time per repetition (CUDA events on the library stream).
+"""
+from __future__ import annotations
+
+import sys
+
+import numpy as np
+
+from . import lib as ml
+from . import manet
+from .perturb import load_table
+
+
+def conv(N: int, reps: int) -> float:
+    net = ml.manet_init(1)
+    g = [ml.alloc_local_grid(N, 2.0 * N, ml.FP32) for _ in range(4)]
+    rng = np.random.default_rng(0)
+    for x in g[:3]:
+        ml.set_box(x, rng.standard_normal((N, N, N)).astype(np.float32))
+    args = [ml._vp(x.box) for x in g]
+    ml.manet_infer(net, N, N + 2, *args)
+    ml.timer_start()
+    for _ in range(reps):
+        ml.manet_infer(net, N, N + 2, *args)
+    ms = ml.timer_stop() / reps
+    for x in g:
+        ml.free_local_grid(x)
+    ml.manet_free(net)
+    return ms
+
+
+def ngenic(N: int, reps: int) -> float:
+    g = ml.alloc_local_grid(N, 2.0 * N, ml.FP32)
+    ml.generate_ngeniclike_grf_dg(g, 1)
+    ml.timer_start()
+    for r in range(reps):
+        ml.generate_ngeniclike_grf_dg(g, 2 + r)
+    ms = ml.timer_stop() / reps
+    ml.free_local_grid(g)
+    return ms
+
+
+def ma(N: int, reps: int) -> float:
+    table = load_table()
+    spline = ml.Spline(table)
+    L = 500.0 * N / 256
+    dens = manet.density(N, L, 3000, table, spline)
+    pot, work = ml.alloc_local_grid(N, L, ml.FP32), ml.alloc_local_grid(N, L, ml.FP32)
+    ml.solveMongeAmpereTol(pot, dens, work, 0.0, 2)
+    ms = 0.0
+    for _ in range(reps):
+        st = ml.solveMongeAmpereTol(pot, dens, work, 0.0, 3)
+        ms += st["ms"]
+    for x in (pot, work, dens):
+        ml.free_local_grid(x)
+    return ms / reps
+
+
+def noise(N: int, reps: int) -> float:
+    g = ml.alloc_local_grid(N, 2.0 * N, ml.FP32)
+    ml.generate_complex_grf(g, ml.rng_init(1))
+    ml.timer_start()
+    for r in range(reps):
+        ml.generate_complex_grf(g, ml.rng_init(2 + r))
+    ms = ml.timer_stop() / reps
+    ml.free_local_grid(g)
+    return ms
+
+
+def ic(N: int, reps: int) -> float:
+    table = load_table()
+    spline = ml.Spline(table)
+    cfg = lambda s: ml.ic_config(N, N, 1000.0 * N / 512, s, table, pk_bins=64, pk_linear=True, precision=ml.FP32)
+    ml.ic_pipeline_run(cfg(1), spline)
+    ml.timer_start()
+    for r in range(reps):
+        ml.ic_pipeline_run(cfg(2 + r), spline)
+    return ml.timer_stop() / reps
+
+
+CASES = {"conv": conv, "ngenic": ngenic, "ma": ma, "noise": noise, "ic": ic}
+
+if __name__ == "__main__":
+    name = sys.argv[1]
+    N = int(sys.argv[2]) if len(sys.argv) > 2 else 256
+    reps = int(sys.argv[3]) if len(sys.argv) > 3 else 3
+    print(f"{name} N={N}: {CASES[name](N, reps):.4f} ms per repetition")

@@ -83,18 +83,17 @@ void count_launch(int n) {
     }
 }
 
-bool make_plan(int n, int E, int tw_len, FFTPlan *pl) {
-    if (n < E || n % E) return false;
-    int rem = n, ns = 0;
-    int rad[MITOS_MAX_STAGES];
-    auto push = [&](int r) { if (ns < MITOS_MAX_STAGES) rad[ns++] = r; };
-    if (E % 8 == 0) {
-        while (rem % 8 == 0) { push(8); rem /= 8; }
+// the plan of length n for the radices rad[0 .. ns-1] (first stage first): each radix one of 2, 3,
+// 4, 8 dividing E (a thread holds E elements: E / R butterflies a stage), their product n
+bool plan_from_radices(int n, int E, int tw_len, const int *rad, int ns, FFTPlan *pl) {
+    if (n < E || n % E || ns < 1 || ns >= MITOS_MAX_STAGES) return false;
+    long prod = 1;
+    for (int i = 0; i < ns; i++) {
+        const int r = rad[i];
+        if ((r != 2 && r != 3 && r != 4 && r != 8) || E % r) return false;
+        prod *= r;
     }
-    while (rem % 4 == 0 && E % 4 == 0) { push(4); rem /= 4; }
-    while (rem % 2 == 0 && E % 2 == 0) { push(2); rem /= 2; }
-    while (rem % 3 == 0 && E % 3 == 0) { push(3); rem /= 3; }
-    if (rem != 1 || ns == 0 || ns >= MITOS_MAX_STAGES) return false;
+    if (prod != n) return false;
     pl->n = n;
     pl->nst = ns;
     pl->tw_scale = tw_len / n;
@@ -109,6 +108,22 @@ bool make_plan(int n, int E, int tw_len, FFTPlan *pl) {
         Ns *= rad[i];
     }
     return true;
+}
+
+// the default schedule: radix 8 stages first (when E allows), then 4, 2 and 3
+bool make_plan(int n, int E, int tw_len, FFTPlan *pl) {
+    if (n < E || n % E) return false;
+    int rem = n, ns = 0;
+    int rad[MITOS_MAX_STAGES];
+    auto push = [&](int r) { if (ns < MITOS_MAX_STAGES) rad[ns++] = r; };
+    if (E % 8 == 0) {
+        while (rem % 8 == 0) { push(8); rem /= 8; }
+    }
+    while (rem % 4 == 0 && E % 4 == 0) { push(4); rem /= 4; }
+    while (rem % 2 == 0 && E % 2 == 0) { push(2); rem /= 2; }
+    while (rem % 3 == 0 && E % 3 == 0) { push(3); rem /= 3; }
+    if (rem != 1 || ns == 0 || ns >= MITOS_MAX_STAGES) return false;
+    return plan_from_radices(n, E, tw_len, rad, ns, pl);
 }
 
 static int elems_for(int N) {
@@ -142,6 +157,7 @@ const GridGeom *geom(int N, int precision) {
     g.plane = (long)N * g.H;
     g.cells = (long)N * g.plane;
     g.E = E;
+    g.custom_radix = 0;
     if (!make_plan(N, E, N, &g.plN) || !make_plan(N / 2, E, N, &g.plH)) {
         delete ge;
         set_error(3, "no FFT schedule for N = %d", N);
@@ -193,6 +209,45 @@ int set_tiles(int N, int precision, int p_xy, int p_z) {
     GridGeom *g = const_cast<GridGeom *>(gc);
     g->P_xy = p_xy;
     g->P_z = p_z;
+    return 0;
+}
+
+int set_radix(int N, int precision, const int *rad_n, int ns_n, const int *rad_h, int ns_h) {
+    const GridGeom *gc = geom(N, precision);
+    if (!gc) return 3;
+    FFTPlan pn, ph;
+    if (!rad_n || !rad_h || !plan_from_radices(N, gc->E, N, rad_n, ns_n, &pn) ||
+        !plan_from_radices(N / 2, gc->E, N, rad_h, ns_h, &ph)) {
+        set_error(1, "radix schedule does not fit N = %d (radices 2, 3, 4, 8 dividing %d, product N and N/2)", N,
+                  gc->E);
+        return 1;
+    }
+    std::lock_guard<std::mutex> lk(g_mu);
+    GridGeom *g = const_cast<GridGeom *>(gc);
+    FFTPlan dn, dh;
+    make_plan(N, g->E, N, &dn);
+    make_plan(N / 2, g->E, N, &dh);
+    auto same = [](const FFTPlan &a, const FFTPlan &b) {
+        if (a.nst != b.nst) return false;
+        for (int i = 0; i < a.nst; i++)
+            if (a.rad[i] != b.rad[i]) return false;
+        return true;
+    };
+    g->plN = pn;
+    g->plH = ph;
+    g->custom_radix = !(same(pn, dn) && same(ph, dh));
+    return 0;
+}
+
+int get_radix(int N, int precision, int *rad_n, int *ns_n, int *rad_h, int *ns_h) {
+    const GridGeom *g = geom(N, precision);
+    if (!g) return 3;
+    *ns_n = g->plN.nst;
+    *ns_h = g->plH.nst;
+    for (int i = 0; i < MITOS_MAX_STAGES; i++) {
+        rad_n[i] = i < g->plN.nst ? g->plN.rad[i] : 0;
+        rad_h[i] = i < g->plH.nst ? g->plH.rad[i] : 0;
+    }
     return 0;
 }
 

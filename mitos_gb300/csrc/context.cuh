@@ -23,6 +23,11 @@ void *workspace(size_t bytes, int slot);
 // passes (the autotuner's knobs); returns 1 when the tile does not fit the kernels' limits
 int set_tiles(int N, int precision, int p_xy, int p_z);
 int get_tiles(int N, int precision, int *p_xy, int *p_z);
+// radix schedules of the length-N (X / Y) and length-N/2 (Z) transforms, first stage first (the
+// autotuner's third knob); returns 1 for a schedule that does not fit.  A schedule other than the
+// default moves the FP32 sizes with compile-time kernels (256, 512, 1024) to the runtime-plan ones.
+int set_radix(int N, int precision, const int *rad_n, int ns_n, const int *rad_h, int ns_h);
+int get_radix(int N, int precision, int *rad_n, int *ns_n, int *rad_h, int *ns_h);
 void release_all();
 // the cached xoshiro jump-polynomial tables (noise.cu) and thermal sampler tables (thermal.cu)
 void release_jump_tables();

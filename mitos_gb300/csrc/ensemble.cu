@@ -269,37 +269,101 @@ extern "C" int ic_ensemble_destroy(struct ic_ensemble *ens) {
     return 0;
 }
 
-// ---- FFT tile autotuner ------------------------------------------------------------------------
+// ---- FFT schedule autotuner --------------------------------------------------------------------
 // Times the whole IC of cfg (pipeline launches on the library stream, CUDA events, best of three
-// after one warm-up) for each candidate tile and keeps the fastest in the grid geometry.
+// after one warm-up) and keeps the fastest schedule in the grid geometry, by coordinate descent
+// over three knobs: the radix schedule of the length-N transforms (X and Y passes), that of the
+// length-N/2 transforms (Z passes), then the tile (pencils per block of the X / Y passes, rows per
+// block of the Z passes).  Radix schedules: every order of radices 8, 4, 3, 2 dividing the
+// elements a thread holds, with at most one stage more than the fewest possible.
+
+// the ordered radix schedules of length n, at most maxst stages
+static void radix_schedules(int n, int E, int maxst, std::vector<std::vector<int>> &out) {
+    std::vector<int> cur;
+    struct Rec {
+        static void go(int rem, int E, int maxst, std::vector<int> &cur, std::vector<std::vector<int>> &out) {
+            if (rem == 1) {
+                if (!cur.empty()) out.push_back(cur);
+                return;
+            }
+            if ((int)cur.size() >= maxst) return;
+            for (int r : {8, 4, 3, 2})
+                if (E % r == 0 && rem % r == 0) {
+                    cur.push_back(r);
+                    go(rem / r, E, maxst, cur, out);
+                    cur.pop_back();
+                }
+        }
+    };
+    Rec::go(n, E, maxst, cur, out);
+}
+
+static int min_stages(const std::vector<std::vector<int>> &c) {
+    size_t m = 99;
+    for (auto &v : c) m = std::min(m, v.size());
+    return (int)m;
+}
+
 extern "C" int mitos_autotune(const struct ic_config *cfg, const struct perturb_spline *spline, int *best_pxy,
                               int *best_pz, double *best_ms) {
     if (!cfg || !spline) return 1;
+    const GridGeom *g = geom(cfg->N, cfg->precision);
+    if (!g) return 3;
     int p0, z0;
     int err = get_tiles(cfg->N, cfg->precision, &p0, &z0);
     if (err) return err;
     cudaEvent_t a, b;
     MITOS_CUDA(cudaEventCreate(&a));
     MITOS_CUDA(cudaEventCreate(&b));
+    auto timed = [&](double &t) -> int {
+        PipeOpts o = {nullptr, false};
+        int e = pipeline_spline(cfg, spline, nullptr, &o);
+        t = 1e30;
+        for (int r = 0; r < 3 && !e; r++) {
+            cudaEventRecord(a, stream());
+            e = pipeline_spline(cfg, spline, nullptr, &o);
+            cudaEventRecord(b, stream());
+            cudaEventSynchronize(b);
+            float ms = 0;
+            cudaEventElapsedTime(&ms, a, b);
+            t = std::min(t, (double)ms);
+        }
+        return e;
+    };
+    int rn[MITOS_MAX_STAGES], rh[MITOS_MAX_STAGES], nn, nh;
+    get_radix(cfg->N, cfg->precision, rn, &nn, rh, &nh);
+    std::vector<int> bn(rn, rn + nn), bh(rh, rh + nh);
     double best = 1e30;
+    err = timed(best);
+    // 1. radix schedule of the length-N transforms, 2. of the length-N/2 transforms
+    for (int knob = 0; knob < 2 && !err; knob++) {
+        std::vector<std::vector<int>> cands;
+        const int n = knob == 0 ? cfg->N : cfg->N / 2;
+        radix_schedules(n, g->E, 64, cands);
+        const int lim = min_stages(cands) + 1;
+        for (auto &c : cands) {
+            if ((int)c.size() > lim) continue;
+            const std::vector<int> &tn = knob == 0 ? c : bn, &th = knob == 0 ? bh : c;
+            if (set_radix(cfg->N, cfg->precision, tn.data(), (int)tn.size(), th.data(), (int)th.size())) continue;
+            double t;
+            err = timed(t);
+            if (err) break;
+            if (t < best) {
+                best = t;
+                (knob == 0 ? bn : bh) = c;
+            }
+        }
+        set_radix(cfg->N, cfg->precision, bn.data(), (int)bn.size(), bh.data(), (int)bh.size());
+    }
+    // 3. tiles with the chosen schedules
     int bp = p0, bz = z0;
     const int cand[] = {1, 2, 4, 8, 16, 32, 64};
     for (int px : cand)
         for (int pz : cand) {
-            if (set_tiles(cfg->N, cfg->precision, px, pz)) continue;
-            PipeOpts o = {nullptr, false};
-            err = pipeline_spline(cfg, spline, nullptr, &o);
             if (err) break;
-            double t = 1e30;
-            for (int r = 0; r < 3 && !err; r++) {
-                cudaEventRecord(a, stream());
-                err = pipeline_spline(cfg, spline, nullptr, &o);
-                cudaEventRecord(b, stream());
-                cudaEventSynchronize(b);
-                float ms = 0;
-                cudaEventElapsedTime(&ms, a, b);
-                t = std::min(t, (double)ms);
-            }
+            if (set_tiles(cfg->N, cfg->precision, px, pz)) continue;
+            double t;
+            err = timed(t);
             if (err) break;
             if (t < best) {
                 best = t;
@@ -316,6 +380,15 @@ extern "C" int mitos_autotune(const struct ic_config *cfg, const struct perturb_
     if (best_pz) *best_pz = bz;
     if (best_ms) *best_ms = best;
     return 0;
+}
+
+extern "C" int mitos_set_radix(int N, int precision, const int *rad_n, int stages_n, const int *rad_h,
+                               int stages_h) {
+    return set_radix(N, precision, rad_n, stages_n, rad_h, stages_h);
+}
+extern "C" int mitos_get_radix(int N, int precision, int *rad_n, int *stages_n, int *rad_h, int *stages_h) {
+    if (!rad_n || !stages_n || !rad_h || !stages_h) return 1;
+    return get_radix(N, precision, rad_n, stages_n, rad_h, stages_h);
 }
 
 extern "C" int mitos_set_tiles(int N, int precision, int p_xy, int p_z) { return set_tiles(N, precision, p_xy, p_z); }

@@ -15,7 +15,10 @@ MITOS_CT_DECL(512)
 MITOS_CT_DECL(1024)
 
 // pencils per block of the specialised X / Y kernels (512 threads of 8 elements)
-static inline bool ct_ok(const GridGeom &g, int N) { return g.N == N && g.E == 8 && g.P_xy == 512 / (N / 8); }
+// (a radix schedule set by set_radix runs on the runtime-plan kernels)
+static inline bool ct_ok(const GridGeom &g, int N) {
+    return g.N == N && g.E == 8 && g.P_xy == 512 / (N / 8) && !g.custom_radix;
+}
 
 template <typename T> int launch_x(const GridGeom &g, XOp op, int sign, const PassArgs &a) {
     if constexpr (sizeof(T) == 4) {

@@ -23,6 +23,7 @@ struct GridGeom {
     int P_xy;     // pencils per block in X/Y passes
     int P_z;      // rows per block in Z passes
     const void *twN;  // device table exp(-2 pi i m / N), m < N, in the grid precision
+    int custom_radix; // 1: radix schedules set by set_radix (the runtime-plan kernels run them)
 };
 
 const GridGeom *geom(int N, int precision);  // cached; NULL if N unsupported

@@ -131,7 +131,7 @@ EXPORTS = ["alloc_local_grid", "free_local_grid", "free_local_real_grid", "free_
            "ic_pipeline_run", "ic_pipeline_run_table", "mitos_timer_start", "mitos_timer_stop",
            "mitos_sync", "mitos_kernel_timing", "mitos_kernel_times", "mitos_stage_times",
            "mitos_ma_history", "mitos_rng_jump", "mitos_noise_column_state", "mitos_cr_log", "mitos_cr_cos",
-           "mitos_sample_norm_cr", "mitos_cr_steps", "snapshot_header_attributes", "manet_set_warm_grid"] + \
+           "mitos_sample_norm_cr", "mitos_cr_steps", "snapshot_header_attributes", "manet_set_warm_grid", "mitos_set_radix", "mitos_get_radix"] + \
           ["kernel_" + k for k in KERNEL_NAMES]
 
 
@@ -671,6 +671,20 @@ def autotune(cfg: ICConfig, spline: Spline) -> tuple:
 
 def set_tiles(N: int, precision: int, pxy: int, pz: int) -> None:
     _check(load().mitos_set_tiles(N, precision, pxy, pz))
+
+
+def set_radix(N: int, precision: int, rad_n, rad_h) -> None:
+    a = (ctypes.c_int * len(rad_n))(*rad_n)
+    b = (ctypes.c_int * len(rad_h))(*rad_h)
+    _check(load().mitos_set_radix(N, precision, a, len(rad_n), b, len(rad_h)))
+
+
+def get_radix(N: int, precision: int) -> tuple:
+    """(radices of the length-N transforms, radices of the length-N/2 transforms)"""
+    a, b = (ctypes.c_int * 12)(), (ctypes.c_int * 12)()
+    na, nb = ctypes.c_int(), ctypes.c_int()
+    _check(load().mitos_get_radix(N, precision, a, ctypes.byref(na), b, ctypes.byref(nb)))
+    return list(a[:na.value]), list(b[:nb.value])
 
 
 def get_tiles(N: int, precision: int) -> tuple:

@@ -74,13 +74,43 @@ def test_autotuner_keeps_results(table, spline):
     N, L = 64, 256.0
     cfg = ml.ic_config(N, N, L, 1000, table, method=ml.METHOD_2LPT, pk_bins=32, precision=ml.FP32)
     default = ml.get_tiles(N, ml.FP32)
+    default_radix = ml.get_radix(N, ml.FP32)
+    assert default_radix == ([8, 8], [8, 4])
     ref = ml.ic_pipeline_run(cfg, spline)
     try:
         pxy, pz, ms = ml.autotune(cfg, spline)
         assert ml.get_tiles(N, ml.FP32) == (pxy, pz) and ms > 0
+        rn, rh = ml.get_radix(N, ml.FP32)
+        assert np.prod(rn) == N and np.prod(rh) == N // 2
         got = ml.ic_pipeline_run(cfg, spline)
         assert np.allclose(got["pk_p"], ref["pk_p"], rtol=1e-5, equal_nan=True)
         with pytest.raises(ml.MitosError):
             ml.set_tiles(N, ml.FP32, 4096, 1)
     finally:
         ml.set_tiles(N, ml.FP32, *default)
+        ml.set_radix(N, ml.FP32, *default_radix)
+
+
+@pytest.mark.parametrize("N,prec,rn,rh", [(64, ml.FP32, [2, 4, 8], [4, 2, 4]), (96, ml.FP32, [3, 4, 4, 2], [2, 3, 4, 2]),
+                                          (64, ml.FP64, [4, 4, 4], [2, 2, 8]), (256, ml.FP32, [4, 8, 8], [8, 4, 4])])
+def test_radix_schedules_keep_results(table, spline, N, prec, rn, rh):
+    """every radix order computes the same transforms: the IC's P(k) and positions with a
+    non-default schedule (for 256^3 FP32 on the runtime-plan kernels instead of the compile-time
+    ones) against the default; a schedule whose product is not N is refused"""
+    L = 4.0 * N
+    cfg = ml.ic_config(N, N, L, 7, table, method=ml.METHOD_2LPT, pk_bins=16, precision=prec)
+    default_radix = ml.get_radix(N, prec)
+    ref = ml.ic_pipeline_run(cfg, spline, want_pos=True)
+    try:
+        ml.set_radix(N, prec, rn, rh)
+        assert ml.get_radix(N, prec) == (rn, rh)
+        got = ml.ic_pipeline_run(cfg, spline, want_pos=True)
+        tol = 1e-5 if prec == ml.FP32 else 1e-12
+        assert np.allclose(got["pk_p"], ref["pk_p"], rtol=tol, equal_nan=True)
+        d = got["pos"].astype(np.float64) - ref["pos"].astype(np.float64)
+        d -= L * np.round(d / L)
+        assert np.abs(d).max() < (1e-3 if prec == ml.FP32 else 1e-9) * L / N
+        with pytest.raises(ml.MitosError):
+            ml.set_radix(N, prec, rn + [2], rh)
+    finally:
+        ml.set_radix(N, prec, *default_radix)
