@@ -281,6 +281,7 @@ __global__ void __launch_bounds__(512, 2) k_x_combine_disp(GridGeom g, PassArgs 
 // keeps all six Hessian rows live
 template <typename T, int E, int OP, int NL>
 __global__ void __launch_bounds__(256, OP == ZOP_HESS_MA ? 1 : 2) k_z_c2r(GridGeom g, PassArgs a) {
+    constexpr bool S2 = OP == ZOP_HESS_2LPT || OP == ZOP_HESS_2LPT_K;  // the 2LPT source passes
     extern __shared__ __align__(16) unsigned char smraw[];
     cplx<T> *sm = reinterpret_cast<cplx<T> *>(smraw);
     const FFTPlan &pl = g.plH;
@@ -293,24 +294,24 @@ __global__ void __launch_bounds__(256, OP == ZOP_HESS_MA ? 1 : 2) k_z_c2r(GridGe
     const cplx<T> *tw = reinterpret_cast<const cplx<T> *>(g.twN);
     // the 2LPT source pass converts the double copies: its 128-register allocation then keeps the
     // transforms free of spills (measured at 512^3: 1.29 ms, against 1.42 with the FP32 copies)
-    const T dk = OP == ZOP_HESS_2LPT ? (T)a.dk : parg<T>(a.dk, a.fdk);
-    const T scale = OP == ZOP_HESS_2LPT ? (T)a.scale : parg<T>(a.scale, a.fscale);
+    const T dk = S2 ? (T)a.dk : parg<T>(a.dk, a.fdk);
+    const T scale = S2 ? (T)a.scale : parg<T>(a.scale, a.fscale);
     cplx<T> *psm = sm + (long)p * spad_len(h);
     const size_t bo = (size_t)blockIdx.y * (size_t)a.bstride;
 
     constexpr int NIN = (OP == ZOP_C2R) ? 1 : (OP == ZOP_DISP) ? 3 : 6;
     // inputs of the Hessian passes are [xx, xy, xz, yy, yz, zz]; the 2LPT source is accumulated
     // in the reference's term order (src/2lpt.c:111-112): zz yy + zz xx + yy xx - xy^2 - yz^2 - xz^2
-    constexpr int NKEEP = (OP == ZOP_HESS_MA) ? 6 : (OP == ZOP_HESS_2LPT) ? 2 : 1;
+    constexpr int NKEEP = (OP == ZOP_HESS_MA) ? 6 : S2 ? 2 : 1;
     cplx<T> o[NKEEP][E];
     cplx<T> acc[E];
     T *dst_row = nullptr;
 #pragma unroll
     for (int q = 0; q < NIN; q++) {
-        const int f = (OP == ZOP_HESS_2LPT) ? (q == 0 ? 0 : q == 1 ? 3 : q == 2 ? 5 : q == 3 ? 1 : q == 4 ? 4 : 2) : q;
+        const int f = S2 ? (q == 0 ? 0 : q == 1 ? 3 : q == 2 ? 5 : q == 3 ? 1 : q == 4 ? 4 : 2) : q;
         // kz factor of input f: 0 -> 1, 1 -> i kz, 2 -> -kz^2
         int fac = 0;
-        if (OP == ZOP_HESS_2LPT || OP == ZOP_HESS_MA) fac = (f == 2 || f == 4) ? 1 : (f == 5 ? 2 : 0);
+        if (S2 || OP == ZOP_HESS_MA) fac = (f == 2 || f == 4) ? 1 : (f == 5 ? 2 : 0);
         if (OP == ZOP_DISP) fac = (f == 2) ? 1 : 0;
         const cplx<T> *src = bat<const cplx<T>>(a.in[f], bo) + row * H;
         // the displacement pass starts the next field's row towards L2 while this one is transformed
@@ -356,7 +357,7 @@ __global__ void __launch_bounds__(256, OP == ZOP_HESS_MA ? 1 : 2) k_z_c2r(GridGe
                 }
                 if (t == 0 && a.rp_out > N) { dst[N] = 0; dst[N + 1] = 0; }
             }
-        } else if constexpr (OP == ZOP_HESS_2LPT) {
+        } else if constexpr (S2) {
 #pragma unroll
             for (int e = 0; e < E; e++) {
                 const cplx<T> x = cscale<T>(v[e], scale);
@@ -375,6 +376,36 @@ __global__ void __launch_bounds__(256, OP == ZOP_HESS_MA ? 1 : 2) k_z_c2r(GridGe
         }
     }
     (void)dst_row;
+    if constexpr (OP == ZOP_HESS_2LPT_K) {
+        // the r2c of the S row, as k_z_r2c does it from global memory: the row to the transform's
+        // input order through the row's exchange buffer, the N/2-point forward FFT, the split into
+        // N/2+1 modes.  Every thread takes part (the exchanges synchronise); invalid rows store nothing.
+#pragma unroll
+        for (int e = 0; e < E; e++) psm[xpos<NL, 1>(nout_any<NL, E>(pl, t, e))] = acc[e];
+        if constexpr (NL > 0) pencil_sync<NL, E, 1>();
+        else __syncthreads();
+        cplx<T> v[E];
+#pragma unroll
+        for (int e = 0; e < E; e++) v[e] = psm[xpos<NL, 1>(nin_any<NL, E>(pl, t, e))];
+        if constexpr (NL > 0) pencil_sync<NL, E, 1>();
+        else __syncthreads();
+        fft_any<T, E, -1, NL, 1>(pl, v, psm, 1, t, tw);
+#pragma unroll
+        for (int e = 0; e < E; e++) psm[xpos<NL, 1>(nout_any<NL, E>(pl, t, e))] = v[e];
+        if constexpr (NL > 0) pencil_sync<NL, E, 1>();
+        else __syncthreads();
+        if (!valid) return;
+        cplx<T> *dst = bat<cplx<T>>(a.out[0], bo) + row * H;
+        for (int k = t; k <= h; k += tpp) {
+            const cplx<T> Z = psm[xpos<NL, 1>(k == h ? 0 : k)];
+            const cplx<T> Zc = psm[xpos<NL, 1>(k == 0 ? 0 : h - k)];
+            const cplx<T> ev = mk<T>((T)0.5 * (Z.x + Zc.x), (T)0.5 * (Z.y - Zc.y));
+            const cplx<T> od = mk<T>((T)0.5 * (Z.y + Zc.y), (T)-0.5 * (Z.x - Zc.x));
+            const cplx<T> w = __ldg(tw + k);
+            dst[k] = cadd<T>(ev, cmul<T>(od, w));
+        }
+        return;
+    }
     if (!valid) return;
     if constexpr (OP == ZOP_HESS_2LPT) {
         T *dst = bat<T>(a.out[0], bo) + row * a.rp_out;
@@ -573,7 +604,8 @@ static int launch_zc_e(const GridGeom &g, const PassArgs &a) {
     const long rows = (long)g.N * g.N;
     auto kern = k_z_c2r<T, E, OP, NLZ>;
     if (smem > 48 * 1024) MITOS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    launch_begin(OP == ZOP_C2R ? "z_c2r" : OP == ZOP_HESS_2LPT ? "z_hess_2lpt" : OP == ZOP_HESS_MA ? "z_hess_ma" : "z_disp");
+    launch_begin(OP == ZOP_C2R ? "z_c2r" : OP == ZOP_HESS_2LPT ? "z_hess_2lpt" : OP == ZOP_HESS_2LPT_K ? "z_hess_2lpt_r2c"
+                 : OP == ZOP_HESS_MA ? "z_hess_ma" : "z_disp");
     kern<<<dim3((unsigned)((rows + P - 1) / P), a.batch > 1 ? a.batch : 1), threads, smem, stream()>>>(g, with_f32(a));
     count_launch();
     MITOS_LAUNCH_CHECK("z c2r pass");
@@ -588,6 +620,7 @@ int launch_zc_t(const GridGeom &g, ZOp op, const PassArgs &a) {
         case ZOP_HESS_2LPT: return launch_zc_e<T, 8, ZOP_HESS_2LPT, NLZ>(g, a);
         case ZOP_HESS_MA: return launch_zc_e<T, 8, ZOP_HESS_MA, NLZ>(g, a);
         case ZOP_DISP: return launch_zc_e<T, 8, ZOP_DISP, NLZ>(g, a);
+        case ZOP_HESS_2LPT_K: return launch_zc_e<T, 8, ZOP_HESS_2LPT_K, NLZ>(g, a);
         }
     } else {
         switch (op) {
@@ -595,6 +628,7 @@ int launch_zc_t(const GridGeom &g, ZOp op, const PassArgs &a) {
         case ZOP_HESS_2LPT: return launch_zc_e<T, 12, ZOP_HESS_2LPT, 0>(g, a);
         case ZOP_HESS_MA: return launch_zc_e<T, 12, ZOP_HESS_MA, 0>(g, a);
         case ZOP_DISP: return launch_zc_e<T, 12, ZOP_DISP, 0>(g, a);
+        case ZOP_HESS_2LPT_K: return launch_zc_e<T, 12, ZOP_HESS_2LPT_K, 0>(g, a);
         }
     }
     return 3;

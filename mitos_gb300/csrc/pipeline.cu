@@ -3,8 +3,8 @@
 // Stage order (src/mitos.c:205-422,794-863,1072-1077 then analyse/src/mitos_read.c:278-419), with
 // the reference's redundant c2r -> r2c round trips removed (exact in exact arithmetic):
 //   S1  noise x sqrt(P_prim) x T(k, tau_src) x rescale x (-1/k^2)  -> phi1(k)   [+ Hermitian planes]
-//   S2  six Hessians of phi1 (X, Y, Z passes) with the 2LPT source fused into the Z pass -> S(x)
-//   S3  S r2c; the last X pass forms phi = f1 phi1 - f2 S/k^2 and undoes the TSC window
+//   S2  six Hessians of phi1 (X, Y, Z passes) with the 2LPT source and its z r2c fused into the Z pass
+//   S3  the Y and X steps of the S r2c; the X pass forms phi = f1 phi1 - f2 S/k^2 and undoes the TSC window
 //       (Monge-Ampere: S2/S3 iterate residual -> phi += -res/k^2 until the tolerance)
 //   S4  three displacement grids (X, Y, Z passes)
 //   S5  lattice + TSC displacement + wrap + CIC deposit
@@ -293,21 +293,18 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     int iters = 0;
     double last_rel = 0;
     if (cfg->method == MITOS_METHOD_2LPT) {
-        // S2: Hessians + source
-        e = grid_hessian(g, prec, L, phi, ZOP_HESS_2LPT, nullptr, S, nullptr, 0, nullptr, B, bs);
+        // S2: Hessians + source, and the source's r2c along z in the same Z pass
+        e = grid_hessian(g, prec, L, phi, ZOP_HESS_2LPT_K, nullptr, Sk, nullptr, 0, nullptr, B, bs);
         if (e) return e;
         tim.mark();
-        // S3: S r2c -> phi = f1 phi1 + f2 (-1/k^2) S, TSC window undone (src/2lpt.c:125-136)
+        // S3: the rest of the S r2c -> phi = f1 phi1 + f2 (-1/k^2) S, TSC window undone
+        // (src/2lpt.c:125-136)
         reset(a);
         a.dk = dk;
         a.scale = 1.0;
-        a.in[0] = S;
-        a.out[0] = Sk;
-        a.rp_in = N + 2;
-        a.rho_a = 1.0;
-        e = launch_z_r2c<T>(g, a);
         a.in[0] = Sk;
-        if (!e) e = launch_y<T>(g, YOP_PLAIN, -1, a);
+        a.out[0] = Sk;
+        e = launch_y<T>(g, YOP_PLAIN, -1, a);
         a.in2 = phi;
         a.scale = V / ((double)N * N * N);
         a.f1 = 1.0;
@@ -457,18 +454,14 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
         if (!e) e = hermitian_planes(g, prec, phi);
         if (e) return e;
         if (cfg->method == MITOS_METHOD_2LPT) {
-            e = grid_hessian(g, prec, L, phi, ZOP_HESS_2LPT, nullptr, S, nullptr, 0);
+            e = grid_hessian(g, prec, L, phi, ZOP_HESS_2LPT_K, nullptr, Sk, nullptr, 0);
             if (e) return e;
             reset(a);
             a.dk = dk;
             a.scale = 1.0;
-            a.in[0] = S;
-            a.out[0] = Sk;
-            a.rp_in = N + 2;
-            a.rho_a = 1.0;
-            e = launch_z_r2c<T>(g, a);
             a.in[0] = Sk;
-            if (!e) e = launch_y<T>(g, YOP_PLAIN, -1, a);
+            a.out[0] = Sk;
+            e = launch_y<T>(g, YOP_PLAIN, -1, a);
             a.in2 = phi;
             a.scale = V / ((double)N * N * N);
             a.f1 = F1_VEL;
