@@ -95,3 +95,12 @@ if __name__ == "__main__":
     N = int(sys.argv[2]) if len(sys.argv) > 2 else 256
     reps = int(sys.argv[3]) if len(sys.argv) > 3 else 3
     print(f"{name} N={N}: {CASES[name](N, reps):.4f} ms per repetition")
+    # the same workload once more with per-launch timing: device time per kernel name
+    ml.kernel_timing(True)
+    CASES[name](N, 1)
+    per = {}
+    for k, t in ml.kernel_times():
+        per.setdefault(k, []).append(t)
+    ml.kernel_timing(False)
+    for k, v in sorted(per.items(), key=lambda kv: -sum(kv[1])):
+        print(f"  {k:24s} {len(v):4d} launches  {sum(v):9.4f} ms")

@@ -280,8 +280,9 @@ __global__ void __launch_bounds__(512, 2) k_x_combine_disp(GridGeom g, PassArgs 
 // two 256-thread blocks per SM (<= 128 registers) except for the Monge-Ampere residual, which
 // keeps all six Hessian rows live
 template <typename T, int E, int OP, int NL>
-__global__ void __launch_bounds__(256, OP == ZOP_HESS_MA ? 1 : 2) k_z_c2r(GridGeom g, PassArgs a) {
+__global__ void __launch_bounds__(256, (OP == ZOP_HESS_MA || OP == ZOP_HESS_MA_K) ? 1 : 2) k_z_c2r(GridGeom g, PassArgs a) {
     constexpr bool S2 = OP == ZOP_HESS_2LPT || OP == ZOP_HESS_2LPT_K;  // the 2LPT source passes
+    constexpr bool MA = OP == ZOP_HESS_MA || OP == ZOP_HESS_MA_K;      // the Monge-Ampere residual passes
     extern __shared__ __align__(16) unsigned char smraw[];
     cplx<T> *sm = reinterpret_cast<cplx<T> *>(smraw);
     const FFTPlan &pl = g.plH;
@@ -302,7 +303,7 @@ __global__ void __launch_bounds__(256, OP == ZOP_HESS_MA ? 1 : 2) k_z_c2r(GridGe
     constexpr int NIN = (OP == ZOP_C2R) ? 1 : (OP == ZOP_DISP) ? 3 : 6;
     // inputs of the Hessian passes are [xx, xy, xz, yy, yz, zz]; the 2LPT source is accumulated
     // in the reference's term order (src/2lpt.c:111-112): zz yy + zz xx + yy xx - xy^2 - yz^2 - xz^2
-    constexpr int NKEEP = (OP == ZOP_HESS_MA) ? 6 : S2 ? 2 : 1;
+    constexpr int NKEEP = MA ? 6 : S2 ? 2 : 1;
     cplx<T> o[NKEEP][E];
     cplx<T> acc[E];
     T *dst_row = nullptr;
@@ -311,7 +312,7 @@ __global__ void __launch_bounds__(256, OP == ZOP_HESS_MA ? 1 : 2) k_z_c2r(GridGe
         const int f = S2 ? (q == 0 ? 0 : q == 1 ? 3 : q == 2 ? 5 : q == 3 ? 1 : q == 4 ? 4 : 2) : q;
         // kz factor of input f: 0 -> 1, 1 -> i kz, 2 -> -kz^2
         int fac = 0;
-        if (S2 || OP == ZOP_HESS_MA) fac = (f == 2 || f == 4) ? 1 : (f == 5 ? 2 : 0);
+        if (S2 || MA) fac = (f == 2 || f == 4) ? 1 : (f == 5 ? 2 : 0);
         if (OP == ZOP_DISP) fac = (f == 2) ? 1 : 0;
         const cplx<T> *src = bat<const cplx<T>>(a.in[f], bo) + row * H;
         // the displacement pass starts the next field's row towards L2 while this one is transformed
@@ -406,7 +407,9 @@ __global__ void __launch_bounds__(256, OP == ZOP_HESS_MA ? 1 : 2) k_z_c2r(GridGe
         }
         return;
     }
-    if (!valid) return;
+    // (the residual passes keep every thread to the end: their reductions and exchanges need the
+    // whole warp and block)
+    if (!valid && !MA) return;
     if constexpr (OP == ZOP_HESS_2LPT) {
         T *dst = bat<T>(a.out[0], bo) + row * a.rp_out;
 #pragma unroll
@@ -417,10 +420,13 @@ __global__ void __launch_bounds__(256, OP == ZOP_HESS_MA ? 1 : 2) k_z_c2r(GridGe
         if (t == 0 && a.rp_out > N) { dst[N] = 0; dst[N + 1] = 0; }
         return;
     }
-    if constexpr (OP == ZOP_HESS_MA) {
+    if constexpr (MA) {
+        // the residual per element (valid rows: the FP64 sums; invalid rows compute on row 0 and
+        // add nothing), stored, or kept for the r2c of ZOP_HESS_MA_K
         T *dst = bat<T>(a.out[0], bo) + row * a.rp_out;
         double sres = 0, srho = 0;
-        const T *rho = (OP == ZOP_HESS_MA) ? bat<const T>(a.in2, bo) + row * a.rp_in : nullptr;
+        const T *rho = bat<const T>(a.in2, bo) + row * a.rp_in;
+        cplx<T> resv[E];
 #pragma unroll
         for (int e = 0; e < E; e++) {
             const int n = nout_any<NL, E>(pl, t, e);
@@ -436,31 +442,59 @@ __global__ void __launch_bounds__(256, OP == ZOP_HESS_MA ? 1 : 2) k_z_c2r(GridGe
                 // second invariant of the Hessian (src/2lpt.c:111-112)
                 const T s2 = zz * yy + zz * xx + yy * xx - xy * xy - yz * yz - xz * xz;
                 s2v[c] = s2;
-                if constexpr (OP == ZOP_HESS_2LPT) {
-                    res2[c] = s2;
-                } else {
-                    // (1 + rho) - det(I + H) = (rho - tr H) - s2 - det H  (src/monge_ampere.c:119-145)
-                    const T d3 = xx * (yy * zz - yz * yz) - xy * (xy * zz - yz * xz) + xz * (xy * yz - yy * xz);
-                    const T r = rho[2 * n + c];
-                    const T res = ((r - xx) - yy - zz) - s2 - d3;
-                    res2[c] = res;
-                    sres += (double)res * (double)res;
-                    srho += (double)r * (double)r;
-                }
+                // (1 + rho) - det(I + H) = (rho - tr H) - s2 - det H  (src/monge_ampere.c:119-145)
+                const T d3 = xx * (yy * zz - yz * yz) - xy * (xy * zz - yz * xz) + xz * (xy * yz - yy * xz);
+                const T r = rho[2 * n + c];
+                const T res = ((r - xx) - yy - zz) - s2 - d3;
+                res2[c] = res;
+                sres += (double)res * (double)res;
+                srho += (double)r * (double)r;
             }
-            *reinterpret_cast<cplx<T> *>(dst + 2 * n) = mk<T>(res2[0], res2[1]);
+            resv[e] = mk<T>(res2[0], res2[1]);
+            if constexpr (OP == ZOP_HESS_MA) {
+                if (valid) *reinterpret_cast<cplx<T> *>(dst + 2 * n) = resv[e];
+            }
             // optional second output: the second-order source S of the same Hessian
-            if (a.out[1]) *reinterpret_cast<cplx<T> *>(bat<T>(a.out[1], bo) + row * a.rp_out + 2 * n) = mk<T>(s2v[0], s2v[1]);
+            if (valid && a.out[1])
+                *reinterpret_cast<cplx<T> *>(bat<T>(a.out[1], bo) + row * a.rp_out + 2 * n) = mk<T>(s2v[0], s2v[1]);
         }
-        if (t == 0 && a.rp_out > N) { dst[N] = 0; dst[N + 1] = 0; }
         if constexpr (OP == ZOP_HESS_MA) {
-            for (int off = 16; off > 0; off >>= 1) {
-                sres += __shfl_down_sync(0xffffffffu, sres, off);
-                srho += __shfl_down_sync(0xffffffffu, srho, off);
-            }
-            if ((threadIdx.x & 31) == 0) {
-                atomicAdd(a.red + (size_t)blockIdx.y * a.acc_stride + 0, sres);
-                atomicAdd(a.red + (size_t)blockIdx.y * a.acc_stride + 1, srho);
+            if (valid && t == 0 && a.rp_out > N) { dst[N] = 0; dst[N + 1] = 0; }
+        }
+        if (!valid) { sres = 0; srho = 0; }
+        for (int off = 16; off > 0; off >>= 1) {
+            sres += __shfl_down_sync(0xffffffffu, sres, off);
+            srho += __shfl_down_sync(0xffffffffu, srho, off);
+        }
+        if ((threadIdx.x & 31) == 0) {
+            atomicAdd(a.red + (size_t)blockIdx.y * a.acc_stride + 0, sres);
+            atomicAdd(a.red + (size_t)blockIdx.y * a.acc_stride + 1, srho);
+        }
+        if constexpr (OP == ZOP_HESS_MA_K) {
+            // the residual row's r2c along z (as in ZOP_HESS_2LPT_K)
+#pragma unroll
+            for (int e = 0; e < E; e++) psm[xpos<NL, 1>(nout_any<NL, E>(pl, t, e))] = resv[e];
+            if constexpr (NL > 0) pencil_sync<NL, E, 1>();
+            else __syncthreads();
+            cplx<T> v[E];
+#pragma unroll
+            for (int e = 0; e < E; e++) v[e] = psm[xpos<NL, 1>(nin_any<NL, E>(pl, t, e))];
+            if constexpr (NL > 0) pencil_sync<NL, E, 1>();
+            else __syncthreads();
+            fft_any<T, E, -1, NL, 1>(pl, v, psm, 1, t, tw);
+#pragma unroll
+            for (int e = 0; e < E; e++) psm[xpos<NL, 1>(nout_any<NL, E>(pl, t, e))] = v[e];
+            if constexpr (NL > 0) pencil_sync<NL, E, 1>();
+            else __syncthreads();
+            if (!valid) return;
+            cplx<T> *dk_row = bat<cplx<T>>(a.out[0], bo) + row * H;
+            for (int k = t; k <= h; k += tpp) {
+                const cplx<T> Z = psm[xpos<NL, 1>(k == h ? 0 : k)];
+                const cplx<T> Zc = psm[xpos<NL, 1>(k == 0 ? 0 : h - k)];
+                const cplx<T> ev = mk<T>((T)0.5 * (Z.x + Zc.x), (T)0.5 * (Z.y - Zc.y));
+                const cplx<T> od = mk<T>((T)0.5 * (Z.y + Zc.y), (T)-0.5 * (Z.x - Zc.x));
+                const cplx<T> w = __ldg(tw + k);
+                dk_row[k] = cadd<T>(ev, cmul<T>(od, w));
             }
         }
     }
@@ -605,7 +639,7 @@ static int launch_zc_e(const GridGeom &g, const PassArgs &a) {
     auto kern = k_z_c2r<T, E, OP, NLZ>;
     if (smem > 48 * 1024) MITOS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     launch_begin(OP == ZOP_C2R ? "z_c2r" : OP == ZOP_HESS_2LPT ? "z_hess_2lpt" : OP == ZOP_HESS_2LPT_K ? "z_hess_2lpt_r2c"
-                 : OP == ZOP_HESS_MA ? "z_hess_ma" : "z_disp");
+                 : OP == ZOP_HESS_MA ? "z_hess_ma" : OP == ZOP_HESS_MA_K ? "z_hess_ma_r2c" : "z_disp");
     kern<<<dim3((unsigned)((rows + P - 1) / P), a.batch > 1 ? a.batch : 1), threads, smem, stream()>>>(g, with_f32(a));
     count_launch();
     MITOS_LAUNCH_CHECK("z c2r pass");
@@ -621,6 +655,7 @@ int launch_zc_t(const GridGeom &g, ZOp op, const PassArgs &a) {
         case ZOP_HESS_MA: return launch_zc_e<T, 8, ZOP_HESS_MA, NLZ>(g, a);
         case ZOP_DISP: return launch_zc_e<T, 8, ZOP_DISP, NLZ>(g, a);
         case ZOP_HESS_2LPT_K: return launch_zc_e<T, 8, ZOP_HESS_2LPT_K, NLZ>(g, a);
+        case ZOP_HESS_MA_K: return launch_zc_e<T, 8, ZOP_HESS_MA_K, NLZ>(g, a);
         }
     } else {
         switch (op) {
@@ -629,6 +664,7 @@ int launch_zc_t(const GridGeom &g, ZOp op, const PassArgs &a) {
         case ZOP_HESS_MA: return launch_zc_e<T, 12, ZOP_HESS_MA, 0>(g, a);
         case ZOP_DISP: return launch_zc_e<T, 12, ZOP_DISP, 0>(g, a);
         case ZOP_HESS_2LPT_K: return launch_zc_e<T, 12, ZOP_HESS_2LPT_K, 0>(g, a);
+        case ZOP_HESS_MA_K: return launch_zc_e<T, 12, ZOP_HESS_MA_K, 0>(g, a);
         }
     }
     return 3;

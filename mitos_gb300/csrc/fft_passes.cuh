@@ -53,9 +53,11 @@ enum ZOp {
     ZOP_HESS_MA,      // same 6 in -> residual (1 + rho) - det(I + H), sums of res^2 and rho^2;
                       // out[1] (optional): the second-order source S of the same Hessian
     ZOP_DISP,         // 3 in (kz factors 1, 1, i kz) -> 3 real out
-    ZOP_HESS_2LPT_K   // ZOP_HESS_2LPT followed by the r2c of S along z in the same pass: out[0] is
+    ZOP_HESS_2LPT_K,  // ZOP_HESS_2LPT followed by the r2c of S along z in the same pass: out[0] is
                       // the complex z-transformed source (N/2+1 per row, unnormalised), as
                       // ZOP_HESS_2LPT + a z r2c with scale 1 would leave it
+    ZOP_HESS_MA_K     // ZOP_HESS_MA with the residual's r2c along z in the same pass (out[0] complex,
+                      // as above; out[1], the optional source, stays real)
 };
 
 struct PassArgs {

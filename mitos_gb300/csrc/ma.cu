@@ -147,6 +147,23 @@ static int warm_coarse(const GridGeom &g, int Ns, double L, struct manet *net, c
     return e;
 }
 
+// phi(k) += G(k) r2c(src)(k) for a source whose z r2c the Z pass already made (Sk: complex, the Y
+// and X steps remain)
+static int add_poisson_zk(const GridGeom &g, int prec, double boxlen, void *Sk, void *phi) {
+    PassArgs a;
+    memset(&a, 0, sizeof a);
+    a.dk = 2 * M_PI / boxlen;
+    a.scale = 1.0;
+    a.in[0] = Sk;
+    a.out[0] = Sk;
+    int e = prec == MITOS_FP32 ? launch_y<float>(g, YOP_PLAIN, -1, a) : launch_y<double>(g, YOP_PLAIN, -1, a);
+    if (e) return e;
+    a.in2 = phi;
+    a.out[0] = phi;
+    a.scale = boxlen * boxlen * boxlen / ((double)g.N * g.N * g.N);
+    return prec == MITOS_FP32 ? launch_x<float>(g, XOP_ADD_POISSON, -1, a) : launch_x<double>(g, XOP_ADD_POISSON, -1, a);
+}
+
 // phi(k) += G(k) r2c(src)(k): src real (pitch N + 2); Sk complex scratch
 static int add_poisson(const GridGeom &g, int prec, double boxlen, const void *src, void *phi, void *Sk) {
     PassArgs a;
@@ -227,7 +244,8 @@ static int ma_run(struct distributed_grid *pot, struct distributed_grid *dens, s
     for (int it = 0; !e; it++) {
         MITOS_CUDA(cudaMemsetAsync(red, 0, 2 * sizeof(double), stream()));
         const bool want_S = it == 0 && (warm || cap);
-        e = grid_hessian(g, prec, L, pot->fbox, ZOP_HESS_MA, dens->box, work->box, red, 0, want_S ? S : nullptr);
+        // the residual leaves the Z pass already transformed along z (into Sk)
+        e = grid_hessian(g, prec, L, pot->fbox, ZOP_HESS_MA_K, dens->box, Sk, red, 0, want_S ? S : nullptr);
         if (e) break;
         double h[2];
         MITOS_CUDA(cudaMemcpyAsync(h, red, sizeof h, cudaMemcpyDeviceToHost, stream()));
@@ -243,7 +261,7 @@ static int ma_run(struct distributed_grid *pot, struct distributed_grid *dens, s
             if (!cap) status = 7;
             break;
         }
-        e = add_poisson(g, prec, L, work->box, pot->fbox, Sk);
+        e = add_poisson_zk(g, prec, L, Sk, pot->fbox);
         if (e) break;
         st->cycles++;
         const int Nw = warm && !cap ? manet_warm_grid(warm) : 0;

@@ -334,18 +334,15 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
         const int maxc = cfg->ma_cycles > 0 ? cfg->ma_cycles : 1;
         for (int it = 0; it < maxc; it++) {
             MITOS_CUDA(cudaMemsetAsync(red, 0, 2 * sizeof(double), stream()));
-            e = grid_hessian(g, prec, L, phi, ZOP_HESS_MA, rhoR, S, red, 0);
+            // the residual with its z r2c in the Z pass (into Sk), then the Y and X steps
+            e = grid_hessian(g, prec, L, phi, ZOP_HESS_MA_K, rhoR, Sk, red, 0);
             if (e) return e;
             reset(a);
             a.dk = dk;
             a.scale = 1.0;
-            a.in[0] = S;
-            a.out[0] = Sk;
-            a.rp_in = N + 2;
-            a.rho_a = 1.0;
-            e = launch_z_r2c<T>(g, a);
             a.in[0] = Sk;
-            if (!e) e = launch_y<T>(g, YOP_PLAIN, -1, a);
+            a.out[0] = Sk;
+            e = launch_y<T>(g, YOP_PLAIN, -1, a);
             a.in2 = phi;
             a.out[0] = phi;
             a.scale = V / ((double)N * N * N);
