@@ -4,7 +4,7 @@ whose grids still exceed L2 but whose device footprint stays at a few GB:
     python -m mitos_gb300.cases conv 256     # network inference (k_conv), 4 layers
     python -m mitos_gb300.cases ngenic 512   # the N-GenIC-like field (k_ngenic)
     python -m mitos_gb300.cases ma 256       # Monge-Ampere cycles (z_hess_ma, x_add_poisson)
-    python -m mitos_gb300.cases noise 512    # white noise (k_noise), FP32
+    python -m mitos_gb300.cases noise 512    # white noise (k_noise), FP32 (noise64: FP64)
     python -m mitos_gb300.cases ic 256       # one FP32 initial condition (every pass)
 
 Each runs its workload `reps` times (third argument, default 3) after one warm-up and prints the
@@ -66,8 +66,8 @@ def ma(N: int, reps: int) -> float:
     return ms / reps
 
 
-def noise(N: int, reps: int) -> float:
-    g = ml.alloc_local_grid(N, 2.0 * N, ml.FP32)
+def noise(N: int, reps: int, prec: int = ml.FP32) -> float:
+    g = ml.alloc_local_grid(N, 2.0 * N, prec)
     ml.generate_complex_grf(g, ml.rng_init(1))
     ml.timer_start()
     for r in range(reps):
@@ -88,7 +88,11 @@ def ic(N: int, reps: int) -> float:
     return ml.timer_stop() / reps
 
 
-CASES = {"conv": conv, "ngenic": ngenic, "ma": ma, "noise": noise, "ic": ic}
+def noise64(N: int, reps: int) -> float:
+    return noise(N, reps, ml.FP64)
+
+
+CASES = {"conv": conv, "ngenic": ngenic, "ma": ma, "noise": noise, "noise64": noise64, "ic": ic}
 
 if __name__ == "__main__":
     name = sys.argv[1]
