@@ -610,6 +610,21 @@ def main():
         k_, p_, o_ = np.zeros(bins), np.zeros(bins), np.zeros(bins, np.int64)
         outs.append((k_, p_, o_, ml.ICResult(k_.ctypes.data_as(ml._dp), p_.ctypes.data_as(ml._dp),
                                              o_.ctypes.data_as(ml._lp), pos_ptrs[i % 2], 0, 0.0)))
+    # the host link's device-to-host rate into the same pinned buffer (one 1.6 GB copy, best of 3;
+    # e2e is bound by it once the kernels take less than a copy)
+    link = []
+    dsrc = torch.empty((npart, 3), dtype=torch.float32, device="cuda")
+    cs = torch.cuda.Stream()
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(cs)
+        with torch.cuda.stream(cs):
+            pinned[0].copy_(dsrc, non_blocking=True)
+        e1.record(cs)
+        cs.synchronize()
+        link.append(npart * 12 / (e0.elapsed_time(e1) / 1e3) / 1e9)
+    del dsrc
+    link_gbps = max(link)
     # warm-up: one submission into each pinned buffer (their first transfers are slow)
     warm = [(np.zeros(bins), np.zeros(bins), np.zeros(bins, np.int64)) for _ in range(2)]
     for j, (k_, p_, o_) in enumerate(warm):
@@ -659,7 +674,8 @@ def main():
             "data": "synthetic (xoshiro256** white noise, BBKS transfer table)", "config": config(args),
             "gpu_launches": int(launches),
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 3 * table.k_size * 8,
-                    "d2h_bytes_per_step": npart * 12 + 3 * bins * 8},
+                    "d2h_bytes_per_step": npart * 12 + 3 * bins * 8, "link_d2h_GBps": link_gbps,
+                    "link_bound_IC_per_s": link_gbps * 1e9 / (npart * 12)},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                          "traffic": traffic, "algorithmic_bytes": algorithmic_bytes(dom, G),

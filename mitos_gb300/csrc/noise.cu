@@ -259,18 +259,30 @@ void release_jump_tables() {
 // state.  (Two consecutive columns a thread, the second continuing the first's stream without a
 // jump, measured slower at 512^3: 0.678 against 0.660 ms, with half the warps to hide the
 // xoshiro dependency chains.)  Values are staged per chunk of z and written as rows.
+// A^i s0 (i < 256) of each realisation's start state, once per launch: the table every block of
+// k_noise reads (a single thread stepping 256 times in each block left the block's other threads
+// waiting at its barrier)
+__global__ void k_state_tables(RngState s0, const RngState *__restrict__ states, int nb, ulonglong4 *__restrict__ tab) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    const RngState s = states ? states[b] : s0;
+    uint64_t a0 = s.s[0], a1 = s.s[1], a2 = s.s[2], a3 = s.s[3];
+    for (int i = 0; i < 256; i++) {
+        tab[(size_t)b * 256 + i] = make_ulonglong4(a0, a1, a2, a3);
+        dnext(a0, a1, a2, a3);
+    }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(NOISE_THREADS)
-k_noise(int N, const uint64_t *__restrict__ polys, RngState s0, T factor, const T *__restrict__ filt,
-        cplx<T> *__restrict__ out, const RngState *__restrict__ states, size_t ostride) {
-    // batched launches: realisation blockIdx.y has its own start state and output grid
-    if (states) {
-        s0 = states[blockIdx.y];
-        out = bat<cplx<T>>(out, (size_t)blockIdx.y * ostride);
-    }
+k_noise(int N, const uint64_t *__restrict__ polys, const ulonglong4 *__restrict__ gtab, T factor,
+        const T *__restrict__ filt, cplx<T> *__restrict__ out, size_t ostride) {
+    // batched launches: realisation blockIdx.y has its own state table and output grid
+    out = bat<cplx<T>>(out, (size_t)blockIdx.y * ostride);
     __shared__ cplx<T> stage[NOISE_THREADS][NOISE_CHUNK + 1];
     __shared__ ulonglong4 tab[256];
-    noise_state_table(s0, tab);
+    for (int i = threadIdx.x; i < 256; i += NOISE_THREADS) tab[i] = gtab[(size_t)blockIdx.y * 256 + i];
+    __syncthreads();
     const int H = N / 2 + 1;
     const long ncol = (long)N * N;
     const long cblock = (long)blockIdx.x * NOISE_THREADS;  // first column of the block
@@ -363,13 +375,20 @@ int noise_generate(const GridGeom &g, int precision, double boxlen, uint64_t st[
     const unsigned blocks = (unsigned)((ncol + NOISE_THREADS - 1) / NOISE_THREADS);
     const dim3 grid(blocks, nb);
     const RngState *sts = (const RngState *)states;
+    ulonglong4 *tab = (ulonglong4 *)workspace(sizeof(ulonglong4) * 256 * (size_t)nb, 160);
+    if (!tab) return 5;
+    launch_begin("state_tables");
+    k_state_tables<<<(nb + 31) / 32, 32, 0, stream()>>>(s0, sts, nb, tab);
+    count_launch();
+    MITOS_LAUNCH_CHECK("noise state tables");
+    const size_t ost = sts ? bstride : 0;
     launch_begin("noise");
     if (precision == MITOS_FP32) {
-        k_noise<float><<<grid, NOISE_THREADS, 0, stream()>>>(g.N, polys, s0, (float)factor, (const float *)filter_by_n2,
-                                                   (float2 *)fbox, sts, bstride);
+        k_noise<float><<<grid, NOISE_THREADS, 0, stream()>>>(g.N, polys, tab, (float)factor, (const float *)filter_by_n2,
+                                                             (float2 *)fbox, ost);
     } else {
-        k_noise<double><<<grid, NOISE_THREADS, 0, stream()>>>(g.N, polys, s0, factor, (const double *)filter_by_n2,
-                                                   (double2 *)fbox, sts, bstride);
+        k_noise<double><<<grid, NOISE_THREADS, 0, stream()>>>(g.N, polys, tab, factor, (const double *)filter_by_n2,
+                                                              (double2 *)fbox, ost);
     }
     count_launch();
     MITOS_LAUNCH_CHECK("noise");
