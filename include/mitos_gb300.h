@@ -543,6 +543,14 @@ int mitos_get_tiles(int N, int precision, int *p_xy, int *p_z);
  * arrays of at least 12 ints. */
 int mitos_set_radix(int N, int precision, const int *rad_n, int stages_n, const int *rad_h, int stages_h);
 int mitos_get_radix(int N, int precision, int *rad_n, int *stages_n, int *rad_h, int *stages_h);
+/* The r2c's Z and Y steps in one thread-block-cluster pass (the x-plane held in the cluster's
+ * distributed shared memory), for FP32 N = 256 and 512 where the device fits the cluster.  mode 0
+ * (the default): off, the Z r2c and Y passes; 1: clusters of 16 CTAs of 512 threads (N = 256: 8),
+ * two column buffers; 2: 16 CTAs of 256 threads (N = 256: 8), one buffer; 3: 8 CTAs of 512 threads
+ * (N = 256: 4), one buffer.  Other values turn it off.  Returns the previous mode.  No reference
+ * counterpart (a switch of this library's FFT; fft_r2c_dg, src/fft.c:219-236, is the transform
+ * either way). */
+int mitos_set_cluster_fft(int mode);
 
 #ifdef __cplusplus
 }

@@ -6,6 +6,8 @@ whose grids still exceed L2 but whose device footprint stays at a few GB:
     python -m mitos_gb300.cases ma 256       # Monge-Ampere cycles (z_hess_ma, x_add_poisson)
     python -m mitos_gb300.cases noise 512    # white noise (k_noise), FP32 (noise64: FP64)
     python -m mitos_gb300.cases ic 256       # one FP32 initial condition (every pass)
+    python -m mitos_gb300.cases r2c 512 3 2  # fft_r2c_dg, FP32; fourth argument: the cluster mode
+                                             # of the Z + Y step (mitos_set_cluster_fft; 0 = off)
 
 Each runs its workload `reps` times (third argument, default 3) after one warm-up and prints the
 device time per repetition (CUDA events on the library stream).
@@ -88,16 +90,30 @@ def ic(N: int, reps: int) -> float:
     return ml.timer_stop() / reps
 
 
+def r2c(N: int, reps: int) -> float:
+    g = ml.alloc_local_grid(N, 2.0 * N, ml.FP32)
+    ml.set_box(g, np.random.default_rng(1).standard_normal((N, N, N + 2)).astype(np.float32))
+    ml.fft_r2c_dg(g)
+    ml.timer_start()
+    for _ in range(reps):
+        ml.fft_r2c_dg(g)
+    ms = ml.timer_stop() / reps
+    ml.free_local_grid(g)
+    return ms
+
+
 def noise64(N: int, reps: int) -> float:
     return noise(N, reps, ml.FP64)
 
 
-CASES = {"conv": conv, "ngenic": ngenic, "ma": ma, "noise": noise, "noise64": noise64, "ic": ic}
+CASES = {"conv": conv, "ngenic": ngenic, "ma": ma, "noise": noise, "noise64": noise64, "ic": ic, "r2c": r2c}
 
 if __name__ == "__main__":
     name = sys.argv[1]
     N = int(sys.argv[2]) if len(sys.argv) > 2 else 256
     reps = int(sys.argv[3]) if len(sys.argv) > 3 else 3
+    if len(sys.argv) > 4:
+        ml.set_cluster_fft(int(sys.argv[4]))
     print(f"{name} N={N}: {CASES[name](N, reps):.4f} ms per repetition")
     # the same workload once more with per-launch timing: device time per kernel name
     ml.kernel_timing(True)

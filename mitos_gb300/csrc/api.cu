@@ -52,6 +52,18 @@ int grid_c2r(const GridGeom &g, int prec, double boxlen, void *fbox, void *box) 
     return prec == MITOS_FP32 ? launch_z_c2r<float>(g, ZOP_C2R, a) : launch_z_c2r<double>(g, ZOP_C2R, a);
 }
 
+// the Z and Y steps of an r2c from a.in[0] (real, pitch a.rp_in) into a.out[0]: one cluster pass
+// where it applies (fft_cluster.cu), else the Z r2c pass and the in-place Y pass
+int grid_r2c_zy(const GridGeom &g, int prec, const PassArgs &a) {
+    int e = launch_zy_r2c(g, prec, a);
+    if (e != -1) return e;
+    e = prec == MITOS_FP32 ? launch_z_r2c<float>(g, a) : launch_z_r2c<double>(g, a);
+    if (e) return e;
+    PassArgs b = a;
+    b.in[0] = a.out[0];
+    return prec == MITOS_FP32 ? launch_y<float>(g, YOP_PLAIN, -1, b) : launch_y<double>(g, YOP_PLAIN, -1, b);
+}
+
 int grid_r2c(const GridGeom &g, int prec, double boxlen, const void *box, int rp, double rho_a,
              double rho_b, void *fbox) {
     PassArgs a;
@@ -63,11 +75,9 @@ int grid_r2c(const GridGeom &g, int prec, double boxlen, const void *box, int rp
     a.rp_in = rp;
     a.rho_a = rho_a;
     a.rho_b = rho_b;
-    int e = prec == MITOS_FP32 ? launch_z_r2c<float>(g, a) : launch_z_r2c<double>(g, a);
+    int e = grid_r2c_zy(g, prec, a);
     if (e) return e;
     a.in[0] = fbox;
-    e = prec == MITOS_FP32 ? launch_y<float>(g, YOP_PLAIN, -1, a) : launch_y<double>(g, YOP_PLAIN, -1, a);
-    if (e) return e;
     a.scale = boxlen * boxlen * boxlen / ((double)g.N * g.N * g.N);  // src/fft.c:91-106
     return prec == MITOS_FP32 ? launch_x<float>(g, XOP_PLAIN, -1, a) : launch_x<double>(g, XOP_PLAIN, -1, a);
 }
@@ -353,6 +363,12 @@ extern "C" int fft_c2r_dg(struct distributed_grid *dg) {
     if (e) return e;
     dg->momentum_space = 0;
     return sync_all();
+}
+
+extern "C" int mitos_set_cluster_fft(int mode) {
+    const int was = cluster_fft();
+    set_cluster_fft(mode >= 0 && mode <= 3 ? mode : 0);
+    return was;
 }
 
 extern "C" int fft_r2c_dg(struct distributed_grid *dg) {

@@ -277,12 +277,39 @@ __global__ void __launch_bounds__(512, 2) k_x_combine_disp(GridGeom g, PassArgs 
 // ------------------------------------------------------------------------------------------
 // Z c2r: rows of N/2+1 complex -> N reals via an N/2-point complex inverse FFT.
 // ------------------------------------------------------------------------------------------
-// two 256-thread blocks per SM (<= 128 registers) except for the Monge-Ampere residual, which
-// keeps all six Hessian rows live
+// one row of the lean Monge-Ampere residual (order xx, yy, zz, yz, xy, xz; see k_z_c2r): h the
+// row's value, o0..o2 the kept rows, R the sum
+template <typename T>
+__device__ __forceinline__ void ma_lean_step(int q, T h, T &o0, T &o1, T &o2, T &R) {
+    if (q == 0) {
+        o0 = h;  // xx
+    } else if (q == 1) {
+        o1 = h;  // yy
+    } else if (q == 2) {  // zz
+        const T xx = o0, yy = o1, zz = h;
+        R = -((xx + yy) + zz) - ((zz * yy + zz * xx) + yy * xx) - (xx * yy) * zz;
+        o0 = (T)1 + xx;
+        o1 = (T)1 + yy;
+        o2 = (T)1 + zz;
+    } else if (q == 3) {  // yz
+        R += h * h * o0;
+        o0 = h;
+    } else if (q == 4) {  // xy
+        R += h * h * o2;
+        o0 = h * o0;
+    } else {  // xz
+        R += h * h * o1 - (T)2 * o0 * h;
+    }
+}
+
+// two 256-thread blocks per SM (<= 128 registers) except for the Monge-Ampere residual passes with
+// the source output, which keep all six Hessian rows live
 template <typename T, int E, int OP, int NL>
-__global__ void __launch_bounds__(256, (OP == ZOP_HESS_MA || OP == ZOP_HESS_MA_K) ? 1 : 2) k_z_c2r(GridGeom g, PassArgs a) {
+__global__ void __launch_bounds__(256, (OP == ZOP_HESS_MA || OP == ZOP_HESS_MA_KS) ? 1 : 2) k_z_c2r(GridGeom g, PassArgs a) {
     constexpr bool S2 = OP == ZOP_HESS_2LPT || OP == ZOP_HESS_2LPT_K;  // the 2LPT source passes
-    constexpr bool MA = OP == ZOP_HESS_MA || OP == ZOP_HESS_MA_K;      // the Monge-Ampere residual passes
+    constexpr bool MA = OP == ZOP_HESS_MA || OP == ZOP_HESS_MA_K || OP == ZOP_HESS_MA_KS;  // residual passes
+    constexpr bool LEAN = OP == ZOP_HESS_MA_K;  // the residual accumulated as the rows arrive
+    constexpr bool MAK = OP == ZOP_HESS_MA_K || OP == ZOP_HESS_MA_KS;  // residual r2c along z in the pass
     extern __shared__ __align__(16) unsigned char smraw[];
     cplx<T> *sm = reinterpret_cast<cplx<T> *>(smraw);
     const FFTPlan &pl = g.plH;
@@ -302,14 +329,23 @@ __global__ void __launch_bounds__(256, (OP == ZOP_HESS_MA || OP == ZOP_HESS_MA_K
 
     constexpr int NIN = (OP == ZOP_C2R) ? 1 : (OP == ZOP_DISP) ? 3 : 6;
     // inputs of the Hessian passes are [xx, xy, xz, yy, yz, zz]; the 2LPT source is accumulated
-    // in the reference's term order (src/2lpt.c:111-112): zz yy + zz xx + yy xx - xy^2 - yz^2 - xz^2
-    constexpr int NKEEP = MA ? 6 : S2 ? 2 : 1;
+    // in the reference's term order (src/2lpt.c:111-112): zz yy + zz xx + yy xx - xy^2 - yz^2 - xz^2.
+    // The lean residual pass takes the rows in the order xx, yy, zz, yz, xy, xz and accumulates
+    // R = -tr H - s2(H) - det H (src/monge_ampere.c:119-145 expanded; residual = rho + R):
+    //   zz:  R = -((xx + yy) + zz) - ((zz yy + zz xx) + yy xx) - (xx yy) zz; keep 1+xx, 1+yy, 1+zz
+    //   yz:  R += yz^2 (1 + xx)              keep yz (in 1+xx's place)
+    //   xy:  R += xy^2 (1 + zz)              keep Q = xy yz
+    //   xz:  R += xz^2 (1 + yy) - 2 Q xz
+    // (the coefficient rows 1 + h carry h's rounding at the size of the product's own; the residual
+    // is never formed as a difference of 1 + rho and det(I + H))
+    constexpr int NKEEP = LEAN ? 3 : MA ? 6 : S2 ? 2 : 1;
     cplx<T> o[NKEEP][E];
     cplx<T> acc[E];
     T *dst_row = nullptr;
 #pragma unroll
     for (int q = 0; q < NIN; q++) {
-        const int f = S2 ? (q == 0 ? 0 : q == 1 ? 3 : q == 2 ? 5 : q == 3 ? 1 : q == 4 ? 4 : 2) : q;
+        const int f = S2 ? (q == 0 ? 0 : q == 1 ? 3 : q == 2 ? 5 : q == 3 ? 1 : q == 4 ? 4 : 2)
+                      : LEAN ? (q == 0 ? 0 : q == 1 ? 3 : q == 2 ? 5 : q == 3 ? 4 : q == 4 ? 1 : 2) : q;
         // kz factor of input f: 0 -> 1, 1 -> i kz, 2 -> -kz^2
         int fac = 0;
         if (S2 || MA) fac = (f == 2 || f == 4) ? 1 : (f == 5 ? 2 : 0);
@@ -370,6 +406,13 @@ __global__ void __launch_bounds__(256, (OP == ZOP_HESS_MA || OP == ZOP_HESS_MA_K
                 } else {  // - xy^2, - yz^2, - xz^2
                     acc[e] = mk<T>(acc[e].x - x.x * x.x, acc[e].y - x.y * x.y);
                 }
+            }
+        } else if constexpr (LEAN) {
+#pragma unroll
+            for (int e = 0; e < E; e++) {
+                const cplx<T> x = cscale<T>(v[e], scale);
+                ma_lean_step<T>(q, x.x, o[0][e].x, o[1][e].x, o[2][e].x, acc[e].x);
+                ma_lean_step<T>(q, x.y, o[0][e].y, o[1][e].y, o[2][e].y, acc[e].y);
             }
         } else {
 #pragma unroll
@@ -433,6 +476,15 @@ __global__ void __launch_bounds__(256, (OP == ZOP_HESS_MA || OP == ZOP_HESS_MA_K
             T res2[2], s2v[2];
 #pragma unroll
             for (int c = 0; c < 2; c++) {
+                if constexpr (LEAN) {
+                    const T r = rho[2 * n + c];
+                    const T res = r + (c ? acc[e].y : acc[e].x);
+                    res2[c] = res;
+                    s2v[c] = 0;
+                    sres += (double)res * (double)res;
+                    srho += (double)r * (double)r;
+                    continue;
+                }
                 const T xx = (c ? o[0][e].y : o[0][e].x) * scale;
                 const T xy = (c ? o[1][e].y : o[1][e].x) * scale;
                 const T xz = (c ? o[2][e].y : o[2][e].x) * scale;
@@ -455,7 +507,7 @@ __global__ void __launch_bounds__(256, (OP == ZOP_HESS_MA || OP == ZOP_HESS_MA_K
                 if (valid) *reinterpret_cast<cplx<T> *>(dst + 2 * n) = resv[e];
             }
             // optional second output: the second-order source S of the same Hessian
-            if (valid && a.out[1])
+            if (!LEAN && valid && a.out[1])
                 *reinterpret_cast<cplx<T> *>(bat<T>(a.out[1], bo) + row * a.rp_out + 2 * n) = mk<T>(s2v[0], s2v[1]);
         }
         if constexpr (OP == ZOP_HESS_MA) {
@@ -470,7 +522,7 @@ __global__ void __launch_bounds__(256, (OP == ZOP_HESS_MA || OP == ZOP_HESS_MA_K
             atomicAdd(a.red + (size_t)blockIdx.y * a.acc_stride + 0, sres);
             atomicAdd(a.red + (size_t)blockIdx.y * a.acc_stride + 1, srho);
         }
-        if constexpr (OP == ZOP_HESS_MA_K) {
+        if constexpr (MAK) {
             // the residual row's r2c along z (as in ZOP_HESS_2LPT_K)
 #pragma unroll
             for (int e = 0; e < E; e++) psm[xpos<NL, 1>(nout_any<NL, E>(pl, t, e))] = resv[e];
@@ -639,7 +691,8 @@ static int launch_zc_e(const GridGeom &g, const PassArgs &a) {
     auto kern = k_z_c2r<T, E, OP, NLZ>;
     if (smem > 48 * 1024) MITOS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     launch_begin(OP == ZOP_C2R ? "z_c2r" : OP == ZOP_HESS_2LPT ? "z_hess_2lpt" : OP == ZOP_HESS_2LPT_K ? "z_hess_2lpt_r2c"
-                 : OP == ZOP_HESS_MA ? "z_hess_ma" : OP == ZOP_HESS_MA_K ? "z_hess_ma_r2c" : "z_disp");
+                 : OP == ZOP_HESS_MA ? "z_hess_ma" : OP == ZOP_HESS_MA_K ? "z_hess_ma_r2c"
+                 : OP == ZOP_HESS_MA_KS ? "z_hess_ma_r2c_s" : "z_disp");
     kern<<<dim3((unsigned)((rows + P - 1) / P), a.batch > 1 ? a.batch : 1), threads, smem, stream()>>>(g, with_f32(a));
     count_launch();
     MITOS_LAUNCH_CHECK("z c2r pass");
@@ -656,6 +709,7 @@ int launch_zc_t(const GridGeom &g, ZOp op, const PassArgs &a) {
         case ZOP_DISP: return launch_zc_e<T, 8, ZOP_DISP, NLZ>(g, a);
         case ZOP_HESS_2LPT_K: return launch_zc_e<T, 8, ZOP_HESS_2LPT_K, NLZ>(g, a);
         case ZOP_HESS_MA_K: return launch_zc_e<T, 8, ZOP_HESS_MA_K, NLZ>(g, a);
+        case ZOP_HESS_MA_KS: return launch_zc_e<T, 8, ZOP_HESS_MA_KS, NLZ>(g, a);
         }
     } else {
         switch (op) {
@@ -665,6 +719,7 @@ int launch_zc_t(const GridGeom &g, ZOp op, const PassArgs &a) {
         case ZOP_DISP: return launch_zc_e<T, 12, ZOP_DISP, 0>(g, a);
         case ZOP_HESS_2LPT_K: return launch_zc_e<T, 12, ZOP_HESS_2LPT_K, 0>(g, a);
         case ZOP_HESS_MA_K: return launch_zc_e<T, 12, ZOP_HESS_MA_K, 0>(g, a);
+        case ZOP_HESS_MA_KS: return launch_zc_e<T, 12, ZOP_HESS_MA_KS, 0>(g, a);
         }
     }
     return 3;

@@ -56,8 +56,10 @@ enum ZOp {
     ZOP_HESS_2LPT_K,  // ZOP_HESS_2LPT followed by the r2c of S along z in the same pass: out[0] is
                       // the complex z-transformed source (N/2+1 per row, unnormalised), as
                       // ZOP_HESS_2LPT + a z r2c with scale 1 would leave it
-    ZOP_HESS_MA_K     // ZOP_HESS_MA with the residual's r2c along z in the same pass (out[0] complex,
-                      // as above; out[1], the optional source, stays real)
+    ZOP_HESS_MA_K,    // ZOP_HESS_MA with the residual's r2c along z in the same pass (out[0] complex,
+                      // as above), without the source output: the residual is accumulated as the
+                      // rows arrive, four rows live instead of six
+    ZOP_HESS_MA_KS    // ZOP_HESS_MA_K with out[1], the second-order source S (real), as well
 };
 
 struct PassArgs {
@@ -114,5 +116,13 @@ template <typename T> int launch_x(const GridGeom &g, XOp op, int sign, const Pa
 template <typename T> int launch_y(const GridGeom &g, YOp op, int sign, const PassArgs &a);
 template <typename T> int launch_z_c2r(const GridGeom &g, ZOp op, const PassArgs &a);
 template <typename T> int launch_z_r2c(const GridGeom &g, const PassArgs &a);
+
+// the r2c's Z and Y steps in one thread-block-cluster pass (fft_cluster.cu); -1: no cluster shape
+// for this grid (FP32 N = 256 and 512 have them) or the pass is off, the caller runs the two passes
+int launch_zy_r2c(const GridGeom &g, int precision, const PassArgs &a);
+void set_cluster_fft(int mode);  // 0: off (the two-pass route); 1..3: a cluster shape
+int cluster_fft();
+// launch_zy_r2c, else the Z r2c pass and the Y pass in place on a.out[0] (api.cu)
+int grid_r2c_zy(const GridGeom &g, int prec, const PassArgs &a);
 
 }  // namespace mitos

@@ -174,11 +174,9 @@ static int add_poisson(const GridGeom &g, int prec, double boxlen, const void *s
     a.out[0] = Sk;
     a.rp_in = g.N + 2;
     a.rho_a = 1.0;
-    int e = prec == MITOS_FP32 ? launch_z_r2c<float>(g, a) : launch_z_r2c<double>(g, a);
+    int e = grid_r2c_zy(g, prec, a);
     if (e) return e;
     a.in[0] = Sk;
-    e = prec == MITOS_FP32 ? launch_y<float>(g, YOP_PLAIN, -1, a) : launch_y<double>(g, YOP_PLAIN, -1, a);
-    if (e) return e;
     a.in2 = phi;
     a.out[0] = phi;
     a.scale = boxlen * boxlen * boxlen / ((double)g.N * g.N * g.N);
@@ -245,7 +243,8 @@ static int ma_run(struct distributed_grid *pot, struct distributed_grid *dens, s
         MITOS_CUDA(cudaMemsetAsync(red, 0, 2 * sizeof(double), stream()));
         const bool want_S = it == 0 && (warm || cap);
         // the residual leaves the Z pass already transformed along z (into Sk)
-        e = grid_hessian(g, prec, L, pot->fbox, ZOP_HESS_MA_K, dens->box, Sk, red, 0, want_S ? S : nullptr);
+        e = grid_hessian(g, prec, L, pot->fbox, want_S ? ZOP_HESS_MA_KS : ZOP_HESS_MA_K, dens->box, Sk, red, 0,
+                         want_S ? S : nullptr);
         if (e) break;
         double h[2];
         MITOS_CUDA(cudaMemcpyAsync(h, red, sizeof h, cudaMemcpyDeviceToHost, stream()));

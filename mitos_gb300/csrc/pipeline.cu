@@ -553,9 +553,8 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     a.rp_in = rho_pitch;
     a.rho_a = 1.0;
     a.rho_b = -1.0;
-    e = launch_z_r2c<T>(g, a);
+    e = grid_r2c_zy(g, sizeof(T) == 4 ? MITOS_FP32 : MITOS_FP64, a);
     a.in[0] = Sk;
-    if (!e) e = launch_y<T>(g, YOP_PLAIN, -1, a);
     a.rho_a = 1.0;
     a.rho_b = 0.0;
     a.out[0] = nullptr;
