@@ -551,6 +551,11 @@ int mitos_get_radix(int N, int precision, int *rad_n, int *stages_n, int *rad_h,
  * counterpart (a switch of this library's FFT; fft_r2c_dg, src/fft.c:219-236, is the transform
  * either way). */
 int mitos_set_cluster_fft(int mode);
+/* Staging of the lattice deposit's displacement tiles: 1 (the default) stages the bricks off the box's
+ * x and y faces with tensor copies (cp.async.bulk.tensor, one thread a brick), 0 stages every brick
+ * with 16-byte cp.async.  The results are identical.  Returns the previous setting.  No reference
+ * counterpart. */
+int mitos_set_lattice_tma(int on);
 
 #ifdef __cplusplus
 }

@@ -371,6 +371,12 @@ extern "C" int mitos_set_cluster_fft(int mode) {
     return was;
 }
 
+extern "C" int mitos_set_lattice_tma(int on) {
+    const int was = lattice_tma() ? 1 : 0;
+    set_lattice_tma(on != 0);
+    return was;
+}
+
 extern "C" int fft_r2c_dg(struct distributed_grid *dg) {
     const GridGeom *g = geom(dg->N, dg->precision);
     if (!g) return 3;

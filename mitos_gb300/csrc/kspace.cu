@@ -125,12 +125,124 @@ __global__ void k_apply(int N, double dk, KernelParams kp, const cplx<T> *__rest
     }
 }
 
+// FP32 grids.  A kernel that depends on k alone is evaluated once per integer |n|^2 (FP64, at
+// k = sqrt(n^2) dk, the reference formulas above) and applied as an FP32 factor; the TSC window undo
+// is separable (one FP64 table of W(k_i)^-order per axis index).  Per mode the FP64 evaluation ran
+// on GB300's FP64 pipe, a small fraction of its FP32 rate (1.17 ms at 256^3 for the transfer
+// function, against the 0.02 ms the grid's bytes take); the factor differs from the per-mode FP64
+// value by an ulp of k or so, far inside the FP32 result's rounding.
+static bool isotropic(int id) {
+    switch (id) {
+    case KID_CONSTANT: case KID_LOWPASS: case KID_HIPASS: case KID_TOPHAT: case KID_GAUSSIAN:
+    case KID_GAUSSIAN_INV: case KID_INV_POISSON: case KID_POWER_NO_TRANSFER: case KID_TRANSFER:
+    case KID_INV_TRANSFER:
+        return true;
+    default:
+        return false;
+    }
+}
+
+// tab[n2] = the kernel's real factor at k = sqrt(n2) dk, n2 <= n2max (isotropic kernels: no
+// imaginary part); through k_apply's own switch on one complex one
+__global__ void k_iso_table(long n2max, double dk, KernelParams kp, float *__restrict__ tab) {
+    for (long n2 = (long)blockIdx.x * blockDim.x + threadIdx.x; n2 <= n2max; n2 += (long)gridDim.x * blockDim.x) {
+        const double k = sqrt((double)n2) * dk;
+        double kr = 0;
+        switch (kp.id) {
+        case KID_CONSTANT: kr = kp.c[0]; break;
+        case KID_LOWPASS: kr = (k < kp.c[0]) ? 1.0 : 0.0; break;
+        case KID_HIPASS: kr = (k > kp.c[0]) ? 1.0 : 0.0; break;
+        case KID_TOPHAT: kr = (k >= kp.c[0] && k <= kp.c[1]) ? 1.0 : 0.0; break;
+        case KID_GAUSSIAN: { double kR = k * kp.c[0]; kr = exp(-kR * kR); break; }
+        case KID_GAUSSIAN_INV: { double kR = k * kp.c[0]; kr = exp(kR * kR); break; }
+        case KID_INV_POISSON: kr = (k > 0) ? -1.0 / k / k : 1.0; break;
+        case KID_POWER_NO_TRANSFER:
+            kr = (k == 0) ? 0.0 : sqrt(kp.c[0] * pow(k / kp.c[2], kp.c[1] - 1.) * k * (2. * M_PI * M_PI));
+            break;
+        case KID_TRANSFER:
+        case KID_INV_TRANSFER:
+            if (k == 0) {
+                kr = 0.0;
+            } else {
+                const double T = transfer_at<double>(kp.tk, kp.tlo, kp.thi, kp.k_size, k, kp.c[0]);
+                kr = (kp.id == KID_TRANSFER) ? T : 1.0 / T;
+            }
+            break;
+        default: break;
+        }
+        tab[n2] = (float)kr;
+    }
+}
+
+// w[j] = W(k_j)^-order for the axis index j < N (kint order), the TSC window undo's factor per axis
+__global__ void k_window_table(int N, double half_cell, int order, double *__restrict__ w) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < N; j += gridDim.x * blockDim.x) {
+        const double x = (double)kint(j, N) * half_cell;
+        const double W = x == 0 ? 1. : sin(x) / x;
+        w[j] = 1.0 / pow(W, (double)order);
+    }
+}
+
+__global__ void k_apply32_iso(int N, const float *__restrict__ tab, const float2 *__restrict__ in,
+                              float2 *__restrict__ out) {
+    const int H = N / 2 + 1;
+    const long total = (long)N * N * H;
+    for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < total; id += (long)gridDim.x * blockDim.x) {
+        const int z = (int)(id % H);
+        const long xy = id / H;
+        const int jy = kint((int)(xy % N), N), jx = kint((int)(xy / N), N);
+        const float f = tab[jx * jx + jy * jy + z * z];
+        const float2 a = in[id];
+        out[id] = make_float2(a.x * f, a.y * f);
+    }
+}
+
+__global__ void k_apply32_window(int N, const double *__restrict__ w, const float2 *__restrict__ in,
+                                 float2 *__restrict__ out) {
+    const int H = N / 2 + 1;
+    const long total = (long)N * N * H;
+    for (long id = (long)blockIdx.x * blockDim.x + threadIdx.x; id < total; id += (long)gridDim.x * blockDim.x) {
+        const int z = (int)(id % H);
+        const long xy = id / H;
+        const int y = (int)(xy % N), x = (int)(xy / N);
+        // k = 0 keeps its mode (the reference's kr = 1 there); w[0] = 1 already
+        const float f = (float)w[x] * (float)w[y] * (float)w[z];
+        const float2 a = in[id];
+        out[id] = make_float2(a.x * f, a.y * f);
+    }
+}
+
 int apply_kernel_launch(int N, double boxlen, int precision, const KernelParams &kp,
                         const void *in, void *out) {
     const double dk = 2 * M_PI / boxlen;
     const long total = (long)N * N * (N / 2 + 1);
     int blocks = (int)((total + 255) / 256);
     if (blocks > 152 * 32) blocks = 152 * 32;
+    if (precision == MITOS_FP32 && (isotropic(kp.id) || kp.id == KID_UNDO_HERMITE)) {
+        if (kp.id == KID_UNDO_HERMITE) {
+            double *w = (double *)workspace(sizeof(double) * (size_t)N, 170);
+            if (!w) return 5;
+            launch_begin("apply_kernel_table");
+            k_window_table<<<(N + 255) / 256, 256, 0, stream()>>>(N, 0.5 * kp.c[0] / kp.c[1] * dk, kp.order, w);
+            count_launch();
+            MITOS_LAUNCH_CHECK("fft_apply_kernel_dg window table");
+            launch_begin("apply_kernel");
+            k_apply32_window<<<blocks, 256, 0, stream()>>>(N, w, (const float2 *)in, (float2 *)out);
+        } else {
+            const long n2max = 3L * (N / 2) * (N / 2);
+            float *tab = (float *)workspace(sizeof(float) * (size_t)(n2max + 1), 171);
+            if (!tab) return 5;
+            launch_begin("apply_kernel_table");
+            k_iso_table<<<(unsigned)((n2max + 256) / 256), 256, 0, stream()>>>(n2max, dk, kp, tab);
+            count_launch();
+            MITOS_LAUNCH_CHECK("fft_apply_kernel_dg table");
+            launch_begin("apply_kernel");
+            k_apply32_iso<<<blocks, 256, 0, stream()>>>(N, tab, (const float2 *)in, (float2 *)out);
+        }
+        count_launch();
+        MITOS_LAUNCH_CHECK("fft_apply_kernel_dg");
+        return 0;
+    }
     launch_begin("apply_kernel");
     if (precision == MITOS_FP32)
         k_apply<float><<<blocks, 256, 0, stream()>>>(N, dk, kp, (const float2 *)in, (float2 *)out);

@@ -13,8 +13,42 @@
 
 #include "context.cuh"
 #include "particles.cuh"
+#include "tma.cuh"
 
 namespace mitos {
+
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
+
+bool encode_grid_map(CUtensorMap *m, const void *base, bool f64, long n2, long n1, long pitch, unsigned b0,
+                     unsigned b1, unsigned b2) {
+    PFN_cuTensorMapEncodeTiled_v12000 fn = tensor_map_encoder();
+    if (!fn) return false;
+    const cuuint64_t es = f64 ? 8 : 4;
+    const cuuint64_t dims[3] = {(cuuint64_t)pitch, (cuuint64_t)n1, (cuuint64_t)n2};
+    const cuuint64_t strides[2] = {(cuuint64_t)pitch * es, (cuuint64_t)(pitch * n1) * es};
+    const cuuint32_t box[3] = {b0, b1, b2};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    return fn(m, f64 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void *>(base), dims,
+              strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// set by a deposit kernel whose tile copies did not complete (it then stops; see lattice_fault)
+__device__ int g_lattice_fault;
 
 template <typename T> __device__ __forceinline__ T dfloor(T x);
 template <> __device__ __forceinline__ float dfloor<float>(float x) { return floorf(x); }
@@ -301,13 +335,21 @@ __device__ __forceinline__ void stage_tiles(T *tiles, int N, int rpd, int x0, in
     }
 }
 
+// tensor maps of the three displacement grids, boxes of the brick tiles: d0 {LB_Z, LB_Y, LB_X}, d1
+// {LB_Z, LB_Y, T1X}, d2 {LB_Z, T2Y, T1X} (z innermost)
+struct LatticeMaps {
+    CUtensorMap m0, m1, m2;
+};
+
 // Persistent: each block walks bricks b = blockIdx.x, blockIdx.x + gridDim.x, ..., staging the
-// next brick's tiles (cp.async, second buffer) while it displaces and deposits the current one.
+// next brick's tiles (second buffer) while it displaces and deposits the current one.  Bricks whose
+// halos stay inside the box (not on an x or y face) are staged by three tensor copies issued by one
+// thread, completing on the buffer's mbarrier; face bricks, whose halos wrap, by 16-byte cp.async.
 template <typename T>
 __global__ void __launch_bounds__(LB_THREADS, 2)
 k_lattice_cic(int N, int rpd, int rpo, float spacing, float Lf, T ginv, const T *__restrict__ d0, const T *__restrict__ d1,
               const T *__restrict__ d2, T *__restrict__ rho, float *__restrict__ pos_out, size_t bstride, FastDiv div_bx,
-              FastDiv div_by, float *__restrict__ posraw_out) {
+              FastDiv div_by, float *__restrict__ posraw_out, const __grid_constant__ LatticeMaps maps, int use_tma) {
     // batched launches: realisation blockIdx.y (its grids bstride bytes apart)
     if (gridDim.y > 1) {
         const size_t bo = (size_t)blockIdx.y * bstride;
@@ -332,11 +374,38 @@ k_lattice_cic(int N, int rpd, int rpo, float spacing, float Lf, T ginv, const T 
         bz = (int)fdiv((unsigned)q, div_by);
         by = q - bz * by_n;
     };
+    // tensor-copy staging: two mbarriers behind the tile buffers, one per buffer; bit b of `phase`
+    // is the parity of buffer b's next completion (uniform in the block, as the brick sequence is)
+    uint64_t *bars = reinterpret_cast<uint64_t *>(tbuf + 2 * TILE_ELEMS);
+    const bool tma = use_tma && gridDim.y == 1 && (smem_u32(tbuf) & 127) == 0;
+    if (tma && threadIdx.x == 0) {
+        mbar_init(bars, 1);
+        mbar_init(bars + 1, 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    unsigned phase = 0;
+    auto by_tma = [&](int bx, int by) { return tma && bx > 0 && bx < bx_n - 1 && by > 0 && by < by_n - 1; };
+    auto stage = [&](int bx, int by, int bz, int bi) {
+        T *dst = tbuf + bi * TILE_ELEMS;
+        const int x0 = bx * LB_X, y0 = by * LB_Y, z0 = bz * LB_Z;
+        if (by_tma(bx, by)) {
+            if (threadIdx.x == 0) {
+                fence_proxy_async();
+                mbar_expect_tx(bars + bi, (unsigned)(TILE_ELEMS * sizeof(T)));
+                tma_load_3d(dst, &maps.m0, z0, y0, x0, bars + bi);
+                tma_load_3d(dst + LB_X * LB_Y * LB_Z, &maps.m1, z0, y0, x0 - TH, bars + bi);
+                tma_load_3d(dst + LB_X * LB_Y * LB_Z + T1X * LB_Y * LB_Z, &maps.m2, z0, y0 - TH, x0 - TH, bars + bi);
+            }
+        } else {
+            stage_tiles<T>(dst, N, rpd, x0, y0, z0, d0, d1, d2);
+        }
+    };
     int b = blockIdx.x;
     if (b < nbricks) {
         int bx, by, bz;
         decode(b, bx, by, bz);
-        stage_tiles<T>(tbuf, N, rpd, bx * LB_X, by * LB_Y, bz * LB_Z, d0, d1, d2);
+        stage(bx, by, bz, 0);
     }
     cp_async_commit();
     const int lz = threadIdx.x % LB_Z, ly = (threadIdx.x / LB_Z) % LB_Y, lxb = threadIdx.x / (LB_Z * LB_Y);
@@ -346,14 +415,29 @@ k_lattice_cic(int N, int rpd, int rpo, float spacing, float Lf, T ginv, const T 
         decode(b, bx, by, bz);
         const int x0 = bx * LB_X, y0 = by * LB_Y, z0 = bz * LB_Z;
         const int bn = b + gridDim.x;
+        bool next_tma = false;
         if (bn < nbricks) {
             int nx, ny, nz;
             decode(bn, nx, ny, nz);
-            stage_tiles<T>(tbuf + (buf ^ 1) * TILE_ELEMS, N, rpd, nx * LB_X, ny * LB_Y, nz * LB_Z, d0, d1, d2);
+            stage(nx, ny, nz, buf ^ 1);
+            next_tma = by_tma(nx, ny);
         }
         cp_async_commit();
         cp_async_wait_prev();
-        __syncthreads();  // this brick's tiles have landed; the accumulators are zero
+        bool ok = true;
+        if (by_tma(bx, by)) {
+            ok = mbar_wait(bars + buf, (phase >> buf) & 1u);
+            phase ^= 1u << buf;
+        }
+        // this brick's tiles have landed; the accumulators are zero
+        if (__syncthreads_or(!ok)) {
+            // a tensor copy that never completed: flag it, let the next brick's copy finish (bounded)
+            // and stop
+            if (threadIdx.x == 0) atomicExch(&g_lattice_fault, 1);
+            if (next_tma) mbar_wait(bars + (buf ^ 1), (phase >> (buf ^ 1)) & 1u);
+            cp_async_wait_all();
+            return;
+        }
         const T *t0 = tbuf + buf * TILE_ELEMS;
         const T *t1 = t0 + LB_X * LB_Y * LB_Z;
         const T *t2 = t1 + T1X * LB_Y * LB_Z;
@@ -470,9 +554,35 @@ k_lattice_cic(int N, int rpd, int rpo, float spacing, float Lf, T ginv, const T 
 }
 
 static size_t lattice_smem(size_t elem) {
-    // the region accumulators have the size of one element in either precision
-    return elem * ((size_t)LR_X * LR_Y * LR_Z + 2 * (size_t)TILE_ELEMS);
+    // the region accumulators have the size of one element in either precision; two mbarriers
+    return elem * ((size_t)LR_X * LR_Y * LR_Z + 2 * (size_t)TILE_ELEMS) + 2 * sizeof(uint64_t);
 }
+
+// the fault flag reaches the host through a pinned word, copied behind the deposit on the library
+// stream and read once the caller has synchronised it
+static int *g_fault_host = nullptr;
+int lattice_fault_fetch() {
+    if (!g_fault_host) {
+        MITOS_CUDA(cudaHostAlloc((void **)&g_fault_host, sizeof(int), cudaHostAllocDefault));
+        *g_fault_host = 0;
+    }
+    MITOS_CUDA(cudaMemcpyFromSymbolAsync(g_fault_host, g_lattice_fault, sizeof(int), 0, cudaMemcpyDeviceToHost, stream()));
+    return 0;
+}
+int lattice_fault_check() {
+    if (!g_fault_host || !*g_fault_host) return 0;
+    *g_fault_host = 0;
+    const int zero = 0;
+    MITOS_CUDA(cudaMemcpyToSymbolAsync(g_lattice_fault, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, stream()));
+    MITOS_CUDA(cudaStreamSynchronize(stream()));
+    set_error(6, "a displacement tile copy of the deposit did not complete (bounded wait timed out)");
+    return 6;
+}
+
+// tensor-copy staging of the interior bricks (on by default; off: 16-byte cp.async for all)
+static bool g_lattice_tma = true;
+void set_lattice_tma(bool on) { g_lattice_tma = on; }
+bool lattice_tma() { return g_lattice_tma; }
 
 template <typename T>
 static int lattice_launch(int N, int rpd, int rpo, float spacing, float Lf, double ginv, const void *d0, const void *d1,
@@ -493,10 +603,18 @@ static int lattice_launch(int N, int rpd, int rpo, float spacing, float Lf, doub
     const long nbricks = (long)(N / LB_X) * (N / LB_Y) * (N / LB_Z);
     const int nb = batch > 1 ? batch : 1;
     const unsigned blocks = (unsigned)std::max<long>(1, std::min<long>(nbricks, (long)sms * bps / nb));
+    // tensor maps of the three grids (one realisation: batched launches stage with cp.async)
+    LatticeMaps maps;
+    memset(&maps, 0, sizeof maps);
+    const bool f64 = sizeof(T) == 8;
+    int use_tma = g_lattice_tma && nb == 1 &&
+                  encode_grid_map(&maps.m0, d0, f64, N, N, rpd, LB_Z, LB_Y, LB_X) &&
+                  encode_grid_map(&maps.m1, d1, f64, N, N, rpd, LB_Z, LB_Y, T1X) &&
+                  encode_grid_map(&maps.m2, d2, f64, N, N, rpd, LB_Z, T2Y, T1X);
     kern<<<dim3(blocks, nb), LB_THREADS, smem, stream()>>>(N, rpd, rpo, spacing, Lf, (T)ginv, (const T *)d0,
                                                            (const T *)d1, (const T *)d2, (T *)rho, pos_out, bstride,
                                                            make_fastdiv((unsigned)(N / LB_X)), make_fastdiv((unsigned)(N / LB_Y)),
-                                                           posraw_out);
+                                                           posraw_out, maps, use_tma);
     return 0;
 }
 

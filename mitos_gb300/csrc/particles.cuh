@@ -16,6 +16,14 @@ int lattice_deposit(int N, double boxlen, int precision, const void *d0, const v
                     int disp_pitch, void *rho, int rho_pitch, float *pos_out, int batch = 1, size_t bstride = 0,
                     float *posraw_out = nullptr);
 bool lattice_aligned(int N, int M, double boxlen);
+// tensor-copy staging of the deposit's interior bricks on (default) or off (16-byte cp.async)
+void set_lattice_tma(bool on);
+bool lattice_tma();
+// a deposit that stops because a tile copy never completed (bounded wait) sets a device flag:
+// lattice_fault_fetch queues its copy to the host behind the deposit; lattice_fault_check, once the
+// library stream is synchronised, returns 6 with the error message if it was set (and clears it)
+int lattice_fault_fetch();
+int lattice_fault_check();
 // particle velocities: TSC gather of the three velocity grids (row pitch `pitch` reals) at the
 // unwrapped positions pos (np x 3), float velocities out (np x 3)
 int velocity_gather(long np, int N, int pitch, double boxlen, int precision, const float *pos, const void *v0,

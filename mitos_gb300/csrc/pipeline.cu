@@ -421,6 +421,7 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     MITOS_CUDA(cudaMemsetAsync(rhoD, 0, rho_bytes, stream()));
     e = aligned ? lattice_deposit(N, L, prec, D0, D1, D2, disp_pitch, rhoD, rho_pitch, dpos, B, bs, dposraw)
                 : displace_and_deposit(N, M, L, prec, D0, D1, D2, rhoD, dpos, dposraw);
+    if (!e && aligned && !(opt && opt->graph)) e = lattice_fault_fetch();
     if (e) return e;
     if (res && res->pos) {
         MITOS_CUDA(cudaEventRecord(pos_event(pslot, 0), stream()));
@@ -601,6 +602,7 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
                                    cudaMemcpyDeviceToHost, stream()));
         MITOS_CUDA(cudaStreamSynchronize(stream()));
         if (dpos || want_vel) MITOS_CUDA(cudaEventSynchronize(pos_event(pslot, 1)));
+        if ((e = lattice_fault_check())) return e;
         if (therr) {
             int h = 0;
             MITOS_CUDA(cudaMemcpy(&h, therr, sizeof(int), cudaMemcpyDeviceToHost));
@@ -619,6 +621,7 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
         res->ma_residual = last_rel;
     } else {
         MITOS_CUDA(cudaStreamSynchronize(stream()));
+        if ((e = lattice_fault_check())) return e;
     }
     tim.finish();
     return 0;
@@ -711,6 +714,7 @@ int finish_slot(int k) {
     MITOS_CUDA(cudaEventSynchronize(acc_event(k)));
     if (s.res && (s.res->pos || s.res->vel || s.res->coords || s.res->vels || s.res->masses || s.res->ids))
         MITOS_CUDA(cudaEventSynchronize(pos_event(k, 1)));
+    if (const int f = lattice_fault_check()) return f;
     if (!s.res) return 0;
     const double *ksum;
     const long long *count;

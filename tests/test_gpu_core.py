@@ -194,6 +194,29 @@ def test_kernels_fp64(name, table, spline):
     ml.free_local_grid(w)
 
 
+@pytest.mark.parametrize("name", ["constant", "lowpass", "hipass", "tophat", "gaussian", "inv_poisson",
+                                  "dx", "power_no_transfer", "transfer_function", "undo_Hermite_window"])
+@pytest.mark.parametrize("N", [32, 96])
+def test_kernels_fp32(name, N, table, spline):
+    """FP32 grids: the k-only kernels from a table per |n|^2, the window undo from per-axis tables
+    (a k-only factor evaluated at k = sqrt(n^2) dk): within FP32 rounding of the FP64 oracle"""
+    L = 4.0 * N
+    src = _rand_c(N, 3)
+    g = ml.alloc_local_grid(N, L, ml.FP32)
+    w = ml.alloc_local_grid(N, L, ml.FP32)
+    ml.set_fbox(g, src)
+    mp, op = _kernel_params(name, N, L, table, spline)
+    assert ml.fft_apply_kernel_dg(w, g, name, mp) == 0
+    got = ml.get_fbox(w)
+    oname = {"transfer_function": "transfer", "undo_Hermite_window": "undo_hermite"}.get(name, name)
+    ref = oracle.apply_kernel(N, L, src.astype(np.complex64).astype(complex), oname, op)
+    assert np.abs(ref).max() > 0
+    tol = 2e-7 if name in ("constant", "lowpass", "hipass", "tophat", "dx") else 1e-6
+    assert rel_err(got, ref) < tol
+    ml.free_local_grid(g)
+    ml.free_local_grid(w)
+
+
 def test_kernel_error_paths():
     g = ml.alloc_local_grid(16, 10.0, ml.FP64)
     w = ml.alloc_local_grid(32, 10.0, ml.FP64)

@@ -1,0 +1,44 @@
+"""The lattice deposit's tile staging by tensor copies (cp.async.bulk.tensor on an mbarrier, the
+bricks off the box's x and y faces) against 16-byte cp.async staging of every brick: the same
+tiles, so bit-identical positions and P(k) (src/particle.c:87-129, analyse/src/mitos_read.c:280-334)."""
+import numpy as np
+import pytest
+
+import mitos_gb300.lib as ml
+from mitos_gb300.perturb import load_table
+
+pytestmark = pytest.mark.gpu
+
+
+def _names(fn):
+    ml.kernel_timing(True)
+    try:
+        fn()
+        return [k for k, _ in ml.kernel_times()]
+    finally:
+        ml.kernel_timing(False)
+
+
+@pytest.mark.parametrize("N,L,prec", [(64, 128.0, ml.FP32), (256, 500.0, ml.FP32), (128, 256.0, ml.FP64),
+                                      (512, 1000.0, ml.FP32)])
+def test_tma_staging_bit_identical(N, L, prec):
+    table = load_table()
+    spline = ml.Spline(table)
+    cfg = ml.ic_config(N, N, L, 11, table, pk_bins=32, pk_linear=True, precision=prec)
+    was = ml.set_lattice_tma(True)
+    try:
+        r1 = ml.ic_pipeline_run(cfg, spline, want_pos=True)
+        assert "lattice_cic" in _names(lambda: ml.ic_pipeline_run(cfg, spline))
+        ml.set_lattice_tma(False)
+        r0 = ml.ic_pipeline_run(cfg, spline, want_pos=True)
+    finally:
+        ml.set_lattice_tma(was)
+    assert np.array_equal(r1["pos"], r0["pos"])
+    ok = r1["pk_obs"] > 0  # empty shells are 0/0 in both
+    assert np.all(np.isfinite(r1["pk_p"][ok])) and r1["pk_p"][ok].max() > 0
+    if prec == ml.FP32:
+        # 32-bit fixed-point deposit sums: exact and order independent
+        assert np.array_equal(r1["pk_p"][ok], r0["pk_p"][ok])
+    else:
+        # FP64 deposit sums are shared-memory double atomics, whose order varies from run to run
+        assert np.abs(r1["pk_p"][ok] / r0["pk_p"][ok] - 1).max() < 1e-12
