@@ -38,10 +38,12 @@ struct NoiseFilter {
     const void *table;  // device, filter value per n2 (precision of the grid), or NULL
 };
 // batched form: states (device, one 32-byte start state per realisation) and batch grids
-// bstride bytes apart; states = nullptr for one realisation started at st
+// bstride bytes apart; states = nullptr for one realisation started at st.  zero / zero_bytes
+// (optional, 16-byte aligned, a multiple of 16 bytes): a buffer the kernel clears as well (the
+// deposit's density grid: the noise is integer-bound and leaves HBM idle, a separate memset not)
 int noise_generate(const GridGeom &g, int precision, double boxlen, uint64_t st[4],
                    const void *filter_by_n2, void *fbox, const void *states = nullptr, int batch = 1,
-                   size_t bstride = 0);
+                   size_t bstride = 0, void *zero = nullptr, size_t zero_bytes = 0);
 int hermitian_planes(const GridGeom &g, int precision, void *fbox, int batch = 1, size_t bstride = 0);
 void rng_jump(uint64_t st[4], unsigned long long n);
 

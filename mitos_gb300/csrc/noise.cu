@@ -276,7 +276,15 @@ __global__ void k_state_tables(RngState s0, const RngState *__restrict__ states,
 template <typename T>
 __global__ void __launch_bounds__(NOISE_THREADS)
 k_noise(int N, const uint64_t *__restrict__ polys, const ulonglong4 *__restrict__ gtab, T factor,
-        const T *__restrict__ filt, cplx<T> *__restrict__ out, size_t ostride) {
+        const T *__restrict__ filt, cplx<T> *__restrict__ out, size_t ostride, uint4 *__restrict__ zero,
+        size_t zero_n16) {
+    // the optional buffer to clear, 16 bytes a store over the whole grid of threads (issued first:
+    // the stores drain while the generator's integer work runs)
+    if (zero) {
+        const size_t nth = (size_t)gridDim.x * gridDim.y * blockDim.x;
+        for (size_t i = ((size_t)blockIdx.y * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x; i < zero_n16; i += nth)
+            zero[i] = make_uint4(0, 0, 0, 0);
+    }
     // batched launches: realisation blockIdx.y has its own state table and output grid
     out = bat<cplx<T>>(out, (size_t)blockIdx.y * ostride);
     __shared__ cplx<T> stage[NOISE_THREADS][NOISE_CHUNK + 1];
@@ -363,7 +371,12 @@ __global__ void k_hermitian(int N, cplx<T> *fbox, size_t bstride) {
 }
 
 int noise_generate(const GridGeom &g, int precision, double boxlen, uint64_t st[4],
-                   const void *filter_by_n2, void *fbox, const void *states, int batch, size_t bstride) {
+                   const void *filter_by_n2, void *fbox, const void *states, int batch, size_t bstride,
+                   void *zero, size_t zero_bytes) {
+    if (zero && (((uintptr_t)zero & 15) || (zero_bytes & 15))) {
+        set_error(3, "noise: the buffer to clear must be 16-byte aligned and sized");
+        return 3;
+    }
     const uint64_t *polys = column_polys(g.N);
     if (!polys) return 5;
     RngState s0;
@@ -385,10 +398,10 @@ int noise_generate(const GridGeom &g, int precision, double boxlen, uint64_t st[
     launch_begin("noise");
     if (precision == MITOS_FP32) {
         k_noise<float><<<grid, NOISE_THREADS, 0, stream()>>>(g.N, polys, tab, (float)factor, (const float *)filter_by_n2,
-                                                             (float2 *)fbox, ost);
+                                                             (float2 *)fbox, ost, (uint4 *)zero, zero_bytes / 16);
     } else {
         k_noise<double><<<grid, NOISE_THREADS, 0, stream()>>>(g.N, polys, tab, factor, (const double *)filter_by_n2,
-                                                              (double2 *)fbox, ost);
+                                                              (double2 *)fbox, ost, (uint4 *)zero, zero_bytes / 16);
     }
     count_launch();
     MITOS_LAUNCH_CHECK("noise");

@@ -282,7 +282,13 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     seed_state(cfg->seed, st);
     int e;
     void *dens_k = ma ? Sk : phi;  // Monge-Ampere keeps delta(k) to build rho(x)
-    e = noise_generate(g, prec, L, st, filt, dens_k, B > 1 ? opt->states : nullptr, B, bs);
+    // the lattice-aligned deposit's density grid (row pitch N + 4), cleared by the noise kernel
+    const int rho_pitch = aligned ? N + 4 : N + 2;
+    const size_t rho_bytes = B > 1 ? db : (size_t)N * N * rho_pitch * (sizeof(T));
+    void *rhoA = aligned ? workspace(rho_bytes, 15) : nullptr;
+    if (aligned && !rhoA) return 5;
+    e = noise_generate(g, prec, L, st, filt, dens_k, B > 1 ? opt->states : nullptr, B, bs, rhoA,
+                       aligned ? rho_bytes : 0);
     if (!e) e = hermitian_planes(g, prec, dens_k, B, bs);
     if (e) return e;
     tim.mark();
@@ -413,12 +419,11 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     // the slot's staging buffers are free once their previous copies are done
     if (dpos || want_vel) MITOS_CUDA(cudaStreamWaitEvent(stream(), pos_event(pslot, 1), 0));
     int *therr = nullptr;  // thermal motion: bit 0 set for an invalid momentum
-    // the aligned deposit uses a row pitch of N + 4 reals (16-byte aligned rows for vector reductions)
-    const int rho_pitch = aligned ? N + 4 : N + 2;
-    const size_t rho_bytes = B > 1 ? db : (size_t)N * N * rho_pitch * (sizeof(T));
-    void *rhoD = aligned ? workspace(rho_bytes, 15) : rho;
+    // the aligned deposit uses a row pitch of N + 4 reals (16-byte aligned rows for vector
+    // reductions) into the grid the noise kernel cleared; the general path into rho
+    void *rhoD = aligned ? rhoA : rho;
     if (!rhoD) return 5;
-    MITOS_CUDA(cudaMemsetAsync(rhoD, 0, rho_bytes, stream()));
+    if (!aligned) MITOS_CUDA(cudaMemsetAsync(rhoD, 0, rho_bytes, stream()));
     e = aligned ? lattice_deposit(N, L, prec, D0, D1, D2, disp_pitch, rhoD, rho_pitch, dpos, B, bs, dposraw)
                 : displace_and_deposit(N, M, L, prec, D0, D1, D2, rhoD, dpos, dposraw);
     if (!e && aligned && !(opt && opt->graph)) e = lattice_fault_fetch();
