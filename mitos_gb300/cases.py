@@ -6,6 +6,8 @@ whose grids still exceed L2 but whose device footprint stays at a few GB:
     python -m mitos_gb300.cases ma 256       # Monge-Ampere cycles (z_hess_ma, x_add_poisson)
     python -m mitos_gb300.cases noise 512    # white noise (k_noise), FP32 (noise64: FP64)
     python -m mitos_gb300.cases ic 256       # one FP32 initial condition (every pass)
+    python -m mitos_gb300.cases ensemble 0 3 # the 48 realisations (16 each of 64^3, 96^3, 128^3) as
+                                             # one graph; the size argument is unused
     python -m mitos_gb300.cases r2c 512 3 2  # fft_r2c_dg, FP32; fourth argument: the cluster mode
                                              # of the Z + Y step (mitos_set_cluster_fft; 0 = off)
 
@@ -102,11 +104,25 @@ def r2c(N: int, reps: int) -> float:
     return ms
 
 
+def ensemble(N: int, reps: int) -> float:
+    """ms per replay of the 48-member graph (2LPT, 32 linear shells, FP32, 4 Mpc/h cells), the
+    library's default tiles and batching"""
+    table = load_table()
+    spline = ml.Spline(table)
+    cfgs = [ml.ic_config(n, n, box, 1000 + 16 * k + i, table, pk_bins=32, pk_linear=True, precision=ml.FP32)
+            for k, (n, box) in enumerate([(64, 256.0), (96, 384.0), (128, 512.0)]) for i in range(16)]
+    ens = ml.Ensemble(cfgs, spline, streams=8)
+    ens.run()
+    ms = sum(ens.run() for _ in range(reps)) / reps
+    ens.close()
+    return ms
+
+
 def noise64(N: int, reps: int) -> float:
     return noise(N, reps, ml.FP64)
 
 
-CASES = {"conv": conv, "ngenic": ngenic, "ma": ma, "noise": noise, "noise64": noise64, "ic": ic, "r2c": r2c}
+CASES = {"conv": conv, "ngenic": ngenic, "ma": ma, "noise": noise, "noise64": noise64, "ic": ic, "r2c": r2c, "ensemble": ensemble}
 
 if __name__ == "__main__":
     name = sys.argv[1]
@@ -115,7 +131,10 @@ if __name__ == "__main__":
     if len(sys.argv) > 4:
         ml.set_cluster_fft(int(sys.argv[4]))
     print(f"{name} N={N}: {CASES[name](N, reps):.4f} ms per repetition")
-    # the same workload once more with per-launch timing: device time per kernel name
+    # the same workload once more with per-launch timing: device time per kernel name (not for the
+    # ensemble: its launches are captured into a graph)
+    if name == "ensemble":
+        sys.exit(0)
     ml.kernel_timing(True)
     CASES[name](N, 1)
     per = {}
