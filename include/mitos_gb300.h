@@ -556,6 +556,12 @@ int mitos_set_cluster_fft(int mode);
  * with 16-byte cp.async.  The results are identical.  Returns the previous setting.  No reference
  * counterpart. */
 int mitos_set_lattice_tma(int on);
+/* Order in which the lattice deposit's blocks walk its 8 x 8 x 32 bricks: 1 (the default, where the
+ * bricks tile into them) by regions of 8 x 8 x 4 bricks, so that the bricks in flight share their
+ * halo tiles and flushed density sectors in L2; 0 by rows (x fastest, then y, then z).  FP32 output
+ * is identical (fixed-point sums); FP64 sums may differ in the last bits (their atomics' order).
+ * Returns the previous setting.  No reference counterpart. */
+int mitos_set_lattice_order(int regions);
 
 #ifdef __cplusplus
 }

@@ -377,6 +377,12 @@ extern "C" int mitos_set_lattice_tma(int on) {
     return was;
 }
 
+extern "C" int mitos_set_lattice_order(int regions) {
+    const int was = lattice_region() ? 1 : 0;
+    set_lattice_region(regions != 0);
+    return was;
+}
+
 extern "C" int fft_r2c_dg(struct distributed_grid *dg) {
     const GridGeom *g = geom(dg->N, dg->precision);
     if (!g) return 3;

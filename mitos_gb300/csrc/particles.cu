@@ -349,7 +349,8 @@ template <typename T>
 __global__ void __launch_bounds__(LB_THREADS, 2)
 k_lattice_cic(int N, int rpd, int rpo, float spacing, float Lf, T ginv, const T *__restrict__ d0, const T *__restrict__ d1,
               const T *__restrict__ d2, T *__restrict__ rho, float *__restrict__ pos_out, size_t bstride, FastDiv div_bx,
-              FastDiv div_by, float *__restrict__ posraw_out, const __grid_constant__ LatticeMaps maps, int use_tma) {
+              FastDiv div_by, float *__restrict__ posraw_out, const __grid_constant__ LatticeMaps maps, int use_tma,
+              int region) {
     // batched launches: realisation blockIdx.y (its grids bstride bytes apart)
     if (gridDim.y > 1) {
         const size_t bo = (size_t)blockIdx.y * bstride;
@@ -369,6 +370,20 @@ k_lattice_cic(int N, int rpd, int rpo, float spacing, float Lf, T ginv, const T 
     for (int i = threadIdx.x; i < LR_X * LR_Y * LR_Z; i += LB_THREADS) reg[i] = 0;
     // brick b -> (bx, by, bz), x fastest
     auto decode = [&](int b, int &bx, int &by, int &bz) {
+        if (region) {
+            // regions of 8 x 8 x 4 bricks (64 x 64 x 128 cells), x fastest inside a region and
+            // across regions: the bricks in flight (about one region) share their halo rows and
+            // flushed sectors in every direction while those are still in L2
+            const int w = b & 255, r = b >> 8;
+            const int rq = (int)fdiv((unsigned)r, div_bx);  // div_bx: regions along x
+            const int rx = r - rq * (bx_n >> 3);
+            const int rz = (int)fdiv((unsigned)rq, div_by);  // div_by: regions along y
+            const int ry = rq - rz * (by_n >> 3);
+            bx = (rx << 3) + (w & 7);
+            by = (ry << 3) + ((w >> 3) & 7);
+            bz = (rz << 2) + (w >> 6);
+            return;
+        }
         const int q = (int)fdiv((unsigned)b, div_bx);
         bx = b - q * bx_n;
         bz = (int)fdiv((unsigned)q, div_by);
@@ -579,6 +594,11 @@ int lattice_fault_check() {
     return 6;
 }
 
+// brick order by 8 x 8 x 4 regions (on by default where the bricks tile into them)
+static bool g_lattice_region = true;
+void set_lattice_region(bool on) { g_lattice_region = on; }
+bool lattice_region() { return g_lattice_region; }
+
 // tensor-copy staging of the interior bricks (on by default; off: 16-byte cp.async for all)
 static bool g_lattice_tma = true;
 void set_lattice_tma(bool on) { g_lattice_tma = on; }
@@ -611,10 +631,13 @@ static int lattice_launch(int N, int rpd, int rpo, float spacing, float Lf, doub
                   encode_grid_map(&maps.m0, d0, f64, N, N, rpd, LB_Z, LB_Y, LB_X) &&
                   encode_grid_map(&maps.m1, d1, f64, N, N, rpd, LB_Z, LB_Y, T1X) &&
                   encode_grid_map(&maps.m2, d2, f64, N, N, rpd, LB_Z, T2Y, T1X);
+    // brick order: regions of 8 x 8 x 4 bricks where they tile the grid, else x, y, z rows
+    const int bxn = N / LB_X, byn = N / LB_Y, bzn = N / LB_Z;
+    const int region = g_lattice_region && bxn % 8 == 0 && byn % 8 == 0 && bzn % 4 == 0;
+    const FastDiv dx = make_fastdiv((unsigned)(region ? bxn / 8 : bxn)), dy = make_fastdiv((unsigned)(region ? byn / 8 : byn));
     kern<<<dim3(blocks, nb), LB_THREADS, smem, stream()>>>(N, rpd, rpo, spacing, Lf, (T)ginv, (const T *)d0,
                                                            (const T *)d1, (const T *)d2, (T *)rho, pos_out, bstride,
-                                                           make_fastdiv((unsigned)(N / LB_X)), make_fastdiv((unsigned)(N / LB_Y)),
-                                                           posraw_out, maps, use_tma);
+                                                           dx, dy, posraw_out, maps, use_tma, region);
     return 0;
 }
 

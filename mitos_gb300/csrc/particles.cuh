@@ -19,6 +19,9 @@ bool lattice_aligned(int N, int M, double boxlen);
 // tensor-copy staging of the deposit's interior bricks on (default) or off (16-byte cp.async)
 void set_lattice_tma(bool on);
 bool lattice_tma();
+// brick order of the deposit: 8 x 8 x 4 regions (default) or x, y, z rows (identical output in FP32)
+void set_lattice_region(bool on);
+bool lattice_region();
 // a deposit that stops because a tile copy never completed (bounded wait) sets a device flag:
 // lattice_fault_fetch queues its copy to the host behind the deposit; lattice_fault_check, once the
 // library stream is synchronised, returns 6 with the error message if it was set (and clears it)

@@ -131,7 +131,7 @@ EXPORTS = ["alloc_local_grid", "free_local_grid", "free_local_real_grid", "free_
            "ic_pipeline_run", "ic_pipeline_run_table", "mitos_timer_start", "mitos_timer_stop",
            "mitos_sync", "mitos_kernel_timing", "mitos_kernel_times", "mitos_stage_times",
            "mitos_ma_history", "mitos_rng_jump", "mitos_noise_column_state", "mitos_cr_log", "mitos_cr_cos",
-           "mitos_sample_norm_cr", "mitos_cr_steps", "snapshot_header_attributes", "manet_set_warm_grid", "mitos_set_radix", "mitos_get_radix", "mitos_set_cluster_fft", "mitos_set_lattice_tma"] + \
+           "mitos_sample_norm_cr", "mitos_cr_steps", "snapshot_header_attributes", "manet_set_warm_grid", "mitos_set_radix", "mitos_get_radix", "mitos_set_cluster_fft", "mitos_set_lattice_tma", "mitos_set_lattice_order"] + \
           ["kernel_" + k for k in KERNEL_NAMES]
 
 
@@ -723,3 +723,8 @@ def set_cluster_fft(mode: int) -> int:
 def set_lattice_tma(on: bool) -> bool:
     """tensor-copy staging of the lattice deposit's tiles on or off; the previous setting"""
     return bool(load().mitos_set_lattice_tma(1 if on else 0))
+
+
+def set_lattice_order(regions: bool) -> bool:
+    """the lattice deposit's brick order: 8 x 8 x 4 regions (True) or rows; the previous setting"""
+    return bool(load().mitos_set_lattice_order(1 if regions else 0))

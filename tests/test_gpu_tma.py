@@ -42,3 +42,22 @@ def test_tma_staging_bit_identical(N, L, prec):
     else:
         # FP64 deposit sums are shared-memory double atomics, whose order varies from run to run
         assert np.abs(r1["pk_p"][ok] / r0["pk_p"][ok] - 1).max() < 1e-12
+
+
+@pytest.mark.parametrize("N,L", [(256, 500.0), (512, 1000.0)])
+def test_region_order_bit_identical(N, L):
+    """the deposit's regional brick order against row order: the same particles into the same
+    fixed-point sums (FP32), so identical positions and P(k)"""
+    table = load_table()
+    spline = ml.Spline(table)
+    cfg = ml.ic_config(N, N, L, 5, table, pk_bins=32, pk_linear=True, precision=ml.FP32)
+    was = ml.set_lattice_order(True)
+    try:
+        r1 = ml.ic_pipeline_run(cfg, spline, want_pos=True)
+        ml.set_lattice_order(False)
+        r0 = ml.ic_pipeline_run(cfg, spline, want_pos=True)
+    finally:
+        ml.set_lattice_order(was)
+    assert np.array_equal(r1["pos"], r0["pos"])
+    ok = r1["pk_obs"] > 0
+    assert np.array_equal(r1["pk_p"][ok], r0["pk_p"][ok])
