@@ -17,7 +17,8 @@
  *     momentum space, 3 unsupported kernel callback or size, 4 CUDA error, 5 out of memory,
  *     6 bounded wait timed out, 7 no convergence, 8 invalid value drawn.  mitos_last_error()
  *     describes the last one.
- *   - Every entry point is synchronous on return (its work on the library stream is done).
+ *   - Every entry point is synchronous on return (its work on the library stream is done),
+ *     unless the calling thread chose asynchronous mode with mitos_set_stream.
  */
 #ifndef MITOS_GB300_H
 #define MITOS_GB300_H
@@ -556,6 +557,17 @@ int mitos_set_cluster_fft(int mode);
  * with 16-byte cp.async.  The results are identical.  Returns the previous setting.  No reference
  * counterpart. */
 int mitos_set_lattice_tma(int on);
+/* The stream the calling thread's entry points launch on: a caller's cudaStream_t, or NULL for the
+ * library's own stream (the default).  async = 1 with a caller's stream: the entry points that only
+ * transform device grids enqueue their work and return without synchronising (the *_async form of
+ * the reference entry points, e.g. for capture into the caller's CUDA graph): fft_r2c_dg,
+ * fft_c2r_dg, fft_apply_kernel_dg (any kernel but the transfer functions, whose spline rows come
+ * from the host), solvePoisson_dg, solve2LPT, generate_complex_grf, enforce_hermiticity,
+ * cic_deposit_dg (device positions).  Entry points that return host results or upload host data (the grid copies,
+ * P(k), the transfer-function kernels, the IC pipeline) still synchronise, so they cannot be
+ * captured.  The first call of an entry point for a grid size allocates its workspace and tables:
+ * make it once outside a capture.  Per thread; returns 0. */
+int mitos_set_stream(void *stream, int async);
 /* Order in which the lattice deposit's blocks walk its 8 x 8 x 32 bricks: 1 (the default, where the
  * bricks tile into them) by regions of 8 x 8 x 4 bricks, so that the bricks in flight share their
  * halo tiles and flushed density sectors in L2; 0 by rows (x fastest, then y, then z).  FP32 output

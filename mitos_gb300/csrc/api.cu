@@ -19,7 +19,13 @@ static inline size_t grid_bytes(const struct distributed_grid *dg) {
     return (size_t)dg->local_size * csize(dg->precision);
 }
 
+// the end of a synchronous entry point; a caller's stream in asynchronous mode (mitos_set_stream)
+// gets the work enqueued only
 static int sync_all() {
+    if (async_mode()) {
+        const cudaError_t ce = cudaGetLastError();
+        return ce == cudaSuccess ? 0 : check_cuda(ce, "an asynchronous entry point");
+    }
     MITOS_CUDA(cudaStreamSynchronize(stream()));
     return 0;
 }
@@ -265,7 +271,8 @@ extern "C" int alloc_local_grid_prec(struct distributed_grid *dg, int N, double 
     cudaMemsetAsync(r, 0, b, stream());
     dg->fbox = (mitos_c128 *)f;
     dg->box = (double *)r;
-    return sync_all();
+    MITOS_CUDA(cudaStreamSynchronize(stream()));  // the grid is ready for any stream
+    return 0;
 }
 
 extern "C" int alloc_local_grid(struct distributed_grid *dg, int N, double boxlen, MPI_Comm comm) {
@@ -290,7 +297,8 @@ extern "C" int dg_copy_to_host(const struct distributed_grid *dg, int which, voi
     const void *src = which == 0 ? (const void *)dg->fbox : (const void *)dg->box;
     if (!src) { set_error(1, "grid part not allocated"); return 1; }
     MITOS_CUDA(cudaMemcpyAsync(host, src, grid_bytes(dg), cudaMemcpyDeviceToHost, stream()));
-    return sync_all();
+    MITOS_CUDA(cudaStreamSynchronize(stream()));  // host memory: synchronous in either mode
+    return 0;
 }
 // writeHeaderAttributes (src/header.c:26-175): the values of its attributes, without the HDF5 calls
 extern "C" int snapshot_header_attributes(double boxlen, double z_ini, int num_types, const char *const *export_names,
@@ -338,13 +346,15 @@ extern "C" int dg_field_to_host(const struct distributed_grid *dg, double *host)
         if (e) return e;
         MITOS_CUDA(cudaMemcpyAsync(host, t, sizeof(double) * n, cudaMemcpyDeviceToHost, stream()));
     }
-    return sync_all();
+    MITOS_CUDA(cudaStreamSynchronize(stream()));  // host memory: synchronous in either mode
+    return 0;
 }
 extern "C" int dg_copy_from_host(struct distributed_grid *dg, int which, const void *host) {
     void *dst = which == 0 ? (void *)dg->fbox : (void *)dg->box;
     if (!dst) { set_error(1, "grid part not allocated"); return 1; }
     MITOS_CUDA(cudaMemcpyAsync(dst, host, grid_bytes(dg), cudaMemcpyHostToDevice, stream()));
-    return sync_all();
+    MITOS_CUDA(cudaStreamSynchronize(stream()));  // host memory: synchronous in either mode
+    return 0;
 }
 
 // ==== FFT ===================================================================================
@@ -369,6 +379,12 @@ extern "C" int mitos_set_cluster_fft(int mode) {
     const int was = cluster_fft();
     set_cluster_fft(mode >= 0 && mode <= 3 ? mode : 0);
     return was;
+}
+
+extern "C" int mitos_set_stream(void *s, int async) {
+    set_stream((cudaStream_t)s);
+    set_async(s != nullptr && async != 0);
+    return 0;
 }
 
 extern "C" int mitos_set_lattice_tma(int on) {

@@ -64,6 +64,8 @@ __device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefe
 cudaStream_t stream();
 int library_device();                 // the device the library stream was created on
 void set_stream(cudaStream_t s);      // this thread's launches go to s (nullptr: the library stream)
+void set_async(bool on);              // this thread's entry points return without synchronising
+bool async_mode();
 void set_workspace_set(int s);        // this thread's workspace() buffers come from set s
 void count_launch(int n = 1);
 void launch_begin(const char *name);  // pairs with count_launch for per-launch timing

@@ -55,6 +55,9 @@ int library_device() {
     return g_stream_dev;
 }
 void set_stream(cudaStream_t s) { t_stream = s; }
+static thread_local bool t_async = false;
+void set_async(bool on) { t_async = on; }
+bool async_mode() { return t_async; }
 void set_workspace_set(int s) { t_ws_set = s; }
 
 // optional per-launch timing: events recorded on the library stream around every launch

@@ -131,7 +131,7 @@ EXPORTS = ["alloc_local_grid", "free_local_grid", "free_local_real_grid", "free_
            "ic_pipeline_run", "ic_pipeline_run_table", "mitos_timer_start", "mitos_timer_stop",
            "mitos_sync", "mitos_kernel_timing", "mitos_kernel_times", "mitos_stage_times",
            "mitos_ma_history", "mitos_rng_jump", "mitos_noise_column_state", "mitos_cr_log", "mitos_cr_cos",
-           "mitos_sample_norm_cr", "mitos_cr_steps", "snapshot_header_attributes", "manet_set_warm_grid", "mitos_set_radix", "mitos_get_radix", "mitos_set_cluster_fft", "mitos_set_lattice_tma", "mitos_set_lattice_order"] + \
+           "mitos_sample_norm_cr", "mitos_cr_steps", "snapshot_header_attributes", "manet_set_warm_grid", "mitos_set_radix", "mitos_get_radix", "mitos_set_cluster_fft", "mitos_set_lattice_tma", "mitos_set_lattice_order", "mitos_set_stream"] + \
           ["kernel_" + k for k in KERNEL_NAMES]
 
 
@@ -728,3 +728,10 @@ def set_lattice_tma(on: bool) -> bool:
 def set_lattice_order(regions: bool) -> bool:
     """the lattice deposit's brick order: 8 x 8 x 4 regions (True) or rows; the previous setting"""
     return bool(load().mitos_set_lattice_order(1 if regions else 0))
+
+
+def set_stream(stream_handle: int = 0, asynchronous: bool = False) -> None:
+    """launch this thread's library work on a caller's CUDA stream (its handle, e.g.
+    torch.cuda.Stream().cuda_stream; 0: the library's stream); asynchronous: return without
+    synchronising (device-only entry points)"""
+    _check(load().mitos_set_stream(ctypes.c_void_p(stream_handle or None), 1 if asynchronous else 0))
