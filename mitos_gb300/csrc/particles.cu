@@ -449,6 +449,7 @@ k_lattice_cic(int N, int rpd, int rpo, float spacing, float Lf, T ginv, const T 
             // a tensor copy that never completed: flag it, let the next brick's copy finish (bounded)
             // and stop
             if (threadIdx.x == 0) atomicExch(&g_lattice_fault, 1);
+            if (by_tma(bx, by)) mbar_wait(bars + buf, ((phase >> buf) & 1u) ^ 1u);  // once more, bounded
             if (next_tma) mbar_wait(bars + (buf ^ 1), (phase >> (buf ^ 1)) & 1u);
             cp_async_wait_all();
             return;
@@ -820,22 +821,49 @@ __global__ void k_vel_gather(long np, int N, int pitch, T boxlen, const float *_
 #define VR_Z (VB_Z + 8)
 #define VR_Z0 4
 
-static size_t vel_tiled_smem(size_t elem) { return 3 * elem * (size_t)VR_X * VR_Y * VR_Z; }
+// the three tiles plus the tensor copies' mbarrier
+static size_t vel_tiled_smem(size_t elem) { return 3 * elem * (size_t)VR_X * VR_Y * VR_Z + sizeof(uint64_t); }
 
+// tensor maps of the three velocity grids, box {VR_Z, VR_Y, VR_X} (z innermost)
+struct VelMaps {
+    CUtensorMap m[3];
+};
+
+// Bricks whose tiles stay inside the box (not on a face in x, y or z) are staged by three tensor
+// copies from one thread on an mbarrier; the others, whose halos wrap, by 16-byte cp.async.
 template <typename T>
 __global__ void __launch_bounds__(VB_THREADS) k_vel_gather_tiled(int N, int pitch, T boxlen, const float *__restrict__ pos,
                                                                  const T *__restrict__ v0, const T *__restrict__ v1,
                                                                  const T *__restrict__ v2, float *__restrict__ vel,
-                                                                 FastDiv div_bx, FastDiv div_by) {
+                                                                 FastDiv div_bx, FastDiv div_by,
+                                                                 const __grid_constant__ VelMaps maps, int use_tma) {
     extern __shared__ __align__(16) unsigned char smraw[];
     T *tile = reinterpret_cast<T *>(smraw);  // [grid][VR_X][VR_Y][VR_Z]
-    const int bx_n = N / VB_X, by_n = N / VB_Y;
+    const int bx_n = N / VB_X, by_n = N / VB_Y, bz_n = N / VB_Z;
     const unsigned b = blockIdx.x;
     const unsigned q = fdiv(b, div_bx);
     const int bx = (int)(b - q * bx_n), bz = (int)fdiv(q, div_by), by = (int)(q - bz * by_n);
     const int x0 = bx * VB_X, y0 = by * VB_Y, z0 = bz * VB_Z;
     const long rp = pitch;
-    {
+    constexpr int TILE = VR_X * VR_Y * VR_Z;
+    const bool tma = use_tma && bx > 0 && bx < bx_n - 1 && by > 0 && by < by_n - 1 && bz > 0 && bz < bz_n - 1 &&
+                     (smem_u32(tile) & 127) == 0;
+    if (tma) {
+        uint64_t *bar = reinterpret_cast<uint64_t *>(tile + 3 * TILE);
+        if (threadIdx.x == 0) {
+            mbar_init(bar, 1);
+            mbar_init_fence();
+            mbar_expect_tx(bar, (unsigned)(3 * TILE * sizeof(T)));
+            for (int g = 0; g < 3; g++) tma_load_3d(tile + g * TILE, &maps.m[g], z0 - VR_Z0, y0 - 1, x0 - 1, bar);
+        }
+        __syncthreads();  // the barrier is initialised before anyone polls it
+        const bool ok = mbar_wait(bar, 0);
+        if (__syncthreads_or(!ok)) {  // a copy that never completed: flag it, wait once more (bounded), stop
+            if (threadIdx.x == 0) atomicExch(&g_lattice_fault, 1);
+            mbar_wait(bar, 0);
+            return;
+        }
+    } else {
         constexpr int CH = 16 / sizeof(T), RC = VR_Z / CH, ROWS = VR_X * VR_Y;
         for (int c = threadIdx.x; c < 3 * ROWS * RC; c += VB_THREADS) {
             const int g = c / (ROWS * RC), r = (c / RC) % ROWS, ch = c % RC;
@@ -877,15 +905,24 @@ int velocity_gather(long np, int N, int pitch, double boxlen, int precision, con
         const size_t smem = vel_tiled_smem(es);
         const unsigned nb = (unsigned)((N / VB_X) * (N / VB_Y) * (N / VB_Z));
         const FastDiv dbx = make_fastdiv((unsigned)(N / VB_X)), dby = make_fastdiv((unsigned)(N / VB_Y));
+        VelMaps maps;
+        memset(&maps, 0, sizeof maps);
+        const bool f64 = precision != MITOS_FP32;
+        const void *vg[3] = {v0, v1, v2};
+        int use_tma = lattice_tma() ? 1 : 0;
+        for (int gi = 0; gi < 3 && use_tma; gi++)
+            use_tma = encode_grid_map(&maps.m[gi], vg[gi], f64, N, N, pitch, VR_Z, VR_Y, VR_X) ? 1 : 0;
         launch_begin("vel_gather");
         if (precision == MITOS_FP32) {
             MITOS_CUDA(cudaFuncSetAttribute(k_vel_gather_tiled<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             k_vel_gather_tiled<float><<<nb, VB_THREADS, smem, stream()>>>(N, pitch, (float)boxlen, pos, (const float *)v0,
-                                                                          (const float *)v1, (const float *)v2, vel, dbx, dby);
+                                                                          (const float *)v1, (const float *)v2, vel, dbx, dby,
+                                                                          maps, use_tma);
         } else {
             MITOS_CUDA(cudaFuncSetAttribute(k_vel_gather_tiled<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             k_vel_gather_tiled<double><<<nb, VB_THREADS, smem, stream()>>>(N, pitch, boxlen, pos, (const double *)v0,
-                                                                           (const double *)v1, (const double *)v2, vel, dbx, dby);
+                                                                           (const double *)v1, (const double *)v2, vel, dbx, dby,
+                                                                           maps, use_tma);
         }
         count_launch();
         MITOS_LAUNCH_CHECK("velocity gather (tiled)");

@@ -426,7 +426,6 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     if (!aligned) MITOS_CUDA(cudaMemsetAsync(rhoD, 0, rho_bytes, stream()));
     e = aligned ? lattice_deposit(N, L, prec, D0, D1, D2, disp_pitch, rhoD, rho_pitch, dpos, B, bs, dposraw)
                 : displace_and_deposit(N, M, L, prec, D0, D1, D2, rhoD, dpos, dposraw);
-    if (!e && aligned && !(opt && opt->graph)) e = lattice_fault_fetch();
     if (e) return e;
     if (res && res->pos) {
         MITOS_CUDA(cudaEventRecord(pos_event(pslot, 0), stream()));
@@ -547,6 +546,12 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
         MITOS_CUDA(cudaEventRecord(pos_event(pslot, 1), copy_stream()));
     }
 
+    // the deposit's and the velocity gather's tile-copy fault flag to the host (read after the
+    // final synchronisation)
+    if (aligned && !(opt && opt->graph)) {
+        e = lattice_fault_fetch();
+        if (e) return e;
+    }
     // S6: overdensity r2c, CIC window undo, P(k) (analyse/src/mitos_read.c:364-419)
     const int *bins = bin_table(N, cfg->pk_bins, cfg->pk_linear, L);
     if (!bins) return 5;

@@ -61,3 +61,24 @@ def test_region_order_bit_identical(N, L):
     assert np.array_equal(r1["pos"], r0["pos"])
     ok = r1["pk_obs"] > 0
     assert np.array_equal(r1["pk_p"][ok], r0["pk_p"][ok])
+
+
+@pytest.mark.parametrize("N,L,prec", [(128, 256.0, ml.FP32), (128, 256.0, ml.FP64), (256, 500.0, ml.FP32)])
+def test_velocity_gather_tma_bit_identical(N, L, prec):
+    """the velocity gather's interior bricks staged by tensor copies against cp.async for all:
+    the same tiles, identical velocities (src/mitos.c:865-908)"""
+    table = load_table()
+    spline = ml.Spline(table)
+    cfg = ml.ic_config(N, N, L, 8, table, pk_bins=16, pk_linear=True, precision=prec,
+                       index_vel=table.index_of("t_cdm"))
+    was = ml.set_lattice_tma(True)
+    try:
+        assert "vel_gather" in _names(lambda: ml.ic_pipeline_run(cfg, spline, want_vel=True))
+        r1 = ml.ic_pipeline_run(cfg, spline, want_pos=True, want_vel=True)
+        ml.set_lattice_tma(False)
+        r0 = ml.ic_pipeline_run(cfg, spline, want_pos=True, want_vel=True)
+    finally:
+        ml.set_lattice_tma(was)
+    assert np.array_equal(r1["pos"], r0["pos"])
+    assert np.array_equal(r1["vel"], r0["vel"])
+    assert np.abs(r1["vel"]).max() > 0
