@@ -228,10 +228,20 @@ __global__ void __launch_bounds__(512, 2) k_x_combine_disp(GridGeom g, PassArgs 
     const size_t bo = (size_t)blockIdx.y * (size_t)a.bstride;
     const cplx<T> *src = bat<const cplx<T>>(a.in[0], bo);
     const cplx<T> *phi1 = bat<const cplx<T>>(a.in2, bo);
-    // phi_1 is read after the forward transform: start its sectors towards L2 now (measured at
-    // 512^3: 0.81 ms against 0.86)
+    // phi_1 is read after the forward transform: its elements go to shared memory by cp.async now
+    // ([e][thread], behind the exchange buffer; each thread reads back only its own copies), so the
+    // loads overlap the transform.  (An L2 prefetch instead: 0.81 ms at 512^3, none: 0.86.)
+    cplx<T> *ph = sm + (long)P * spad_len(N) + threadIdx.x;
 #pragma unroll
-    for (int e = 0; e < E; e++) prefetch_l2(phi1 + col + (long)nout_any<NL, E>(pl, t, e) * g.plane);
+    for (int e = 0; e < E; e++) {
+        const cplx<T> *src1 = phi1 + col + (long)nout_any<NL, E>(pl, t, e) * g.plane;
+        const unsigned d = (unsigned)__cvta_generic_to_shared(ph + e * blockDim.x);
+        if (sizeof(cplx<T>) == 8)
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src1) : "memory");
+        else
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src1) : "memory");
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
     cplx<T> v[E];
 #pragma unroll
     for (int e = 0; e < E; e++) v[e] = valid ? src[col + (long)nin_any<NL, E>(pl, t, e) * g.plane] : mk<T>(0, 0);
@@ -243,7 +253,8 @@ __global__ void __launch_bounds__(512, 2) k_x_combine_disp(GridGeom g, PassArgs 
         const int jx = kint(n, N);
         const int n2 = jx * jx + iy * iy + iz * iz;  // int: see the strided X passes
         const T G = (n2 > 0) ? (T)-1 / ((T)n2 * dk * dk) : (T)1;
-        const cplx<T> q = valid ? phi1[col + (long)n * g.plane] : mk<T>(0, 0);
+        if (e == 0) asm volatile("cp.async.wait_all;" ::: "memory");
+        const cplx<T> q = valid ? ph[e * blockDim.x] : mk<T>(0, 0);
         const cplx<T> r = cscale<T>(v[e], scale);
         cplx<T> o = mk<T>(f1 * q.x + f2 * G * r.x, f1 * q.y + f2 * G * r.y);
         if (win) o = cscale<T>(o, win[jx + N / 2] * wyz);
@@ -646,7 +657,8 @@ int launch_x_t(const GridGeom &g, XOp op, int sign, const PassArgs &a) {
     case XOP_COMBINE_DISP: {
         const int P = PC > 0 ? PC : g.P_xy;
         const int threads = P * (g.N / g.E);
-        const size_t smem = (size_t)P * spad_len(g.N) * sizeof(cplx<T>);
+        // the exchange buffer, then phi_1's elements of every thread
+        const size_t smem = (size_t)P * spad_len(g.N) * sizeof(cplx<T>) + (size_t)threads * g.E * sizeof(cplx<T>);
         const long blocks = (g.plane + P - 1) / P;
         launch_begin("x_combine_disp");
         if (NL > 0 || g.E == 8) {
