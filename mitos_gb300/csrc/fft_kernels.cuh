@@ -87,6 +87,25 @@ __global__ void __launch_bounds__(strided_threads<AXIS, OP, NL, PC, E>(), stride
         __syncthreads();
     }
 
+    // the forward X passes that combine with a second grid (2LPT combine, Monge-Ampere update) read
+    // it after their transform: its elements go to shared memory by cp.async first ([e][thread],
+    // behind the exchange buffer; each thread reads back only its own copies)
+    constexpr bool STAGE2 = AXIS == 0 && (OP == XOP_COMBINE_2LPT || OP == XOP_ADD_POISSON);
+    cplx<T> *ph = sm + (long)P * spad_len(N) + threadIdx.x;
+    if constexpr (STAGE2) {
+        const cplx<T> *in2 = bat<const cplx<T>>(a.in2, bo);
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+            const cplx<T> *s2 = in2 + base + (long)nout_any<NL, E>(pl, t, e) * stride;
+            const unsigned d = (unsigned)__cvta_generic_to_shared(ph + e * blockDim.x);
+            if (sizeof(cplx<T>) == 8)
+                asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(s2) : "memory");
+            else
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(s2) : "memory");
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    }
+
     constexpr int NIN = 1;
     cplx<T> raw[E];
     cplx<T> v[E];
@@ -133,6 +152,7 @@ __global__ void __launch_bounds__(strided_threads<AXIS, OP, NL, PC, E>(), stride
             }
             fft_any<T, E, SIGN, NL, PC>(pl, v, psm, P, t, tw);
             // the P(k) epilogue keeps the whole warp together (warp-level bin sums)
+            if constexpr (STAGE2) asm volatile("cp.async.wait_all;" ::: "memory");  // every thread
             if (!valid && OP != XOP_PK) continue;
             cplx<T> *dst = bat<cplx<T>>(a.out[outs[m]], bo);
 #pragma unroll
@@ -170,7 +190,7 @@ __global__ void __launch_bounds__(strided_threads<AXIS, OP, NL, PC, E>(), stride
                     } else {
                         const T kk2 = (T)n2 * dk * dk;
                         const T G = (n2 > 0) ? (T)-1 / kk2 : (T)1;
-                        const cplx<T> q = bat<const cplx<T>>(a.in2, bo)[idx];
+                        const cplx<T> q = ph[e * blockDim.x];
                         cplx<T> o;
                         if constexpr (OP == XOP_COMBINE_2LPT) {
                             const T f1 = parg<T>(a.f1, a.ff1), f2 = parg<T>(a.f2, a.ff2);
@@ -337,7 +357,6 @@ __global__ void __launch_bounds__(256, (OP == ZOP_HESS_MA || OP == ZOP_HESS_MA_K
     const T scale = S2 ? (T)a.scale : parg<T>(a.scale, a.fscale);
     cplx<T> *psm = sm + (long)p * spad_len(h);
     const size_t bo = (size_t)blockIdx.y * (size_t)a.bstride;
-
     constexpr int NIN = (OP == ZOP_C2R) ? 1 : (OP == ZOP_DISP) ? 3 : 6;
     // inputs of the Hessian passes are [xx, xy, xz, yy, yz, zz]; the 2LPT source is accumulated
     // in the reference's term order (src/2lpt.c:111-112): zz yy + zz xx + yy xx - xy^2 - yz^2 - xz^2.
@@ -618,6 +637,7 @@ static int launch_strided_e(const GridGeom &g, const PassArgs &a, const T *win) 
     const int threads = P * (g.N / E);
     size_t smem = (size_t)P * spad_len(g.N) * sizeof(cplx<T>);
     if (OP == XOP_PK && AXIS == 0) smem += (size_t)a.nbins * (threads / 32) * sizeof(T);
+    if ((OP == XOP_COMBINE_2LPT || OP == XOP_ADD_POISSON) && AXIS == 0) smem += (size_t)threads * E * sizeof(cplx<T>);
     long blocks = (AXIS == 0) ? (g.plane + P - 1) / P : (long)g.N * ((g.H + P - 1) / P);
     auto kern = k_strided<T, E, SIGN, AXIS, OP, NL, PC>;
     if (smem > 48 * 1024) MITOS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
