@@ -5,7 +5,7 @@ whose grids still exceed L2 but whose device footprint stays at a few GB:
     python -m mitos_gb300.cases ngenic 512   # the N-GenIC-like field (k_ngenic)
     python -m mitos_gb300.cases ma 256       # Monge-Ampere cycles (z_hess_ma, x_add_poisson)
     python -m mitos_gb300.cases noise 512    # white noise (k_noise), FP32 (noise64: FP64)
-    python -m mitos_gb300.cases ic 256       # one FP32 initial condition (every pass)
+    python -m mitos_gb300.cases ic 256       # one FP32 initial condition (every pass; ic64: FP64)
     python -m mitos_gb300.cases ensemble 0 3 # the 48 realisations (16 each of 64^3, 96^3, 128^3) as
                                              # one graph; the size argument is unused
     python -m mitos_gb300.cases r2c 512 3 2  # fft_r2c_dg, FP32; fourth argument: the cluster mode
@@ -81,10 +81,10 @@ def noise(N: int, reps: int, prec: int = ml.FP32) -> float:
     return ms
 
 
-def ic(N: int, reps: int) -> float:
+def ic(N: int, reps: int, prec: int = ml.FP32) -> float:
     table = load_table()
     spline = ml.Spline(table)
-    cfg = lambda s: ml.ic_config(N, N, 1000.0 * N / 512, s, table, pk_bins=64, pk_linear=True, precision=ml.FP32)
+    cfg = lambda s: ml.ic_config(N, N, 1000.0 * N / 512, s, table, pk_bins=64, pk_linear=True, precision=prec)
     ml.ic_pipeline_run(cfg(1), spline)
     ml.timer_start()
     for r in range(reps):
@@ -122,7 +122,11 @@ def noise64(N: int, reps: int) -> float:
     return noise(N, reps, ml.FP64)
 
 
-CASES = {"conv": conv, "ngenic": ngenic, "ma": ma, "noise": noise, "noise64": noise64, "ic": ic, "r2c": r2c, "ensemble": ensemble}
+def ic64(N: int, reps: int) -> float:
+    return ic(N, reps, ml.FP64)
+
+
+CASES = {"conv": conv, "ngenic": ngenic, "ma": ma, "noise": noise, "noise64": noise64, "ic": ic, "ic64": ic64, "r2c": r2c, "ensemble": ensemble}
 
 if __name__ == "__main__":
     name = sys.argv[1]
