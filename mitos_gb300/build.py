@@ -13,7 +13,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmitos_gb300.so")
 
 SOURCES = ["context.cu", "noise.cu", "kspace.cu", "fft_passes.cu", "particles.cu", "api.cu", "pipeline.cu", "noalloc.cu",
-           "fft_ct64.cu", "fft_ct128.cu", "fft_ct256.cu", "fft_ct512.cu", "fft_ct1024.cu", "fft_cluster.cu", "manet.cu", "ma.cu", "ensemble.cu", "ngenic.cu",
+           "fft_ct64.cu", "fft_ct96.cu", "fft_ct128.cu", "fft_ct256.cu", "fft_ct512.cu", "fft_ct1024.cu", "fft_cluster.cu", "manet.cu", "ma.cu", "ensemble.cu", "ngenic.cu",
            "bispectrum.cu", "thermal.cu"]
 # files whose FP64 arithmetic follows the reference operation by operation: no FMA contraction
 NO_FMAD = {"kspace.cu"}

@@ -651,7 +651,8 @@ static int launch_strided_e(const GridGeom &g, const PassArgs &a, const T *win) 
 
 template <typename T, int SIGN, int AXIS, int OP, int NL, int PC>
 static int launch_strided(const GridGeom &g, const PassArgs &a, const T *win) {
-    if constexpr (NL > 0) return launch_strided_e<T, 8, SIGN, AXIS, OP, NL, PC>(g, a, win);
+    // the compile-time lengths: 8 elements a thread for 2^k, 12 for 3 2^k
+    if constexpr (NL > 0) return launch_strided_e<T, (NL % 3 == 0 ? 12 : 8), SIGN, AXIS, OP, NL, PC>(g, a, win);
     else {
         if (g.E == 8) return launch_strided_e<T, 8, SIGN, AXIS, OP, 0, 0>(g, a, win);
         return launch_strided_e<T, 12, SIGN, AXIS, OP, 0, 0>(g, a, win);
@@ -682,7 +683,7 @@ int launch_x_t(const GridGeom &g, XOp op, int sign, const PassArgs &a) {
         const long blocks = (g.plane + P - 1) / P;
         launch_begin("x_combine_disp");
         if (NL > 0 || g.E == 8) {
-            auto kern = k_x_combine_disp<T, 8, NL, PC>;
+            auto kern = k_x_combine_disp<T, (NL > 0 && NL % 3 == 0 ? 12 : 8), NL, PC>;
             if (smem > 48 * 1024) MITOS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             kern<<<dim3((unsigned)blocks, a.batch > 1 ? a.batch : 1), threads, smem, stream()>>>(g, with_f32(a), win);
         } else {
@@ -733,15 +734,16 @@ static int launch_zc_e(const GridGeom &g, const PassArgs &a) {
 
 template <typename T, int NLZ>
 int launch_zc_t(const GridGeom &g, ZOp op, const PassArgs &a) {
+    constexpr int EC = (NLZ > 0 && NLZ % 3 == 0) ? 12 : 8;  // the compile-time lengths' elements
     if (NLZ > 0 || g.E == 8) {
         switch (op) {
-        case ZOP_C2R: return launch_zc_e<T, 8, ZOP_C2R, NLZ>(g, a);
-        case ZOP_HESS_2LPT: return launch_zc_e<T, 8, ZOP_HESS_2LPT, NLZ>(g, a);
-        case ZOP_HESS_MA: return launch_zc_e<T, 8, ZOP_HESS_MA, NLZ>(g, a);
-        case ZOP_DISP: return launch_zc_e<T, 8, ZOP_DISP, NLZ>(g, a);
-        case ZOP_HESS_2LPT_K: return launch_zc_e<T, 8, ZOP_HESS_2LPT_K, NLZ>(g, a);
-        case ZOP_HESS_MA_K: return launch_zc_e<T, 8, ZOP_HESS_MA_K, NLZ>(g, a);
-        case ZOP_HESS_MA_KS: return launch_zc_e<T, 8, ZOP_HESS_MA_KS, NLZ>(g, a);
+        case ZOP_C2R: return launch_zc_e<T, EC, ZOP_C2R, NLZ>(g, a);
+        case ZOP_HESS_2LPT: return launch_zc_e<T, EC, ZOP_HESS_2LPT, NLZ>(g, a);
+        case ZOP_HESS_MA: return launch_zc_e<T, EC, ZOP_HESS_MA, NLZ>(g, a);
+        case ZOP_DISP: return launch_zc_e<T, EC, ZOP_DISP, NLZ>(g, a);
+        case ZOP_HESS_2LPT_K: return launch_zc_e<T, EC, ZOP_HESS_2LPT_K, NLZ>(g, a);
+        case ZOP_HESS_MA_K: return launch_zc_e<T, EC, ZOP_HESS_MA_K, NLZ>(g, a);
+        case ZOP_HESS_MA_KS: return launch_zc_e<T, EC, ZOP_HESS_MA_KS, NLZ>(g, a);
         }
     } else {
         switch (op) {
@@ -775,7 +777,7 @@ static int launch_zr_e(const GridGeom &g, const PassArgs &a) {
 
 template <typename T, int NLZ>
 int launch_zr_t(const GridGeom &g, const PassArgs &a) {
-    if (NLZ > 0 || g.E == 8) return launch_zr_e<T, 8, NLZ>(g, a);
+    if (NLZ > 0 || g.E == 8) return launch_zr_e<T, (NLZ > 0 && NLZ % 3 == 0 ? 12 : 8), NLZ>(g, a);
     return launch_zr_e<T, 12, 0>(g, a);
 }
 
