@@ -8,6 +8,7 @@
 // over its 8 cells, so the overdensity is the deposited value minus one.
 #include <math.h>
 #include <stdint.h>
+#include <string.h>
 
 #include <algorithm>
 
