@@ -261,9 +261,17 @@ template <int NL, int SN> __device__ __forceinline__ int xpos(int i) {
 template <int NL, int E, int SN> constexpr bool warp_pencil() {
     return SN == 1 && NL / E <= 32 && 32 % (NL / E) == 0;
 }
+// A pencil of whole warps whose threads are contiguous (SN == 1, NL / E a multiple of 32: the Z
+// passes of N = 1024, two warps a row) synchronises on a named barrier of its own warps, id 1 + its
+// index in the block (the Z tiles hold at most 256 threads, so at most 4 such pencils).
 template <int NL, int E, int SN> __device__ __forceinline__ void pencil_sync() {
-    if constexpr (warp_pencil<NL, E, SN>()) __syncwarp();
-    else __syncthreads();
+    if constexpr (warp_pencil<NL, E, SN>()) {
+        __syncwarp();
+    } else if constexpr (NL > 0 && SN == 1 && (NL / E) % 32 == 0) {
+        asm volatile("bar.sync %0, %1;" ::"r"(1 + (int)threadIdx.x / (NL / E)), "n"(NL / E) : "memory");
+    } else {
+        __syncthreads();
+    }
 }
 
 template <typename T, int E, int SIGN, int NL, int SN, int S>
