@@ -100,6 +100,7 @@ bool plan_from_radices(int n, int E, int tw_len, const int *rad, int ns, FFTPlan
     pl->n = n;
     pl->nst = ns;
     pl->tw_scale = tw_len / n;
+    pl->twst = nullptr;
     int Ns = 1;
     for (int i = 0; i < ns; i++) {
         pl->rad[i] = rad[i];
@@ -140,7 +141,37 @@ static int elems_for(int N) {
 struct GeomEntry {
     GridGeom g;
     void *tw = nullptr;
+    void *twst[2] = {nullptr, nullptr};  // the stage twiddle tables of plN and plH
 };
+
+// the stage table of a plan (FFTPlan::twst) from the double twiddle table tw (length N, of the
+// grid), in the grid's precision: the values the table twN holds, regrouped per stage and butterfly
+static void *stage_twiddles(const FFTPlan &pl, const std::vector<double> &tw, int precision) {
+    std::vector<double> st;
+    int Ns = pl.rad[0];
+    for (int s = 1; s < pl.nst; s++) {
+        const int R = pl.rad[s], TR = tw_row(R);
+        for (int jm = 0; jm < Ns; jm++)
+            for (int k = 0; k < TR; k++) {
+                const int r = k + 1;
+                const long idx = r < R ? (long)r * jm * (pl.n / (Ns * R)) * pl.tw_scale : 0;
+                st.push_back(r < R ? tw[2 * idx] : 0.0);
+                st.push_back(r < R ? tw[2 * idx + 1] : 0.0);
+            }
+        Ns *= R;
+    }
+    if (st.empty()) st.assign(4, 0.0);
+    void *d = nullptr;
+    if (precision == MITOS_FP32) {
+        std::vector<float> f(st.begin(), st.end());
+        if (cudaMalloc(&d, sizeof(float) * f.size()) != cudaSuccess) return nullptr;
+        cudaMemcpy(d, f.data(), sizeof(float) * f.size(), cudaMemcpyHostToDevice);
+    } else {
+        if (cudaMalloc(&d, sizeof(double) * st.size()) != cudaSuccess) return nullptr;
+        cudaMemcpy(d, st.data(), sizeof(double) * st.size(), cudaMemcpyHostToDevice);
+    }
+    return d;
+}
 static std::map<std::pair<int, int>, GeomEntry *> g_geoms;
 
 const GridGeom *geom(int N, int precision) {
@@ -192,6 +223,16 @@ const GridGeom *geom(int N, int precision) {
         cudaMemcpy(ge->tw, tw.data(), sizeof(double) * 2 * N, cudaMemcpyHostToDevice);
     }
     g.twN = ge->tw;
+    ge->twst[0] = stage_twiddles(g.plN, tw, precision);
+    ge->twst[1] = stage_twiddles(g.plH, tw, precision);
+    if (!ge->twst[0] || !ge->twst[1]) {
+        cudaGetLastError();
+        delete ge;
+        set_error(5, "stage twiddles");
+        return nullptr;
+    }
+    g.plN.twst = ge->twst[0];
+    g.plH.twst = ge->twst[1];
     g_geoms[key] = ge;
     return &ge->g;
 }
@@ -236,6 +277,9 @@ int set_radix(int N, int precision, const int *rad_n, int ns_n, const int *rad_h
             if (a.rad[i] != b.rad[i]) return false;
         return true;
     };
+    // the stage tables belong to the default schedules, the only ones the compile-time kernels run
+    pn.twst = g->plN.twst;
+    ph.twst = g->plH.twst;
     g->plN = pn;
     g->plH = ph;
     g->custom_radix = !(same(pn, dn) && same(ph, dh));

@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(THREADS, THREADS == 256 ? 2 : 1) k_zy_r2c_clus
 #pragma unroll
             for (int zi = 0; zi < S::ZB; zi++) {
                 const int y = r * S::RPC + (z0 + zi) * S::RZ + pr;
-                fft_regs_ct<T, 8, -1, S::H2, 1>(v[zi], zs, tz, tw, g.plH.tw_scale);
+                fft_regs_ct<T, 8, -1, S::H2, 1>(v[zi], zs, tz, reinterpret_cast<const cplx<T> *>(g.plH.twst));
 #pragma unroll
                 for (int e = 0; e < 8; e++) zs[xpos<S::H2, 1>(n_out_ct<S::H2, 8>(tz, e))] = v[zi][e];
                 pencil_sync<S::H2, 8, 1>();
@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(THREADS, THREADS == 256 ? 2 : 1) k_zy_r2c_clus
             cplx<T> w[8];
 #pragma unroll
             for (int e = 0; e < 8; e++) w[e] = col[n_in_ct<NL, 8>(ty, e)];
-            fft_regs_ct<T, 8, -1, NL, P>(w, scr + p, ty, tw, g.plN.tw_scale);
+            fft_regs_ct<T, 8, -1, NL, P>(w, scr + p, ty, reinterpret_cast<const cplx<T> *>(g.plN.twst));
             const bool packed = r == 0 && j == 0;
 #pragma unroll
             for (int e = 0; e < 8; e++) {

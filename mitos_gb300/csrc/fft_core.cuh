@@ -27,7 +27,14 @@ struct FFTPlan {
     int tw_scale;                  // twiddle table length / n
     int lgNs[MITOS_MAX_STAGES];    // log2 of the combined length before stage s, -1 if not 2^k
     int twstep[MITOS_MAX_STAGES];  // n / (Ns R) * tw_scale: table stride of stage s
+    // the compile-time kernels' twiddles (the default schedule), stage by stage: for each stage
+    // s >= 1, Ns rows (jm < Ns) of w^(r jm n / (Ns R)), r = 1 .. R-1, each row tw_row(R) entries
+    // (16-byte aligned for vector loads); the same values as the table twN holds
+    const void *twst;
 };
+
+// entries of a stage's twiddle row (R - 1 used)
+__host__ __device__ constexpr int tw_row(int R) { return R - 1 <= 2 ? 2 : (R - 1 <= 4 ? 4 : 8); }
 
 // j / Ns and j % Ns, by shifts when Ns is a power of two
 __device__ __forceinline__ void divmod_ns(int j, int Ns, int lg, int &q, int &r) {
@@ -236,6 +243,12 @@ template <int NL, int E> struct CTSched {
     }
     static constexpr int first = radix_at(0);
     static constexpr int last = radix_at(nst - 1);
+    // offset (entries) of stage s's rows in the stage twiddle table
+    static constexpr int tw_off(int s) {
+        int o = 0;
+        for (int i = 1; i < s; i++) o += ns_before(i) * tw_row(radix_at(i));
+        return o;
+    }
 };
 
 // padded index of i + D from the padded index of i, when D is a multiple of 8 (or i + D stays
@@ -277,8 +290,7 @@ template <int NL, int E, int SN> __device__ __forceinline__ void pencil_sync() {
 template <typename T, int E, int SIGN, int NL, int SN, int S>
 struct CTStage {
     using Sch = CTSched<NL, E>;
-    static __device__ __forceinline__ void run(cplx<T> *v, cplx<T> *sm, int t, const cplx<T> *__restrict__ tw,
-                                               int tw_scale) {
+    static __device__ __forceinline__ void run(cplx<T> *v, cplx<T> *sm, int t, const cplx<T> *__restrict__ twst) {
         if constexpr (S < Sch::nst) {
             constexpr int Rp = Sch::radix_at(S - 1);
             constexpr int Nsp = Sch::ns_before(S - 1);
@@ -311,8 +323,22 @@ struct CTStage {
             for (int b = 0; b < E / R; b++) {
                 const int j = t + b * (NL / E);
                 const int jm = j % Ns;
-                const int step = jm * (NL / (Ns * R)) * tw_scale;
                 const int base = spad(j);
+                // the butterfly's R - 1 twiddles, one contiguous row: 16-byte vector loads
+                constexpr int TR = tw_row(R);
+                const cplx<T> *row = twst + Sch::tw_off(S) + jm * TR;
+                cplx<T> tws[TR];
+                if constexpr (sizeof(cplx<T>) == 8) {
+#pragma unroll
+                    for (int k = 0; k < TR / 2; k++) {
+                        const float4 q = __ldg(reinterpret_cast<const float4 *>(row) + k);
+                        tws[2 * k] = mk<T>(q.x, q.y);
+                        tws[2 * k + 1] = mk<T>(q.z, q.w);
+                    }
+                } else {
+#pragma unroll
+                    for (int k = 0; k < R - 1; k++) tws[k] = __ldg(row + k);
+                }
 #pragma unroll
                 for (int r = 0; r < R; r++) {
                     constexpr int D = NL / R;
@@ -320,7 +346,7 @@ struct CTStage {
                                   : ((D % 8) == 0) ? base + r * D + (r * D) / 8 : spad(j + r * D);
                     cplx<T> x = sm[o * SN];
                     if (r > 0) {
-                        cplx<T> w = __ldg(tw + r * step);
+                        cplx<T> w = tws[r - 1];
                         if (SIGN > 0) w.y = -w.y;
                         x = cmul<T>(x, w);
                     }
@@ -329,17 +355,17 @@ struct CTStage {
                 dft<T, R, SIGN>(v + b * R);
             }
             pencil_sync<NL, E, SN>();
-            CTStage<T, E, SIGN, NL, SN, S + 1>::run(v, sm, t, tw, tw_scale);
+            CTStage<T, E, SIGN, NL, SN, S + 1>::run(v, sm, t, twst);
         }
     }
 };
 
-// fft_regs with the length, the exchange stride SN and the schedule fixed at compile time
+// fft_regs with the length, the exchange stride SN and the schedule fixed at compile time; twst:
+// the plan's stage twiddle table (FFTPlan::twst)
 template <typename T, int E, int SIGN, int NL, int SN>
-__device__ __forceinline__ void fft_regs_ct(cplx<T> *v, cplx<T> *sm, int t, const cplx<T> *__restrict__ tw,
-                                            int tw_scale) {
+__device__ __forceinline__ void fft_regs_ct(cplx<T> *v, cplx<T> *sm, int t, const cplx<T> *__restrict__ twst) {
     stage_first<T, E, CTSched<NL, E>::first, SIGN>(v);
-    CTStage<T, E, SIGN, NL, SN, 1>::run(v, sm, t, tw, tw_scale);
+    CTStage<T, E, SIGN, NL, SN, 1>::run(v, sm, t, twst);
 }
 
 template <int NL, int E> __device__ __forceinline__ int n_in_ct(int t, int e) {
@@ -355,7 +381,7 @@ template <int NL, int E> __device__ __forceinline__ int n_out_ct(int t, int e) {
 template <typename T, int E, int SIGN, int NL, int SN>
 __device__ __forceinline__ void fft_any(const FFTPlan &pl, cplx<T> *v, cplx<T> *sm, int sn, int t,
                                         const cplx<T> *__restrict__ tw) {
-    if constexpr (NL > 0) fft_regs_ct<T, E, SIGN, NL, SN>(v, sm, t, tw, pl.tw_scale);
+    if constexpr (NL > 0) fft_regs_ct<T, E, SIGN, NL, SN>(v, sm, t, reinterpret_cast<const cplx<T> *>(pl.twst));
     else fft_regs<T, E, SIGN>(pl, v, sm, sn, t, tw);
 }
 template <int NL, int E> __device__ __forceinline__ int nin_any(const FFTPlan &pl, int t, int e) {
