@@ -40,6 +40,26 @@ template <typename T> __host__ __device__ __forceinline__ cplx<T> cmul_is(cplx<T
 template <typename T> __host__ __device__ __forceinline__ cplx<T> cconj(cplx<T> a) {
     return mk<T>(a.x, -a.y);
 }
+// FP32 complex add and subtract as one packed instruction on both lanes (sm_100 and later: the
+// FP32x2 add and fused multiply-add).  Each lane rounds as the scalar operation: a - b is
+// fma(b, -1, a), whose product is exact.
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000 && !defined(MITOS_NO_FP32X2)
+#define MITOS_FP32X2 1
+#endif
+template <> __host__ __device__ __forceinline__ float2 cadd<float>(float2 a, float2 b) {
+#ifdef MITOS_FP32X2
+    return __fadd2_rn(a, b);
+#else
+    return make_float2(a.x + b.x, a.y + b.y);
+#endif
+}
+template <> __host__ __device__ __forceinline__ float2 csub<float>(float2 a, float2 b) {
+#ifdef MITOS_FP32X2
+    return __ffma2_rn(b, make_float2(-1.f, -1.f), a);
+#else
+    return make_float2(a.x - b.x, a.y - b.y);
+#endif
+}
 
 // ---- error state ----------------------------------------------------------------------
 void set_error(int code, const char *fmt, ...);

@@ -59,13 +59,22 @@ template <typename T, int SIGN> __device__ __forceinline__ cplx<T> rot90(cplx<T>
     return SIGN < 0 ? mk<T>(a.y, -a.x) : mk<T>(-a.y, a.x);
 }
 
+// a + rot90(b) and a - rot90(b) lane by lane: the rotation swaps the lanes, so a packed pair
+// operation would first have to move them
+template <typename T, int SIGN> __device__ __forceinline__ cplx<T> add_rot(cplx<T> a, cplx<T> b) {
+    return SIGN < 0 ? mk<T>(a.x + b.y, a.y - b.x) : mk<T>(a.x - b.y, a.y + b.x);
+}
+template <typename T, int SIGN> __device__ __forceinline__ cplx<T> sub_rot(cplx<T> a, cplx<T> b) {
+    return SIGN < 0 ? mk<T>(a.x - b.y, a.y + b.x) : mk<T>(a.x + b.y, a.y - b.x);
+}
+
 template <typename T, int SIGN> __device__ __forceinline__ void dft4(cplx<T> *v) {
     cplx<T> a0 = cadd<T>(v[0], v[2]), a1 = csub<T>(v[0], v[2]);
-    cplx<T> b0 = cadd<T>(v[1], v[3]), b1 = rot90<T, SIGN>(csub<T>(v[1], v[3]));
+    cplx<T> b0 = cadd<T>(v[1], v[3]), d = csub<T>(v[1], v[3]);
     v[0] = cadd<T>(a0, b0);
     v[2] = csub<T>(a0, b0);
-    v[1] = cadd<T>(a1, b1);
-    v[3] = csub<T>(a1, b1);
+    v[1] = add_rot<T, SIGN>(a1, d);
+    v[3] = sub_rot<T, SIGN>(a1, d);
 }
 
 template <typename T, int SIGN> __device__ __forceinline__ void dft8(cplx<T> *v) {
@@ -76,14 +85,13 @@ template <typename T, int SIGN> __device__ __forceinline__ void dft8(cplx<T> *v)
     dft4<T, SIGN>(o);
     // w8^k = exp(SIGN 2 pi i k / 8)
     cplx<T> o1 = mk<T>((o[1].x - SIGN * o[1].y) * h, (o[1].y + SIGN * o[1].x) * h);
-    cplx<T> o2 = rot90<T, SIGN>(o[2]);  // w8^2 = SIGN i
     cplx<T> o3 = mk<T>((-o[3].x - SIGN * o[3].y) * h, (-o[3].y + SIGN * o[3].x) * h);
     v[0] = cadd<T>(e[0], o[0]);
     v[4] = csub<T>(e[0], o[0]);
     v[1] = cadd<T>(e[1], o1);
     v[5] = csub<T>(e[1], o1);
-    v[2] = cadd<T>(e[2], o2);
-    v[6] = csub<T>(e[2], o2);
+    v[2] = add_rot<T, SIGN>(e[2], o[2]);  // w8^2 = SIGN i
+    v[6] = sub_rot<T, SIGN>(e[2], o[2]);
     v[3] = cadd<T>(e[3], o3);
     v[7] = csub<T>(e[3], o3);
 }
