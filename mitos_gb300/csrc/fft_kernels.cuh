@@ -228,8 +228,9 @@ __global__ void __launch_bounds__(strided_threads<AXIS, OP, NL, PC, E>(), stride
 // forward FFT of the source spectrum, phi = (f1 phi1 - f2 S/k^2) / W_TSC, then the inverse
 // FFTs of phi and i kx phi (with the on-node stencil of the d_x chain when requested).
 // ------------------------------------------------------------------------------------------
+// (16 elements a thread: one block an SM, up to 128 registers)
 template <typename T, int E, int NL, int PC>
-__global__ void __launch_bounds__(512, 2) k_x_combine_disp(GridGeom g, PassArgs a, const T *__restrict__ win) {
+__global__ void __launch_bounds__(512, E > 12 ? 1 : 2) k_x_combine_disp(GridGeom g, PassArgs a, const T *__restrict__ win) {
     extern __shared__ __align__(16) unsigned char smraw[];
     cplx<T> *sm = reinterpret_cast<cplx<T> *>(smraw);
     const FFTPlan &pl = g.plN;
@@ -649,14 +650,41 @@ static int launch_strided_e(const GridGeom &g, const PassArgs &a, const T *win) 
     return 0;
 }
 
+// Elements a thread of the compile-time passes: 8 for 2^k, 12 for 3 2^k, and 16 for the 1024-point
+// Hessian and combine X passes.  Those keep the block's threads (512) with twice the pencils, eight
+// instead of four: 64-byte row segments, half the requests for each x-plane the block touches.
+template <int NL, int AXIS, int OP> constexpr int ct_elems() {
+    return NL % 3 == 0 ? 12 : (NL == 1024 && AXIS == 0 && (OP == XOP_HESS || OP == XOP_COMBINE_DISP)) ? 16 : 8;
+}
+// pencils a block for ct_elems (PC: the pencils of the length's default elements)
+template <int NL, int AXIS, int OP, int PC> constexpr int ct_pencils() {
+    return PC * ct_elems<NL, AXIS, OP>() / (NL % 3 == 0 ? 12 : 8);
+}
+
 template <typename T, int SIGN, int AXIS, int OP, int NL, int PC>
 static int launch_strided(const GridGeom &g, const PassArgs &a, const T *win) {
-    // the compile-time lengths: 8 elements a thread for 2^k, 12 for 3 2^k
-    if constexpr (NL > 0) return launch_strided_e<T, (NL % 3 == 0 ? 12 : 8), SIGN, AXIS, OP, NL, PC>(g, a, win);
+    if constexpr (NL > 0)
+        return launch_strided_e<T, ct_elems<NL, AXIS, OP>(), SIGN, AXIS, OP, NL, ct_pencils<NL, AXIS, OP, PC>()>(g, a, win);
     else {
         if (g.E == 8) return launch_strided_e<T, 8, SIGN, AXIS, OP, 0, 0>(g, a, win);
         return launch_strided_e<T, 12, SIGN, AXIS, OP, 0, 0>(g, a, win);
     }
+}
+
+template <typename T, int E, int NL, int PC>
+static int launch_combine_disp(const GridGeom &g, const PassArgs &a, const T *win) {
+    const int P = PC > 0 ? PC : g.P_xy;
+    const int threads = P * (g.N / E);
+    // the exchange buffer, then phi_1's elements of every thread
+    const size_t smem = (size_t)P * spad_len(g.N) * sizeof(cplx<T>) + (size_t)threads * E * sizeof(cplx<T>);
+    const long blocks = (g.plane + P - 1) / P;
+    launch_begin("x_combine_disp");
+    auto kern = k_x_combine_disp<T, E, NL, PC>;
+    if (smem > 48 * 1024) MITOS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<dim3((unsigned)blocks, a.batch > 1 ? a.batch : 1), threads, smem, stream()>>>(g, with_f32(a), win);
+    count_launch();
+    MITOS_LAUNCH_CHECK("x combine + displacement pass");
+    return 0;
 }
 
 // pencils per block of the multi-output Y passes of the compile-time lengths (256 threads)
@@ -675,26 +703,11 @@ int launch_x_t(const GridGeom &g, XOp op, int sign, const PassArgs &a) {
     case XOP_COMBINE_2LPT: return launch_strided<T, -1, 0, XOP_COMBINE_2LPT, NL, PC>(g, a, win);
     case XOP_ADD_POISSON: return launch_strided<T, -1, 0, XOP_ADD_POISSON, NL, PC>(g, a, win);
     case XOP_PK: return launch_strided<T, -1, 0, XOP_PK, NL, PC>(g, a, win);
-    case XOP_COMBINE_DISP: {
-        const int P = PC > 0 ? PC : g.P_xy;
-        const int threads = P * (g.N / g.E);
-        // the exchange buffer, then phi_1's elements of every thread
-        const size_t smem = (size_t)P * spad_len(g.N) * sizeof(cplx<T>) + (size_t)threads * g.E * sizeof(cplx<T>);
-        const long blocks = (g.plane + P - 1) / P;
-        launch_begin("x_combine_disp");
-        if (NL > 0 || g.E == 8) {
-            auto kern = k_x_combine_disp<T, (NL > 0 && NL % 3 == 0 ? 12 : 8), NL, PC>;
-            if (smem > 48 * 1024) MITOS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            kern<<<dim3((unsigned)blocks, a.batch > 1 ? a.batch : 1), threads, smem, stream()>>>(g, with_f32(a), win);
-        } else {
-            auto kern = k_x_combine_disp<T, 12, 0, 0>;
-            if (smem > 48 * 1024) MITOS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            kern<<<dim3((unsigned)blocks, a.batch > 1 ? a.batch : 1), threads, smem, stream()>>>(g, with_f32(a), win);
-        }
-        count_launch();
-        MITOS_LAUNCH_CHECK("x combine + displacement pass");
-        return 0;
-    }
+    case XOP_COMBINE_DISP:
+        if constexpr (NL > 0)
+            return launch_combine_disp<T, ct_elems<NL, 0, XOP_COMBINE_DISP>(), NL, ct_pencils<NL, 0, XOP_COMBINE_DISP, PC>()>(g, a, win);
+        else if (g.E == 8) return launch_combine_disp<T, 8, 0, 0>(g, a, win);
+        else return launch_combine_disp<T, 12, 0, 0>(g, a, win);
     }
     return 3;
 }
