@@ -154,9 +154,25 @@ template <typename T> __device__ __forceinline__ T fwrapT(T x, T L);
 template <> __device__ __forceinline__ float fwrapT<float>(float x, float L) { return fmodf(fmodf(x, L) + L, L); }
 template <> __device__ __forceinline__ double fwrapT<double>(double x, double L) { return fmod(fmod(x, L) + L, L); }
 
+// Grid coordinate x N / L of a position.  FP32: N / L as the unevaluated sum g + g_lo of two floats
+// and one FMA, so the coordinate is the exactly scaled position rounded once.  A rounded N / L (or
+// L / N) alone scales every coordinate by its relative rounding error (up to 6e-8): the particle
+// distribution stretched against the periodic grid, which moved the power of the box-scale modes
+// along the axes by up to 4e-4 (1024^3 and 256^3, L = 2000 Mpc/h).  FP64: the product (g_lo = 0).
+template <typename T> __device__ __forceinline__ T grid_coord(T p, T g, T g_lo) {
+    if constexpr (sizeof(T) == 4) return fmaf(p, g, p * g_lo);
+    else return p * g;
+}
+// host: N / L split for grid_coord (g_lo = 0 in FP64)
+template <typename T> static void grid_scale(int N, double boxlen, T &g, T &g_lo) {
+    const double s = N / boxlen;
+    g = (T)s;
+    g_lo = sizeof(T) == 4 ? (T)(s - (double)g) : (T)0;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256)
-k_displace_cic(int N, int M, float spacing, T boxlen, T gfac, T val,
+k_displace_cic(int N, int M, float spacing, T boxlen, T gfac, T g, T g_lo, T val,
                const T *__restrict__ d0, const T *__restrict__ d1, const T *__restrict__ d2,
                T *__restrict__ rho, float *__restrict__ pos_out, float *__restrict__ posraw_out) {
     const long np = (long)M * M * M;
@@ -170,9 +186,13 @@ k_displace_cic(int N, int M, float spacing, T boxlen, T gfac, T val,
     const T Nf = (T)N;
 #pragma unroll
     for (int dir = 0; dir < 3; dir++) {
-        // X = x N / boxlen (src/grids_interp.c:269-271)
-        const T disp = tsc_gather<T>(dd[dir], N, (T)p[0] * Nf / boxlen, (T)p[1] * Nf / boxlen,
-                                     (T)p[2] * Nf / boxlen);
+        // X = x N / boxlen (src/grids_interp.c:269-271); FP32 through grid_coord
+        T disp;
+        if constexpr (sizeof(T) == 4)
+            disp = tsc_gather<T>(dd[dir], N, grid_coord<T>(p[0], g, g_lo), grid_coord<T>(p[1], g, g_lo),
+                                 grid_coord<T>(p[2], g, g_lo));
+        else
+            disp = tsc_gather<T>(dd[dir], N, (T)p[0] * Nf / boxlen, (T)p[1] * Nf / boxlen, (T)p[2] * Nf / boxlen);
         p[dir] = (float)((T)p[dir] - disp);
     }
     if (posraw_out) {  // before the wrap: the velocity gather's positions (src/mitos.c:865-908)
@@ -188,8 +208,17 @@ k_displace_cic(int N, int M, float spacing, T boxlen, T gfac, T val,
         pos_out[3 * id + 1] = p[1];
         pos_out[3 * id + 2] = p[2];
     }
-    // CIC: X = x / (L / N) (analyse/src/mitos_read.c:288-333)
-    const T X = (T)p[0] / gfac, Y = (T)p[1] / gfac, Z = (T)p[2] / gfac;
+    // CIC: X = x / (L / N) (analyse/src/mitos_read.c:288-333); FP32 through grid_coord
+    T X, Y, Z;
+    if constexpr (sizeof(T) == 4) {
+        X = grid_coord<T>(p[0], g, g_lo);
+        Y = grid_coord<T>(p[1], g, g_lo);
+        Z = grid_coord<T>(p[2], g, g_lo);
+    } else {
+        X = (T)p[0] / gfac;
+        Y = (T)p[1] / gfac;
+        Z = (T)p[2] / gfac;
+    }
     const int iX = (int)dfloor<T>(X), iY = (int)dfloor<T>(Y), iZ = (int)dfloor<T>(Z);
     const T dx = X - iX, dy = Y - iY, dz = Z - iZ;
     const T tx = 1 - dx, ty = 1 - dy, tz = 1 - dz;
@@ -253,17 +282,17 @@ __device__ __forceinline__ void red_add_v4(float *p, float a, float b, float c, 
 // for the brick's shared tiles (rare); same arithmetic as the tiled path.  rpd: row pitch of
 // the displacement grids.
 template <typename T>
-__device__ __noinline__ void displace_global(int N, int rpd, T ginv, const T *d1, const T *d2, int y, int z,
-                                             float &p0, float &p1, float &p2) {
+__device__ __noinline__ void displace_global(int N, int rpd, T ginv, T ginv_lo, const T *d1, const T *d2, int y,
+                                             int z, float &p0, float &p1, float &p2) {
     const long yz = (long)y * rpd + z;
-    const T Xg = (T)p0 * ginv;
+    const T Xg = grid_coord<T>((T)p0, ginv, ginv_lo);
     const int nx = ifloor<T>(Xg + (T)0.5);
     T wx[3];
     tsc_w<T>(Xg - (T)nx, wx);
     long xo[3];
     for (int i = 0; i < 3; i++) xo[i] = (long)wrapn(nx - 1 + i, N) * N * rpd;
     p1 = (float)((T)p1 - (wx[0] * d1[xo[0] + yz] + wx[1] * d1[xo[1] + yz] + wx[2] * d1[xo[2] + yz]));
-    const T Yg = (T)p1 * ginv;
+    const T Yg = grid_coord<T>((T)p1, ginv, ginv_lo);
     const int ny = ifloor<T>(Yg + (T)0.5);
     T wy[3];
     tsc_w<T>(Yg - (T)ny, wy);
@@ -348,7 +377,7 @@ struct LatticeMaps {
 // thread, completing on the buffer's mbarrier; face bricks, whose halos wrap, by 16-byte cp.async.
 template <typename T>
 __global__ void __launch_bounds__(LB_THREADS, 2)
-k_lattice_cic(int N, int rpd, int rpo, float spacing, float Lf, T ginv, const T *__restrict__ d0, const T *__restrict__ d1,
+k_lattice_cic(int N, int rpd, int rpo, float spacing, float Lf, T ginv, T ginv_lo, const T *__restrict__ d0, const T *__restrict__ d1,
               const T *__restrict__ d2, T *__restrict__ rho, float *__restrict__ pos_out, size_t bstride, FastDiv div_bx,
               FastDiv div_by, float *__restrict__ posraw_out, const __grid_constant__ LatticeMaps maps, int use_tma,
               int region) {
@@ -468,7 +497,7 @@ k_lattice_cic(int N, int rpd, int rpo, float spacing, float Lf, T ginv, const T 
             // direction 0: on nodes (stencil folded into d0)
             p0 = (float)((T)p0 - t0[(lx * LB_Y + ly) * LB_Z + lz]);
             // direction 1: x off node (src/grids_interp.c:269-306), y and z on nodes (folded into d1)
-            const T Xg = (T)p0 * ginv;
+            const T Xg = grid_coord<T>((T)p0, ginv, ginv_lo);
             T fnx;
             const int nx = floor_split<T>(Xg + (T)0.5, fnx);
             const int ix = nx - 1 - (x0 - TH);  // tile x index of the first stencil node
@@ -479,7 +508,7 @@ k_lattice_cic(int N, int rpd, int rpo, float spacing, float Lf, T ginv, const T 
                 const T *r1 = t1 + (ix * LB_Y + ly) * LB_Z + lz;
                 p1 = (float)((T)p1 - (wx[0] * r1[0] + wx[1] * r1[LB_Y * LB_Z] + wx[2] * r1[2 * LB_Y * LB_Z]));
                 // direction 2: x and y off nodes, z on nodes (folded into d2)
-                const T Yg = (T)p1 * ginv;
+                const T Yg = grid_coord<T>((T)p1, ginv, ginv_lo);
                 T fny;
                 const int ny = floor_split<T>(Yg + (T)0.5, fny);
                 const int iy = ny - 1 - (y0 - TH);
@@ -499,7 +528,7 @@ k_lattice_cic(int N, int rpd, int rpo, float spacing, float Lf, T ginv, const T 
                 // restart the off-node gathers from global memory
                 p1 = y * spacing;
                 p2 = z * spacing;
-                displace_global<T>(N, rpd, ginv, d1, d2, y, z, p0, p1, p2);
+                displace_global<T>(N, rpd, ginv, ginv_lo, d1, d2, y, z, p0, p1, p2);
             }
             if (posraw_out) {  // before the wrap: the velocity gather's positions
                 const long id = ((long)x * N + y) * N + z;
@@ -517,7 +546,8 @@ k_lattice_cic(int N, int rpd, int rpo, float spacing, float Lf, T ginv, const T 
                 pos_out[3 * id + 2] = p2;
             }
             // CIC (analyse/src/mitos_read.c:288-333), one unit of mean density per particle (M = N)
-            const T X = (T)p0 * ginv, Y = (T)p1 * ginv, Z = (T)p2 * ginv;
+            const T X = grid_coord<T>((T)p0, ginv, ginv_lo), Y = grid_coord<T>((T)p1, ginv, ginv_lo),
+                    Z = grid_coord<T>((T)p2, ginv, ginv_lo);
             T fX, fY, fZ;
             const int iX = floor_split<T>(X, fX), iY = floor_split<T>(Y, fY), iZ = floor_split<T>(Z, fZ);
             const T dx = X - fX, dy = Y - fY, dz = Z - fZ;
@@ -607,7 +637,7 @@ void set_lattice_tma(bool on) { g_lattice_tma = on; }
 bool lattice_tma() { return g_lattice_tma; }
 
 template <typename T>
-static int lattice_launch(int N, int rpd, int rpo, float spacing, float Lf, double ginv, const void *d0, const void *d1,
+static int lattice_launch(int N, int rpd, int rpo, float spacing, float Lf, double boxlen, const void *d0, const void *d1,
                           const void *d2, void *rho, float *pos_out, int batch, size_t bstride, float *posraw_out) {
     static int blocks_per_sm[2] = {0, 0};  // per precision, for the current device
     static int sms = 0;
@@ -637,7 +667,9 @@ static int lattice_launch(int N, int rpd, int rpo, float spacing, float Lf, doub
     const int bxn = N / LB_X, byn = N / LB_Y, bzn = N / LB_Z;
     const int region = g_lattice_region && bxn % 8 == 0 && byn % 8 == 0 && bzn % 4 == 0;
     const FastDiv dx = make_fastdiv((unsigned)(region ? bxn / 8 : bxn)), dy = make_fastdiv((unsigned)(region ? byn / 8 : byn));
-    kern<<<dim3(blocks, nb), LB_THREADS, smem, stream()>>>(N, rpd, rpo, spacing, Lf, (T)ginv, (const T *)d0,
+    T g, g_lo;
+    grid_scale<T>(N, boxlen, g, g_lo);
+    kern<<<dim3(blocks, nb), LB_THREADS, smem, stream()>>>(N, rpd, rpo, spacing, Lf, g, g_lo, (const T *)d0,
                                                            (const T *)d1, (const T *)d2, (T *)rho, pos_out, bstride,
                                                            dx, dy, posraw_out, maps, use_tma, region);
     return 0;
@@ -654,9 +686,9 @@ int lattice_deposit(int N, double boxlen, int precision, const void *d0, const v
     const float spacing = Lf / N;  // src/particle.c:102-103 with M = N
     launch_begin("lattice_cic");
     const int e = precision == MITOS_FP32
-                      ? lattice_launch<float>(N, disp_pitch, rho_pitch, spacing, Lf, N / boxlen, d0, d1, d2, rho, pos_out,
+                      ? lattice_launch<float>(N, disp_pitch, rho_pitch, spacing, Lf, boxlen, d0, d1, d2, rho, pos_out,
                                               batch, bstride, posraw_out)
-                      : lattice_launch<double>(N, disp_pitch, rho_pitch, spacing, Lf, N / boxlen, d0, d1, d2, rho, pos_out,
+                      : lattice_launch<double>(N, disp_pitch, rho_pitch, spacing, Lf, boxlen, d0, d1, d2, rho, pos_out,
                                                batch, bstride, posraw_out);
     if (e) return e;
     count_launch();
@@ -670,10 +702,13 @@ bool lattice_aligned(int N, int M, double boxlen) {
     if (M != N || N % LB_Z || N % LB_Y || N % LB_X) return false;
     const float Lf = (float)boxlen;
     const float spacing = Lf / M;
+    float g, g_lo;
+    grid_scale<float>(N, boxlen, g, g_lo);
     for (int i = 0; i < M; i++) {
         const float x = i * spacing;
         if ((double)x * N / boxlen != (double)i) return false;
         if ((float)x * (float)N / Lf != (float)i) return false;
+        if (fmaf(x, g, x * g_lo) != (float)i) return false;  // grid_coord of the FP32 kernels
         if ((double)x / (boxlen / N) != (double)i) return false;
     }
     return true;
@@ -681,13 +716,22 @@ bool lattice_aligned(int N, int M, double boxlen) {
 
 // CIC of given positions (cic_deposit_dg)
 template <typename T>
-__global__ void k_cic(long n, int N, T gfac, T val, const float *__restrict__ pos, T *__restrict__ rho) {
+__global__ void k_cic(long n, int N, T L, T gfac, T g, T g_lo, T val, const float *__restrict__ pos, T *__restrict__ rho) {
     const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    // x = fwrap(x, L) in the working precision, X = x / (L / N) (analyse/src/mitos_read.c:284-290)
-    const T L = gfac * (T)N;
-    const T X = fwrapT<T>((T)pos[3 * i], L) / gfac, Y = fwrapT<T>((T)pos[3 * i + 1], L) / gfac,
-            Z = fwrapT<T>((T)pos[3 * i + 2], L) / gfac;
+    // x = fwrap(x, L) in the working precision, X = x / (L / N) (analyse/src/mitos_read.c:284-290);
+    // FP32 through grid_coord
+    const T px = fwrapT<T>((T)pos[3 * i], L), py = fwrapT<T>((T)pos[3 * i + 1], L), pz = fwrapT<T>((T)pos[3 * i + 2], L);
+    T X, Y, Z;
+    if constexpr (sizeof(T) == 4) {
+        X = grid_coord<T>(px, g, g_lo);
+        Y = grid_coord<T>(py, g, g_lo);
+        Z = grid_coord<T>(pz, g, g_lo);
+    } else {
+        X = px / gfac;
+        Y = py / gfac;
+        Z = pz / gfac;
+    }
     const int iX = (int)dfloor<T>(X), iY = (int)dfloor<T>(Y), iZ = (int)dfloor<T>(Z);
     const T dx = X - iX, dy = Y - iY, dz = Z - iZ;
     const T tx = 1 - dx, ty = 1 - dy, tz = 1 - dz;
@@ -714,14 +758,17 @@ int displace_and_deposit(int N, int M, double boxlen, int precision, const void 
     const double val = ((double)N * N * N) / ((double)M * M * M);
     const unsigned blocks = (unsigned)((np + 255) / 256);
     launch_begin("displace_cic");
-    if (precision == MITOS_FP32)
-        k_displace_cic<float><<<blocks, 256, 0, stream()>>>(N, M, spacing, (float)boxlen, (float)gfac, (float)val,
+    if (precision == MITOS_FP32) {
+        float g, g_lo;
+        grid_scale<float>(N, boxlen, g, g_lo);
+        k_displace_cic<float><<<blocks, 256, 0, stream()>>>(N, M, spacing, (float)boxlen, (float)gfac, g, g_lo, (float)val,
                                                             (const float *)d0, (const float *)d1, (const float *)d2,
                                                             (float *)rho, pos_out, posraw_out);
-    else
-        k_displace_cic<double><<<blocks, 256, 0, stream()>>>(N, M, spacing, boxlen, gfac, val, (const double *)d0,
+    } else {
+        k_displace_cic<double><<<blocks, 256, 0, stream()>>>(N, M, spacing, boxlen, gfac, 0.0, 0.0, val, (const double *)d0,
                                                              (const double *)d1, (const double *)d2, (double *)rho,
                                                              pos_out, posraw_out);
+    }
     count_launch();
     MITOS_LAUNCH_CHECK("displace + CIC");
     return 0;
@@ -987,10 +1034,13 @@ int cic_positions(long n, int N, double boxlen, int precision, const float *pos,
     const double gfac = boxlen / N;
     const unsigned blocks = (unsigned)((n + 255) / 256);
     launch_begin("cic");
-    if (precision == MITOS_FP32)
-        k_cic<float><<<blocks, 256, 0, stream()>>>(n, N, (float)gfac, (float)val, pos, (float *)rho);
-    else
-        k_cic<double><<<blocks, 256, 0, stream()>>>(n, N, gfac, val, pos, (double *)rho);
+    if (precision == MITOS_FP32) {
+        float g, g_lo;
+        grid_scale<float>(N, boxlen, g, g_lo);
+        k_cic<float><<<blocks, 256, 0, stream()>>>(n, N, (float)boxlen, (float)gfac, g, g_lo, (float)val, pos, (float *)rho);
+    } else {
+        k_cic<double><<<blocks, 256, 0, stream()>>>(n, N, boxlen, gfac, 0.0, 0.0, val, pos, (double *)rho);
+    }
     count_launch();
     MITOS_LAUNCH_CHECK("CIC");
     return 0;
