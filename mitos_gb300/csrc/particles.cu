@@ -282,17 +282,17 @@ __device__ __forceinline__ void red_add_v4(float *p, float a, float b, float c, 
 // for the brick's shared tiles (rare); same arithmetic as the tiled path.  rpd: row pitch of
 // the displacement grids.
 template <typename T>
-__device__ __noinline__ void displace_global(int N, int rpd, T ginv, T ginv_lo, const T *d1, const T *d2, int y,
-                                             int z, float &p0, float &p1, float &p2) {
+__device__ __noinline__ void displace_global(int N, int rpd, T ginv, const T *d1, const T *d2, int y, int z,
+                                             float &p0, float &p1, float &p2) {
     const long yz = (long)y * rpd + z;
-    const T Xg = grid_coord<T>((T)p0, ginv, ginv_lo);
+    const T Xg = (T)p0 * ginv;
     const int nx = ifloor<T>(Xg + (T)0.5);
     T wx[3];
     tsc_w<T>(Xg - (T)nx, wx);
     long xo[3];
     for (int i = 0; i < 3; i++) xo[i] = (long)wrapn(nx - 1 + i, N) * N * rpd;
     p1 = (float)((T)p1 - (wx[0] * d1[xo[0] + yz] + wx[1] * d1[xo[1] + yz] + wx[2] * d1[xo[2] + yz]));
-    const T Yg = grid_coord<T>((T)p1, ginv, ginv_lo);
+    const T Yg = (T)p1 * ginv;
     const int ny = ifloor<T>(Yg + (T)0.5);
     T wy[3];
     tsc_w<T>(Yg - (T)ny, wy);
@@ -496,8 +496,10 @@ k_lattice_cic(int N, int rpd, int rpo, float spacing, float Lf, T ginv, T ginv_l
                   p2 = small_int_to_float(z) * spacing;
             // direction 0: on nodes (stencil folded into d0)
             p0 = (float)((T)p0 - t0[(lx * LB_Y + ly) * LB_Z + lz]);
-            // direction 1: x off node (src/grids_interp.c:269-306), y and z on nodes (folded into d1)
-            const T Xg = grid_coord<T>((T)p0, ginv, ginv_lo);
+            // direction 1: x off node (src/grids_interp.c:269-306), y and z on nodes (folded into d1).
+            // (The stencil coordinates take the plain product: N / L's rounding shifts where the
+            // displacement is read by at most 6e-8 of the coordinate, far below a position's ulp.)
+            const T Xg = (T)p0 * ginv;
             T fnx;
             const int nx = floor_split<T>(Xg + (T)0.5, fnx);
             const int ix = nx - 1 - (x0 - TH);  // tile x index of the first stencil node
@@ -508,7 +510,7 @@ k_lattice_cic(int N, int rpd, int rpo, float spacing, float Lf, T ginv, T ginv_l
                 const T *r1 = t1 + (ix * LB_Y + ly) * LB_Z + lz;
                 p1 = (float)((T)p1 - (wx[0] * r1[0] + wx[1] * r1[LB_Y * LB_Z] + wx[2] * r1[2 * LB_Y * LB_Z]));
                 // direction 2: x and y off nodes, z on nodes (folded into d2)
-                const T Yg = grid_coord<T>((T)p1, ginv, ginv_lo);
+                const T Yg = (T)p1 * ginv;
                 T fny;
                 const int ny = floor_split<T>(Yg + (T)0.5, fny);
                 const int iy = ny - 1 - (y0 - TH);
@@ -528,7 +530,7 @@ k_lattice_cic(int N, int rpd, int rpo, float spacing, float Lf, T ginv, T ginv_l
                 // restart the off-node gathers from global memory
                 p1 = y * spacing;
                 p2 = z * spacing;
-                displace_global<T>(N, rpd, ginv, ginv_lo, d1, d2, y, z, p0, p1, p2);
+                displace_global<T>(N, rpd, ginv, d1, d2, y, z, p0, p1, p2);
             }
             if (posraw_out) {  // before the wrap: the velocity gather's positions
                 const long id = ((long)x * N + y) * N + z;
