@@ -36,7 +36,7 @@ template <int AXIS, int OP, int NL, int PC, int E> constexpr int strided_threads
 }
 template <int AXIS, int OP, int NL, int PC, int E> constexpr int strided_min_blocks() {
     return (NL > 0 && AXIS == 0 && OP == XOP_HESS) ? 1
-           : (NL > 0 && AXIS == 1 && (OP == YOP_DISP_A || OP == YOP_HESS_A || OP == YOP_HESS_B)) ? 3 : 2;
+           : (NL > 0 && AXIS == 1 && (OP == YOP_DISP_A || OP == YOP_HESS_A || OP == YOP_HESS_B)) ? (E > 12 ? 2 : 3) : 2;
 }
 
 template <typename T, int E, int SIGN, int AXIS, int OP, int NL, int PC>
@@ -651,10 +651,12 @@ static int launch_strided_e(const GridGeom &g, const PassArgs &a, const T *win) 
 }
 
 // Elements a thread of the compile-time passes: 8 for 2^k, 12 for 3 2^k, and 16 for the 1024-point
-// Hessian and combine X passes.  Those keep the block's threads (512) with twice the pencils, eight
-// instead of four: 64-byte row segments, half the requests for each x-plane the block touches.
+// Y passes and Hessian and combine X passes.  Those keep the block's threads with twice the pencils
+// (eight instead of four in 512 threads, four instead of two in the 256-thread multi-output Y
+// passes): row segments twice as long, half the requests for each plane the block touches.
 template <int NL, int AXIS, int OP> constexpr int ct_elems() {
-    return NL % 3 == 0 ? 12 : (NL == 1024 && AXIS == 0 && (OP == XOP_HESS || OP == XOP_COMBINE_DISP)) ? 16 : 8;
+    return NL % 3 == 0 ? 12
+           : (NL == 1024 && (AXIS == 1 || OP == XOP_HESS || OP == XOP_COMBINE_DISP)) ? 16 : 8;
 }
 // pencils a block for ct_elems (PC: the pencils of the length's default elements)
 template <int NL, int AXIS, int OP, int PC> constexpr int ct_pencils() {
