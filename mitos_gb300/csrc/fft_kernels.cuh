@@ -282,15 +282,16 @@ __global__ void __launch_bounds__(512, E > 12 ? 1 : 2) k_x_combine_disp(GridGeom
         psm[spad(n) * P] = o;
     }
     __syncthreads();
-    cplx<T> phi[E];
+    // phi to this thread's own slots of the staging area (phi_1 is consumed): both inverse
+    // transforms read it from there rather than keep E more values in registers
 #pragma unroll
-    for (int e = 0; e < E; e++) phi[e] = psm[spad(nin_any<NL, E>(pl, t, e)) * P];
+    for (int e = 0; e < E; e++) ph[e * blockDim.x] = psm[spad(nin_any<NL, E>(pl, t, e)) * P];
     __syncthreads();
 #pragma unroll 1
     for (int m = 0; m < 2; m++) {
 #pragma unroll
         for (int e = 0; e < E; e++) {
-            cplx<T> x = phi[e];
+            cplx<T> x = ph[e * blockDim.x];
             if (m == 1) {
                 const int jx = kint(nin_any<NL, E>(pl, t, e), N);
                 x = cmul_is<T>(x, (T)jx * dk);
