@@ -1,5 +1,5 @@
 // fft_ct1024.cu -- compile-time specialised FP32 FFT passes for N = 1024 (X / Y length 1024,
-// Z length 512; 4 pencils per X / Y block, 8 in the 16-element Hessian and combine X passes).
+// Z length 512; 4 pencils per X / Y block at 8 elements a thread, twice that at 16).
 #include "fft_kernels.cuh"
 
 namespace mitos {
