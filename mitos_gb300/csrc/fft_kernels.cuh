@@ -651,16 +651,18 @@ static int launch_strided_e(const GridGeom &g, const PassArgs &a, const T *win) 
     return 0;
 }
 
-// Elements a thread of the compile-time passes: 8 for 2^k, 12 for 3 2^k, and 16 for the 512- and
-// 1024-point Y passes and Hessian and P(k) X passes and the 1024-point combine X pass.  Those keep
+// Elements a thread of the compile-time passes: 8 for 2^k, 12 for 3 2^k, and 16 for the 256-, 512-
+// and 1024-point Y passes and Hessian and P(k) X passes and the 1024-point combine X pass.  Those keep
 // the block's threads with twice the pencils (sixteen or eight in 512 threads, eight or four in the
 // 256-thread multi-output Y passes): row segments twice as long, half the requests for each plane
 // the block touches.  At 512^3: y_hess_a 0.72 -> 0.55 ms, x_hess 0.71 -> 0.62, y_hess_b and
 // y_disp_a 0.44 -> 0.39, x_pk 0.43 -> 0.40, y_plain 0.25 -> 0.23; the 512-point combine pass stays
-// at 8 (0.75 against 0.86 ms: its phi_1 staging makes a 16-element block one an SM).
+// at 8 (0.75 against 0.86 ms: its phi_1 staging makes a 16-element block one an SM).  At 256^3
+// (where the rows are already 64 or 128 bytes) the IC 1.208 -> 1.187 ms, a Monge-Ampere solve
+// 2.758 -> 2.699 ms.
 template <int NL, int AXIS, int OP> constexpr int ct_elems() {
     return NL % 3 == 0 ? 12
-           : ((NL == 512 || NL == 1024) && (AXIS == 1 || OP == XOP_HESS || OP == XOP_PK)) ? 16
+           : ((NL == 256 || NL == 512 || NL == 1024) && (AXIS == 1 || OP == XOP_HESS || OP == XOP_PK)) ? 16
            : (NL == 1024 && OP == XOP_COMBINE_DISP) ? 16 : 8;
 }
 // pencils a block for ct_elems (PC: the pencils of the length's default elements)
