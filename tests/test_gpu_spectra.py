@@ -42,7 +42,10 @@ def test_bispectrum_fp64_vs_oracle(N, btype, vol, bins3):
                             theta=4 * np.pi / 3, k3=0.4)
     full = ref["B"] != 0
     assert full.sum() >= 3
-    assert np.array_equal(got["B"] == 0, ~full)  # the same empty bins
+    assert np.all(got["B"][~full] == 0)  # the same empty bins
+    # a filled bin may sum to exactly zero in the GPU's summation order only at the cancellation
+    # scale (the atomic order varies from run to run)
+    assert np.all(np.abs(ref["B"][full & (got["B"] == 0)]) < 1e-9 * np.abs(ref["B"]).max())
     for key in ("k1", "k2", "k3"):
         assert np.allclose(got[key], ref[key], rtol=1e-13, atol=0), key
     # the sums run in another order: cancellation sets the scale of the difference
