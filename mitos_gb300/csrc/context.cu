@@ -475,6 +475,34 @@ int bin_geometry(int N, int bins, int linear, double boxlen, const double **ksum
     return 0;
 }
 
+// ---- the Z passes' row-copy fault word ---------------------------------------------------
+static int *g_zrow_fault_host = nullptr, *g_zrow_fault_dev = nullptr;
+int *zrow_fault_device() {
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!g_zrow_fault_host) {
+        int *hp = nullptr, *dp = nullptr;
+        if (cudaHostAlloc((void **)&hp, sizeof(int), cudaHostAllocMapped) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        if (cudaHostGetDevicePointer((void **)&dp, hp, 0) != cudaSuccess) {
+            cudaGetLastError();
+            cudaFreeHost(hp);
+            return nullptr;
+        }
+        *hp = 0;
+        g_zrow_fault_host = hp;
+        g_zrow_fault_dev = dp;
+    }
+    return g_zrow_fault_dev;
+}
+int zrow_fault_check() {
+    if (!g_zrow_fault_host || !*(volatile int *)g_zrow_fault_host) return 0;
+    *g_zrow_fault_host = 0;
+    set_error(6, "a Z pass's row copy did not complete (bounded wait timed out; rows read from global memory)");
+    return 6;
+}
+
 // ---- workspace: grid-sized device buffers reused across calls --------------------------
 static std::map<std::pair<size_t, int>, std::vector<void *>> g_ws;
 void *workspace(size_t bytes, int slot) {

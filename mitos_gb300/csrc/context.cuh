@@ -19,6 +19,10 @@ int bin_n2_range(int N, int bins, int linear, double boxlen, int b, long *lo, lo
 int bin_geometry(int N, int bins, int linear, double boxlen, const double **ksum, const long long **count);
 // grid-sized scratch buffer number `slot` of `bytes` bytes (kept until mitos_release_all)
 void *workspace(size_t bytes, int slot);
+// the Z passes' row-copy fault word: its device address (a mapped pinned host int), and the
+// host-side check, status 6 when set (call after the library stream has synchronised)
+int *zrow_fault_device();
+int zrow_fault_check();
 // FFT tiles of one grid size: pencils per block of the X / Y passes and rows per block of the Z
 // passes (the autotuner's knobs); returns 1 when the tile does not fit the kernels' limits
 int set_tiles(int N, int precision, int p_xy, int p_z);

@@ -4,6 +4,7 @@
 #pragma once
 
 #include "context.cuh"
+#include "tma.cuh"
 
 namespace mitos {
 
@@ -374,10 +375,54 @@ __global__ void __launch_bounds__(256, (OP == ZOP_HESS_MA || OP == ZOP_HESS_MA_K
     cplx<T> o[NKEEP][E];
     cplx<T> acc[E];
     T *dst_row = nullptr;
+    auto field = [&](int q) {
+        return S2 ? (q == 0 ? 0 : q == 1 ? 3 : q == 2 ? 5 : q == 3 ? 1 : q == 4 ? 4 : 2)
+                  : LEAN ? (q == 0 ? 0 : q == 1 ? 3 : q == 2 ? 5 : q == 3 ? 4 : q == 4 ? 1 : 2) : q;
+    };
+    // Input rows of the lean Monge-Ampere residual pass (FP32, compile-time lengths with one pencil
+    // a warp or half a warp): the pencil's first lane copies each row into one of the pencil's two row buffers
+    // with a bulk copy (cp.async.bulk) completing on the buffer's mbarrier, two rows ahead, so the
+    // global reads run while the rows before transform, and the lanes read X[k] and X[h - k] from
+    // shared memory.  A row is copied from the 16-byte boundary below it to the one above its end
+    // (its own bytes and at most 8 of each neighbour's: inside the grid, whose size is a multiple
+    // of 16).  A wait that times out (bounded) flags a.fault and the pencil's warp reads the rest
+    // from global memory.  (At 256^3 the pass takes 0.316 against 0.323 ms, its spills 64 bytes a
+    // thread against 380.  The 2LPT-source and displacement passes ran slower this way at 512^3:
+    // 1.49 against 1.25 ms and 0.81 against 0.66; they read their rows from global memory.)
+    constexpr bool ZT = sizeof(T) == 4 && LEAN && NL > 0 && (NL / E == 32 || NL / E == 16);
+    const int zrb = ((H * (int)sizeof(cplx<T>) + 8 + 15) / 16) * 16;  // bytes a row buffer
+    unsigned char *zb0 = nullptr;
+    uint64_t *zbar = nullptr;
+    bool zok = true;              // warp-uniform: the row buffers are in use
+    unsigned zph = 0, zpend = 0;  // per buffer: parity of its next completion, a copy in flight
+    auto zissue = [&](int q, int b) {  // the pencil's first lane: row of input q into buffer b
+        const uintptr_t s = reinterpret_cast<uintptr_t>(bat<const cplx<T>>(a.in[field(q)], bo) + row * H);
+        const uintptr_t s0 = s & ~(uintptr_t)15;
+        const uintptr_t s1 = (s + (uintptr_t)H * sizeof(cplx<T>) + 15) & ~(uintptr_t)15;
+        fence_proxy_async();  // the lanes' reads of the buffer before the copy's writes
+        mbar_expect_tx(zbar + b, (unsigned)(s1 - s0));
+        bulk_load_g2s(zb0 + b * zrb, reinterpret_cast<const void *>(s0), (unsigned)(s1 - s0), zbar + b);
+    };
+    if constexpr (ZT) {
+        const int pb = (int)blockDim.x / tpp;  // pencils a block
+        unsigned char *zbase = smraw + (((size_t)pb * spad_len(h) * sizeof(cplx<T>) + 15) & ~(size_t)15);
+        zb0 = zbase + (size_t)p * 2 * zrb;
+        zbar = reinterpret_cast<uint64_t *>(zbase + (size_t)pb * 2 * zrb) + 2 * p;
+        if (t == 0) {
+            mbar_init(zbar, 1);
+            mbar_init(zbar + 1, 1);
+            mbar_init_fence();
+        }
+        __syncwarp();
+        if (t == 0) {
+            zissue(0, 0);
+            zissue(1, 1);
+        }
+        zpend = 3;
+    }
 #pragma unroll
     for (int q = 0; q < NIN; q++) {
-        const int f = S2 ? (q == 0 ? 0 : q == 1 ? 3 : q == 2 ? 5 : q == 3 ? 1 : q == 4 ? 4 : 2)
-                      : LEAN ? (q == 0 ? 0 : q == 1 ? 3 : q == 2 ? 5 : q == 3 ? 4 : q == 4 ? 1 : 2) : q;
+        const int f = field(q);
         // kz factor of input f: 0 -> 1, 1 -> i kz, 2 -> -kz^2
         int fac = 0;
         if (S2 || MA) fac = (f == 2 || f == 4) ? 1 : (f == 5 ? 2 : 0);
@@ -393,11 +438,27 @@ __global__ void __launch_bounds__(256, (OP == ZOP_HESS_MA || OP == ZOP_HESS_MA_K
                 for (int sct = t; sct < nsec; sct += tpp) prefetch_l2(nxt + 32 * sct);
             }
         }
+        const cplx<T> *rs = src;  // where this row's X[k] and X[h - k] are read
+        if constexpr (ZT) {
+            const int b = q & 1;
+            if (zok) {
+                const bool got = __all_sync(0xffffffffu, mbar_wait(zbar + b, (zph >> b) & 1u));
+                if (got) {
+                    zph ^= 1u << b;
+                    zpend &= ~(1u << b);
+                    const uintptr_t sa = reinterpret_cast<uintptr_t>(src);
+                    rs = reinterpret_cast<const cplx<T> *>(zb0 + b * zrb) + ((sa & 15) ? 1 : 0);
+                } else {
+                    zok = false;
+                    if (t == 0 && a.fault) atomicExch(a.fault, 1);
+                }
+            }
+        }
         cplx<T> v[E];
 #pragma unroll
         for (int e = 0; e < E; e++) {
             const int k = nin_any<NL, E>(pl, t, e);
-            cplx<T> X = src[k], Y = src[h - k];
+            cplx<T> X = rs[k], Y = rs[h - k];
             if (fac != 0) {
                 const T k1 = (T)k * dk, k2 = (T)(h - k) * dk;
                 if (fac == 1) { X = cmul_is<T>(X, k1); Y = cmul_is<T>(Y, k2); }
@@ -414,6 +475,14 @@ __global__ void __launch_bounds__(256, (OP == ZOP_HESS_MA || OP == ZOP_HESS_MA_K
             const cplx<T> D = mk<T>(X.x - Y.x, X.y + Y.y);
             const cplx<T> Op = mk<T>(D.x * w.x + D.y * w.y, D.y * w.x - D.x * w.y);
             v[e] = mk<T>(Ep.x - Op.y, Ep.y + Op.x);
+        }
+        if constexpr (ZT) {
+            // every lane has read buffer q & 1: it takes row q + 2
+            if (zok && q + 2 < NIN) {
+                __syncwarp();
+                if (t == 0) zissue(q + 2, q & 1);
+                zpend |= 1u << (q & 1);
+            }
         }
         fft_any<T, E, 1, NL, 1>(pl, v, psm, 1, t, tw);
         if constexpr (OP == ZOP_C2R || OP == ZOP_DISP) {
@@ -452,6 +521,14 @@ __global__ void __launch_bounds__(256, (OP == ZOP_HESS_MA || OP == ZOP_HESS_MA_K
         }
     }
     (void)dst_row;
+    if constexpr (ZT) {
+        // after a timed-out wait: the copies still in flight land (bounded) before the block's
+        // shared memory is released
+        if (!zok) {
+            for (int b = 0; b < 2; b++)
+                if ((zpend >> b) & 1u) mbar_wait(zbar + b, (zph >> b) & 1u);
+        }
+    }
     if constexpr (OP == ZOP_HESS_2LPT_K) {
         // the r2c of the S row, as k_z_r2c does it from global memory: the row to the transform's
         // input order through the row's exchange buffer, the N/2-point forward FFT, the split into
@@ -741,14 +818,23 @@ static int launch_zc_e(const GridGeom &g, const PassArgs &a) {
     const int tpp = h / E;
     int P = g.P_z;
     const int threads = P * tpp;
-    const size_t smem = (size_t)P * spad_len(h) * sizeof(cplx<T>);
+    size_t smem = (size_t)P * spad_len(h) * sizeof(cplx<T>);
+    // the lean Monge-Ampere residual pass (FP32, compile-time lengths with one pencil a warp or half
+    // a warp): two row buffers and two mbarriers a pencil behind the exchange buffer (k_z_c2r)
+    constexpr bool ZT = sizeof(T) == 4 && OP == ZOP_HESS_MA_K && NLZ > 0 && (NLZ / E == 32 || NLZ / E == 16);
+    PassArgs b = with_f32(a);
+    if constexpr (ZT) {
+        const size_t zrb = ((g.H * sizeof(cplx<T>) + 8 + 15) / 16) * 16;
+        smem = ((smem + 15) & ~(size_t)15) + (size_t)P * 2 * zrb + (size_t)P * 2 * sizeof(uint64_t);
+        if (!b.fault) b.fault = zrow_fault_device();
+    }
     const long rows = (long)g.N * g.N;
     auto kern = k_z_c2r<T, E, OP, NLZ>;
     if (smem > 48 * 1024) MITOS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     launch_begin(OP == ZOP_C2R ? "z_c2r" : OP == ZOP_HESS_2LPT ? "z_hess_2lpt" : OP == ZOP_HESS_2LPT_K ? "z_hess_2lpt_r2c"
                  : OP == ZOP_HESS_MA ? "z_hess_ma" : OP == ZOP_HESS_MA_K ? "z_hess_ma_r2c"
                  : OP == ZOP_HESS_MA_KS ? "z_hess_ma_r2c_s" : "z_disp");
-    kern<<<dim3((unsigned)((rows + P - 1) / P), a.batch > 1 ? a.batch : 1), threads, smem, stream()>>>(g, with_f32(a));
+    kern<<<dim3((unsigned)((rows + P - 1) / P), a.batch > 1 ? a.batch : 1), threads, smem, stream()>>>(g, b);
     count_launch();
     MITOS_LAUNCH_CHECK("z c2r pass");
     return 0;

@@ -89,6 +89,9 @@ struct PassArgs {
     // FP32 copies of scale, dk, f1, f2, rho_a, rho_b, filled at launch (with_f32): the FP32
     // kernels read these, as a double -> float conversion per thread runs on the FP64 pipe
     float fscale, fdk, ff1, ff2, frho_a, frho_b;
+    // mapped host word a Z pass sets when one of its row copies never completed (bounded wait;
+    // the pass then reads the rows from global memory); filled at launch
+    int *fault;
 };
 
 // the kernel's copy of a with the FP32 scalars filled

@@ -33,6 +33,14 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, i
         : "memory");
 }
 
+// untiled bulk copy of `bytes` (a multiple of 16) from global src to shared dst (both 16-byte
+// aligned), completing on bar
+__device__ __forceinline__ void bulk_load_g2s(void *dst, const void *src, unsigned bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
 // wait for the phase of the given parity to complete, at most about 2^22 polls (a suspended poll
 // plus a short sleep each: well under a few seconds); false if it never did
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
