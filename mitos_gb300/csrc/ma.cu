@@ -249,6 +249,7 @@ static int ma_run(struct distributed_grid *pot, struct distributed_grid *dens, s
         double h[2];
         MITOS_CUDA(cudaMemcpyAsync(h, red, sizeof h, cudaMemcpyDeviceToHost, stream()));
         MITOS_CUDA(cudaStreamSynchronize(stream()));
+        if ((e = zrow_fault_check())) break;
         const double rel = sqrt(h[0] / h[1]);
         st->evaluations++;
         st->rel = rel;

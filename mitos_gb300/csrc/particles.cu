@@ -619,6 +619,8 @@ int lattice_fault_fetch() {
     return 0;
 }
 int lattice_fault_check() {
+    // the Z passes' row copies too (their word is written by the kernels themselves)
+    if (const int z = zrow_fault_check()) return z;
     if (!g_fault_host || !*g_fault_host) return 0;
     *g_fault_host = 0;
     const int zero = 0;
