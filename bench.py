@@ -39,10 +39,11 @@ UNIT = "IC/s"
 
 
 def algorithmic_bytes(name: str, G: float) -> float:
-    """minimum bytes a launch of each kernel must move, in units of one complex grid G (the IC's
-    noise launch writes the noise and clears the deposit's density grid: 2 G)"""
-    table = {"noise": 2, "x_hess": 4, "y_hess": 9, "y_hess_a": 4, "y_hess_b": 3, "y_disp_a": 3, "y_stn": 2, "z_hess_2lpt": 7,
-             "z_hess_2lpt_r2c": 7, "z_hess_ma": 8, "z_hess_ma_r2c": 8, "z_r2c": 2,
+    """minimum bytes a launch of each kernel must move, in units of one complex grid G (in the 2LPT
+    IC the 2LPT-source Z pass also clears the deposit's density grid: 7 + 1 G; the noise launch
+    writes the noise, 1 G)"""
+    table = {"noise": 1, "x_hess": 4, "y_hess": 9, "y_hess_a": 4, "y_hess_b": 3, "y_disp_a": 3, "y_stn": 2, "z_hess_2lpt": 7,
+             "z_hess_2lpt_r2c": 8, "z_hess_ma": 8, "z_hess_ma_r2c": 8, "z_r2c": 2,
              "y_plain": 2, "x_plain": 2, "x_combine": 3, "x_add_poisson": 3, "x_disp": 3,
              "y_disp": 5, "z_disp": 6, "displace_cic": 4, "x_pk": 1, "z_c2r": 2,
              "lattice_cic": 4, "x_combine_disp": 4, "filter": 0}

@@ -92,7 +92,7 @@ int grid_r2c(const GridGeom &g, int prec, double boxlen, const void *box, int rp
 // ZOP_HESS_2LPT writes the second-order source, ZOP_HESS_MA the Monge-Ampere residual
 int grid_hessian(const GridGeom &g, int prec, double boxlen, const void *phi, int zop,
                  const void *rho, void *out, double *red, int window_order, void *out2, int batch,
-                 size_t bstride) {
+                 size_t bstride, void *zero, size_t zero_bytes) {
     // batched (batch > 1): every grid holds batch realisations bstride bytes apart
     const size_t gb = batch > 1 ? (size_t)batch * bstride : (size_t)g.cells * csize(prec);
     void *A[3], *B[6];
@@ -138,6 +138,10 @@ int grid_hessian(const GridGeom &g, int prec, double boxlen, const void *phi, in
     a.rp_in = g.N + 2;
     a.rp_out = g.N + 2;
     a.scale = 1.0 / (boxlen * boxlen * boxlen);
+    if (zop == ZOP_HESS_2LPT_K) {
+        a.zero = zero;
+        a.zero_bytes = zero_bytes;
+    }
     return prec == MITOS_FP32 ? launch_z_c2r<float>(g, (ZOp)zop, a) : launch_z_c2r<double>(g, (ZOp)zop, a);
 }
 

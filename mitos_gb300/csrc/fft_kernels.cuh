@@ -547,6 +547,15 @@ __global__ void __launch_bounds__(256, (OP == ZOP_HESS_MA || OP == ZOP_HESS_MA_K
         for (int e = 0; e < E; e++) psm[xpos<NL, 1>(nout_any<NL, E>(pl, t, e))] = v[e];
         if constexpr (NL > 0) pencil_sync<NL, E, 1>();
         else __syncthreads();
+        if (a.zero) {
+            // this block's slice of the region to clear (the deposit's density grid; under 2^31
+            // 16-byte words), streaming stores
+            const unsigned n16 = (unsigned)(a.zero_bytes / 16), nb = gridDim.x * gridDim.y;
+            const unsigned per = (n16 + nb - 1) / nb, b0 = (blockIdx.y * gridDim.x + blockIdx.x) * per;
+            const unsigned b1 = min(b0 + per, n16);
+            uint4 *z = reinterpret_cast<uint4 *>(a.zero);
+            for (unsigned i = b0 + threadIdx.x; i < b1; i += blockDim.x) __stcs(z + i, make_uint4(0u, 0u, 0u, 0u));
+        }
         if (!valid) return;
         cplx<T> *dst = bat<cplx<T>>(a.out[0], bo) + row * H;
         for (int k = t; k <= h; k += tpp) {

@@ -92,6 +92,10 @@ struct PassArgs {
     // mapped host word a Z pass sets when one of its row copies never completed (bounded wait;
     // the pass then reads the rows from global memory); filled at launch
     int *fault;
+    // a region the 2LPT-source Z pass zeroes on the side with streaming stores (16-byte aligned,
+    // zero_bytes a multiple of 16; its blocks take consecutive slices): the deposit's density grid
+    void *zero;
+    size_t zero_bytes;
 };
 
 // the kernel's copy of a with the FP32 scalars filled

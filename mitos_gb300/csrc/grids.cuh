@@ -14,8 +14,10 @@ int grid_r2c(const GridGeom &g, int prec, double boxlen, const void *box, int rp
 // six Hessian components of phi (k space) through the fused X / Y / Z passes into out (real);
 // ZOP_HESS_2LPT writes the second-order source, ZOP_HESS_MA the Monge-Ampere residual (and, when
 // out2 is given, the second-order source too)
+// (zero / zero_bytes: a region the 2LPT-source Z pass clears on the side)
 int grid_hessian(const GridGeom &g, int prec, double boxlen, const void *phi, int zop, const void *rho, void *out,
-                 double *red, int window_order, void *out2 = nullptr, int batch = 1, size_t bstride = 0);
+                 double *red, int window_order, void *out2 = nullptr, int batch = 1, size_t bstride = 0,
+                 void *zero = nullptr, size_t zero_bytes = 0);
 int axpby(int prec, long n, double a, const void *x, double b, const void *y, void *out);
 inline size_t csize(int prec) { return prec == MITOS_FP32 ? 8 : 16; }
 

@@ -282,13 +282,15 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     seed_state(cfg->seed, st);
     int e;
     void *dens_k = ma ? Sk : phi;  // Monge-Ampere keeps delta(k) to build rho(x)
-    // the lattice-aligned deposit's density grid (row pitch N + 4), cleared by the noise kernel
+    // the lattice-aligned deposit's density grid (row pitch N + 4), cleared on the side by the
+    // 2LPT-source Z pass (latency-bound, with HBM bandwidth to spare) or else by the noise kernel
     const int rho_pitch = aligned ? N + 4 : N + 2;
     const size_t rho_bytes = B > 1 ? db : (size_t)N * N * rho_pitch * (sizeof(T));
     void *rhoA = aligned ? workspace(rho_bytes, 15) : nullptr;
     if (aligned && !rhoA) return 5;
-    e = noise_generate(g, prec, L, st, filt, dens_k, B > 1 ? opt->states : nullptr, B, bs, rhoA,
-                       aligned ? rho_bytes : 0);
+    const bool clear_in_z = aligned && cfg->method == MITOS_METHOD_2LPT;
+    e = noise_generate(g, prec, L, st, filt, dens_k, B > 1 ? opt->states : nullptr, B, bs,
+                       clear_in_z ? nullptr : rhoA, aligned && !clear_in_z ? rho_bytes : 0);
     if (!e) e = hermitian_planes(g, prec, dens_k, B, bs);
     if (e) return e;
     tim.mark();
@@ -300,7 +302,8 @@ static int run_pipeline(const struct ic_config *cfg, const double *ktab, const d
     double last_rel = 0;
     if (cfg->method == MITOS_METHOD_2LPT) {
         // S2: Hessians + source, and the source's r2c along z in the same Z pass
-        e = grid_hessian(g, prec, L, phi, ZOP_HESS_2LPT_K, nullptr, Sk, nullptr, 0, nullptr, B, bs);
+        e = grid_hessian(g, prec, L, phi, ZOP_HESS_2LPT_K, nullptr, Sk, nullptr, 0, nullptr, B, bs,
+                         clear_in_z ? rhoA : nullptr, clear_in_z ? rho_bytes : 0);
         if (e) return e;
         tim.mark();
         // S3: the rest of the S r2c -> phi = f1 phi1 + f2 (-1/k^2) S, TSC window undone
