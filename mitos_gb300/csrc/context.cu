@@ -101,6 +101,7 @@ bool plan_from_radices(int n, int E, int tw_len, const int *rad, int ns, FFTPlan
     pl->nst = ns;
     pl->tw_scale = tw_len / n;
     pl->twst = nullptr;
+    pl->twst16 = nullptr;
     int Ns = 1;
     for (int i = 0; i < ns; i++) {
         pl->rad[i] = rad[i];
@@ -142,6 +143,7 @@ struct GeomEntry {
     GridGeom g;
     void *tw = nullptr;
     void *twst[2] = {nullptr, nullptr};  // the stage twiddle tables of plN and plH
+    void *twst16 = nullptr;              // plN's for the 16-element schedule
 };
 
 // the stage table of a plan (FFTPlan::twst) from the double twiddle table tw (length N, of the
@@ -225,6 +227,18 @@ const GridGeom *geom(int N, int precision) {
     g.twN = ge->tw;
     ge->twst[0] = stage_twiddles(g.plN, tw, precision);
     ge->twst[1] = stage_twiddles(g.plH, tw, precision);
+    {
+        // the 16-element compile-time kernels' schedule (ct_radix_at), where it exists for N
+        FFTPlan p16 = g.plN;
+        p16.nst = 0;
+        while (p16.nst < MITOS_MAX_STAGES && ct_radix_at(N, 16, p16.nst)) {
+            p16.rad[p16.nst] = ct_radix_at(N, 16, p16.nst);
+            p16.nst++;
+        }
+        int prod = 1;
+        for (int s = 0; s < p16.nst; s++) prod *= p16.rad[s];
+        ge->twst16 = prod == N ? stage_twiddles(p16, tw, precision) : nullptr;
+    }
     if (!ge->twst[0] || !ge->twst[1]) {
         cudaGetLastError();
         delete ge;
@@ -233,6 +247,8 @@ const GridGeom *geom(int N, int precision) {
     }
     g.plN.twst = ge->twst[0];
     g.plH.twst = ge->twst[1];
+    g.plN.twst16 = ge->twst16;
+    g.plH.twst16 = nullptr;
     g_geoms[key] = ge;
     return &ge->g;
 }
@@ -280,6 +296,8 @@ int set_radix(int N, int precision, const int *rad_n, int ns_n, const int *rad_h
     // the stage tables belong to the default schedules, the only ones the compile-time kernels run
     pn.twst = g->plN.twst;
     ph.twst = g->plH.twst;
+    pn.twst16 = g->plN.twst16;
+    ph.twst16 = g->plH.twst16;
     g->plN = pn;
     g->plH = ph;
     g->custom_radix = !(same(pn, dn) && same(ph, dh));

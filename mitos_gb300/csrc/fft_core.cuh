@@ -29,12 +29,32 @@ struct FFTPlan {
     int twstep[MITOS_MAX_STAGES];  // n / (Ns R) * tw_scale: table stride of stage s
     // the compile-time kernels' twiddles (the default schedule), stage by stage: for each stage
     // s >= 1, Ns rows (jm < Ns) of w^(r jm n / (Ns R)), r = 1 .. R-1, each row tw_row(R) entries
-    // (16-byte aligned for vector loads); the same values as the table twN holds
+    // (16-byte aligned for vector loads); the same values as the table twN holds.  twst16: the
+    // same for the schedule of the 16-element compile-time kernels (ct_radix_at(n, 16, s))
     const void *twst;
+    const void *twst16;
 };
 
 // entries of a stage's twiddle row (R - 1 used)
-__host__ __device__ constexpr int tw_row(int R) { return R - 1 <= 2 ? 2 : (R - 1 <= 4 ? 4 : 8); }
+__host__ __device__ constexpr int tw_row(int R) { return R - 1 <= 2 ? 2 : (R - 1 <= 4 ? 4 : (R - 1 <= 8 ? 8 : 16)); }
+
+// Radix of stage s of the compile-time schedule of length NL at E elements a thread (0 past the
+// last stage): 8s, 4s, 2s, 3s, after 16s for the 256-point 16-element kernels ([16, 16]: one
+// exchange instead of two; 256^3 IC 1.191 -> 1.151 ms, Monge-Ampere solve 2.645 -> 2.544 ms).  At
+// 512 ([16, 16, 2] against [8, 8, 8]) the IC took 8.01 -> 8.14 ms and at 1024 ([16, 16, 4]) 74.15 ->
+// 73.92, so those keep 8s.
+__host__ __device__ constexpr bool ct_r16(int NL) { return NL == 256; }
+__host__ __device__ constexpr int ct_radix_at(int NL, int E, int s) {
+    int rem = NL, idx = 0;
+    if (E % 16 == 0 && ct_r16(NL))
+        while (rem % 16 == 0) { if (idx == s) return 16; rem /= 16; idx++; }
+    if (E % 8 == 0)
+        while (rem % 8 == 0) { if (idx == s) return 8; rem /= 8; idx++; }
+    while (E % 4 == 0 && rem % 4 == 0) { if (idx == s) return 4; rem /= 4; idx++; }
+    while (E % 2 == 0 && rem % 2 == 0) { if (idx == s) return 2; rem /= 2; idx++; }
+    while (E % 3 == 0 && rem % 3 == 0) { if (idx == s) return 3; rem /= 3; idx++; }
+    return 0;
+}
 
 // j / Ns and j % Ns, by shifts when Ns is a power of two
 __device__ __forceinline__ void divmod_ns(int j, int Ns, int lg, int &q, int &r) {
@@ -108,11 +128,43 @@ template <typename T, int SIGN> __device__ __forceinline__ void dft3(cplx<T> *v)
     v[2] = mk<T>(m.x + s * t2.y, m.y - s * t2.x);
 }
 
+// 16-point DFT as 4 x 4 (n = 4 n1 + n2, k = k1 + 4 k2): DFT4s over n1 for each n2, the twiddles
+// w16^(n2 k1) with w16 = exp(SIGN 2 pi i / 16), DFT4s over n2 for each k1; natural order in and out
+template <typename T, int SIGN> __device__ __forceinline__ void dft16(cplx<T> *v) {
+    const T c1 = (T)0.92387953251128675613, s1 = (T)0.38268343236508977173, h = (T)0.70710678118654752440;
+    const T S = (T)SIGN;
+    cplx<T> y[16];  // y[4 n2 + k1]
+#pragma unroll
+    for (int n2 = 0; n2 < 4; n2++) {
+        cplx<T> q[4] = {v[n2], v[4 + n2], v[8 + n2], v[12 + n2]};
+        dft4<T, SIGN>(q);
+#pragma unroll
+        for (int k1 = 0; k1 < 4; k1++) y[4 * n2 + k1] = q[k1];
+    }
+    y[5] = cmul<T>(y[5], mk<T>(c1, S * s1));     // w^1
+    y[6] = cmul<T>(y[6], mk<T>(h, S * h));       // w^2
+    y[7] = cmul<T>(y[7], mk<T>(s1, S * c1));     // w^3
+    y[9] = cmul<T>(y[9], mk<T>(h, S * h));       // w^2
+    y[10] = rot90<T, SIGN>(y[10]);               // w^4 = SIGN i
+    y[11] = cmul<T>(y[11], mk<T>(-h, S * h));    // w^6
+    y[13] = cmul<T>(y[13], mk<T>(s1, S * c1));   // w^3
+    y[14] = cmul<T>(y[14], mk<T>(-h, S * h));    // w^6
+    y[15] = cmul<T>(y[15], mk<T>(-c1, -S * s1)); // w^9
+#pragma unroll
+    for (int k1 = 0; k1 < 4; k1++) {
+        cplx<T> q[4] = {y[k1], y[4 + k1], y[8 + k1], y[12 + k1]};
+        dft4<T, SIGN>(q);
+#pragma unroll
+        for (int k2 = 0; k2 < 4; k2++) v[k1 + 4 * k2] = q[k2];
+    }
+}
+
 template <typename T, int R, int SIGN> __device__ __forceinline__ void dft(cplx<T> *v) {
     if constexpr (R == 2) dft2<T, SIGN>(v[0], v[1]);
     else if constexpr (R == 3) dft3<T, SIGN>(v);
     else if constexpr (R == 4) dft4<T, SIGN>(v);
     else if constexpr (R == 8) dft8<T, SIGN>(v);
+    else if constexpr (R == 16) dft16<T, SIGN>(v);
 }
 
 // padded shared-memory index of element n (one pad slot every 8) to spread bank accesses
@@ -229,15 +281,7 @@ __device__ __forceinline__ int n_out(const FFTPlan &pl, int E, int t, int e) {
 // Same schedule and stage arithmetic as fft_regs with every length, radix and stride a
 // constant, so shared-memory offsets and index splits fold away.
 template <int NL, int E> struct CTSched {
-    static constexpr int radix_at(int s) {
-        int rem = NL, idx = 0;
-        if (E % 8 == 0)
-            while (rem % 8 == 0) { if (idx == s) return 8; rem /= 8; idx++; }
-        while (E % 4 == 0 && rem % 4 == 0) { if (idx == s) return 4; rem /= 4; idx++; }
-        while (E % 2 == 0 && rem % 2 == 0) { if (idx == s) return 2; rem /= 2; idx++; }
-        while (E % 3 == 0 && rem % 3 == 0) { if (idx == s) return 3; rem /= 3; idx++; }
-        return 0;
-    }
+    static constexpr int radix_at(int s) { return ct_radix_at(NL, E, s); }
     static constexpr int count() {
         int n = 0;
         while (radix_at(n)) n++;
@@ -389,7 +433,8 @@ template <int NL, int E> __device__ __forceinline__ int n_out_ct(int t, int e) {
 template <typename T, int E, int SIGN, int NL, int SN>
 __device__ __forceinline__ void fft_any(const FFTPlan &pl, cplx<T> *v, cplx<T> *sm, int sn, int t,
                                         const cplx<T> *__restrict__ tw) {
-    if constexpr (NL > 0) fft_regs_ct<T, E, SIGN, NL, SN>(v, sm, t, reinterpret_cast<const cplx<T> *>(pl.twst));
+    if constexpr (NL > 0)
+        fft_regs_ct<T, E, SIGN, NL, SN>(v, sm, t, reinterpret_cast<const cplx<T> *>(E == 16 ? pl.twst16 : pl.twst));
     else fft_regs<T, E, SIGN>(pl, v, sm, sn, t, tw);
 }
 template <int NL, int E> __device__ __forceinline__ int nin_any(const FFTPlan &pl, int t, int e) {
